@@ -1,0 +1,157 @@
+/*
+ * rkdg_gpu.h — C ABI of the GB300 (sm_103a) RKDG hot path.
+ *
+ * This is the drop-in boundary for the reference's explicit DG right-hand
+ * side, limiter and Runge-Kutta stage loop.  Every entry point takes plain
+ * pointers and sizes; state vectors are DEVICE pointers unless a name says
+ * "host".  State layout is the reference's (MFEM Ordering::byNODES, main.cpp:
+ * 119-141): x[k*NDofs + e*nd + i] for equation k, element e, node i, i.e.
+ * structure-of-arrays by variable, element-contiguous inside a variable.
+ *
+ * Every call returns an rkdg_status.  A context owns one CUDA stream, all
+ * device tables and all scratch buffers.  A context is not thread-safe;
+ * distinct contexts are independent.  There are no process globals: the
+ * physics constants the reference keeps in globals (main.cpp:39-56) live in
+ * the context.
+ */
+#ifndef RKDG_GPU_H
+#define RKDG_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rkdg_ctx rkdg_ctx;
+
+typedef enum {
+  RKDG_OK = 0,
+  RKDG_ERR_INVALID = 1,      /* bad argument or call order */
+  RKDG_ERR_UNPHYSICAL = 2,   /* a Riemann solver saw a non-physical state; the
+                                reference exits here (face_integrator.cpp:214-218) */
+  RKDG_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+  RKDG_ERR_NOMESH = 4,       /* no mesh uploaded */
+  RKDG_ERR_TIMEOUT = 5,      /* a bounded device wait gave up */
+  RKDG_ERR_UNSUPPORTED = 6,  /* element type / order / geometry not supported */
+  RKDG_ERR_ALLOC = 7,        /* device allocation failed */
+  RKDG_ERR_NOT_FOUND = 8     /* the CUDA extension or a device is missing */
+} rkdg_status;
+
+/* Geometry codes follow MFEM's Geometry::Type numbering. */
+enum { RKDG_GEOM_TRIANGLE = 2, RKDG_GEOM_SQUARE = 3, RKDG_GEOM_CUBE = 5 };
+enum { RKDG_RS_RUSANOV = 0, RKDG_RS_LLF = 1, RKDG_RS_HLL = 2, RKDG_RS_HLLC = 3 };
+enum { RKDG_AVG_TRRS = 0, RKDG_AVG_EINFELDT = 1 };
+enum {
+  RKDG_BC_SLIP = 0,             /* boundary_integrator_slip.cpp:7-17 */
+  RKDG_BC_OPEN = 1,             /* "outlet", boundary_integrator_open.cpp:9-12 */
+  RKDG_BC_FIXED_ROTATED = 2,    /* BoundaryIntegratorConstant, boundary_integrator_constant.cpp:8-20 */
+  RKDG_BC_SUPERSONIC_INLET = 3, /* boundary_integrator_supersonic_inlet.cpp:8-19 */
+  RKDG_BC_WALL = 4              /* boundary_integrator_wall.cpp:7-17 (same as slip) */
+};
+enum { RKDG_LIM_FINDIFF = 0, RKDG_LIM_MULTI = 1 };
+enum { RKDG_IND_NOWHERE = 0, RKDG_IND_EVERYWHERE = 1, RKDG_IND_BJ = 2 };
+enum { RKDG_FUN_BJ = 0, RKDG_FUN_VENKATAKRISHNAN = 1, RKDG_FUN_MICHALAK = 2 };
+/* quirk flags of rkdg_set_limiter: 0 reproduces the shipped reference. */
+enum { RKDG_QUIRK_MULTIPLIER_ONCE = 1 };
+enum { RKDG_FP64 = 0, RKDG_FP32_BULK = 1 };
+
+/* Mesh as the host (MFEM) sees it after every adapt.  elem_vertices are
+ * topological vertex ids in MFEM local order (periodic meshes share ids
+ * across the periodic seam); elem_coords are each element's own corner
+ * coordinates in the same order; boundary faces carry 1-based attributes. */
+typedef struct {
+  int dim;                   /* 2 or 3 */
+  int geom;                  /* RKDG_GEOM_* */
+  int order;                 /* polynomial order p of DG_FECollection(p, dim) */
+  int num_elements;
+  const int* elem_vertices;  /* [num_elements][verts per element] */
+  const double* elem_coords; /* [num_elements][verts per element][dim] */
+  int num_bdr;
+  const int* bdr_vertices;   /* [num_bdr][verts per face] */
+  const int* bdr_attr;       /* [num_bdr] */
+} rkdg_mesh_desc;
+
+/* ---- context ---------------------------------------------------------- */
+int rkdg_create(rkdg_ctx** out, int device);
+int rkdg_destroy(rkdg_ctx* ctx);
+/* Message and offending element / face id of the last error. */
+const char* rkdg_last_error(rkdg_ctx* ctx, long long* where);
+/* Use an external cudaStream_t (NULL = the context's own stream). */
+int rkdg_set_stream(rkdg_ctx* ctx, void* cuda_stream);
+int rkdg_synchronize(rkdg_ctx* ctx);
+
+/* ---- setup -------------------------------------------------------------
+ * Replaces the RiemannSolver factory (case_manager.cpp:523-543) and the
+ * physics globals (case_manager.cpp:84-101). */
+int rkdg_set_physics(rkdg_ctx* ctx, int rsolver, int averaging, double gamma,
+                     double covolume, double gas_constant);
+/* Replaces FE_Evolution::UpdateInverseMassMatrix / UpdateAfluxPointer
+ * (fe_evolution.hpp:78-81) and the integrator set-up of main.cpp:148-164:
+ * builds every device face / element / stencil table.  Idempotent; call it
+ * after every AMR adapt (main.cpp:610-611). */
+int rkdg_upload_mesh(rkdg_ctx* ctx, const rkdg_mesh_desc* mesh);
+/* Replaces CaseManager::addBoundaryIntegrators (case_manager.cpp:614-820)
+ * for one boundary attribute.  state: conservative variables or NULL. */
+int rkdg_set_bc(rkdg_ctx* ctx, int attr, int type, const double* state);
+/* Replaces CaseManager::loadLimiter (case_manager.cpp:545-612). */
+int rkdg_set_limiter(rkdg_ctx* ctx, int limiter, int indicator, int function,
+                     int last_hope, int quirk_flags);
+/* Replaces the ExplicitRKLimitedSolver constructor arguments
+ * (rk_explicit_limited.hpp:46-48, tableaux case_manager.cpp:822-895):
+ * MFEM lower-triangular packing a[s*(s-1)/2], b[s], c[s-1].  1 <= s <= 4. */
+int rkdg_set_tableau(rkdg_ctx* ctx, int s, const double* a, const double* b,
+                     const double* c);
+int rkdg_set_precision(rkdg_ctx* ctx, int precision);
+
+/* ---- queries ------------------------------------------------------------ */
+/* NDofs (scalar nodes), nodes per element, number of equations. */
+int rkdg_sizes(rkdg_ctx* ctx, long long* ndofs, int* nd, int* neq);
+/* Physical node coordinates (host buffer [dim][NDofs]) for nodal projection
+ * of initial conditions (GridFunction::ProjectCoefficient on nodal L2). */
+int rkdg_node_coords_host(rkdg_ctx* ctx, double* out);
+/* h_min = min over elements of Mesh::GetElementSize(i, 1) (main.cpp:191-201) */
+int rkdg_hmin(rkdg_ctx* ctx, double* hmin);
+
+/* ---- hot path ----------------------------------------------------------- */
+/* FE_Evolution::Mult (fe_evolution.hpp:75, fe_evolution.cpp:102-216):
+ * y = M^-1 [(F(u), grad phi) - <Fhat.n, phi>], x and y device arrays of
+ * length NDofs*neq.  *max_char_speed_out (host) receives the global
+ * max_char_speed the reference leaves in main.cpp:50. */
+int rkdg_rhs(rkdg_ctx* ctx, const double* x_dev, double* y_dev,
+             double* max_char_speed_out);
+/* A.Mult only (face and boundary terms), the initial-dt evaluation of
+ * main.cpp:473-483: returns the face-only max characteristic speed. */
+int rkdg_face_speed(rkdg_ctx* ctx, const double* x_dev, double* max_char_speed_out);
+/* Limiter::update (limiter.hpp:111, limiter.cpp:22-94), in place. */
+int rkdg_limit(rkdg_ctx* ctx, double* x_dev);
+/* Averager::computeMeanValues (averager.cpp:84-109): means[k*NE + e]. */
+int rkdg_cell_means(rkdg_ctx* ctx, const double* x_dev, double* means_dev);
+/* ExplicitRKLimitedSolver::Step (rk_explicit_limited.cpp:30-82): all stages,
+ * limiter after every stage and after the combination.  Does not advance t
+ * (as the reference).  *next_mcs (host, may be NULL) = max_char_speed of the
+ * last stage, which the reference turns into the next dt (main.cpp:538-547). */
+int rkdg_step(rkdg_ctx* ctx, double* x_dev, double dt, double* next_mcs);
+/* The time loop of main.cpp:467-553,701-733.
+ * dt_mode 0: dynamic CFL dt; 1: dt from CFL once at t=0, then constant;
+ * 2: constant dt0.  max_steps > 0 stops early.  Outputs (host, may be NULL):
+ * steps taken, t as the reference books it (t += new dt), last dt, and the
+ * physical time actually integrated (sum of dt_real). */
+int rkdg_run(rkdg_ctx* ctx, double* x_dev, double t_end, double cfl, double dt0,
+             int dt_mode, int max_steps, int* steps_out, double* t_out,
+             double* dt_out, double* sum_dt_out);
+/* Discretely conserved totals sum_e sum_j (int phi_j) u_j per equation
+ * (host output [neq]); the device form of check_total_energy.cpp:3-62. */
+int rkdg_totals(rkdg_ctx* ctx, const double* x_dev, double* totals_host);
+/* Pointwise Riemann solver (test hook for RiemannSolver::Eval,
+ * rs_basic.hpp:49-50): device arrays u1,u2 [n][neq], nor [n][dim] (unit),
+ * flux [n][neq], speed [n] (-1 where the reference returns -1). */
+int rkdg_riemann_batch(rkdg_ctx* ctx, int n, const double* u1, const double* u2,
+                       const double* nor, double* flux, double* speed);
+/* Number of kernels this context launched since creation (instrumentation). */
+long long rkdg_kernel_launches(rkdg_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

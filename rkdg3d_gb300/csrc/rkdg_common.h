@@ -1,0 +1,125 @@
+// Shared host/device declarations of the GB300 RKDG library: reference-element
+// tables, device mesh tables and kernel parameter blocks.
+#pragma once
+
+#include <cstdint>
+
+#define RKDG_MAX_ND 27    // hex Q2 = 27 nodes
+#define RKDG_MAX_NFPE 6
+#define RKDG_MAX_NQF 16   // hex Q2 face rule: 4x4
+#define RKDG_MAX_NQL 4    // limiter face rule (order 2): 2 (segment) or 2x2
+#define RKDG_MAX_NV 8
+#define RKDG_MAX_PERM 64
+#define RKDG_MAX_BC 32
+
+namespace rkdg {
+
+// Element traits: compile-time sizes of the supported (geometry, order) pairs.
+// Face rules follow the reference's DGTraceIntegrator order (face_integrator.cpp
+// :45-58): OrderW + 2p, +1 on simplices; OrderW = 0 (triangle), 1 (bilinear
+// quad), 2 (trilinear hex); a segment rule of order q has q/2+1 GL points.
+template <int G, int P>
+struct El;
+template <int P>
+struct El<2, P> {  // triangle
+  static constexpr int DIM = 2, ND = (P + 1) * (P + 2) / 2, NFPE = 3, NQF = P + 1, NQL = 2,
+                       NV = 3, NEQ = 4;
+};
+template <int P>
+struct El<3, P> {  // quadrilateral
+  static constexpr int DIM = 2, ND = (P + 1) * (P + 1), NFPE = 4, NQF = P + 1, NQL = 2, NV = 4,
+                       NEQ = 4;
+};
+template <int P>
+struct El<5, P> {  // hexahedron
+  static constexpr int DIM = 3, ND = (P + 1) * (P + 1) * (P + 1), NFPE = 6,
+                       NQF = (P + 2) * (P + 2), NQL = 4, NV = 8, NEQ = 5;
+};
+
+// Reference-element tables (built on the host in FP64, copied to the device).
+struct RefTables {
+  int dim, geom, p, nd, nfpe, nqf, nql, nv, nperm, n1, nq1;
+  double D[3][RKDG_MAX_ND][RKDG_MAX_ND];     // D[r][j][m] = sum_q w phi_m d_r phi_j
+  double Minv[RKDG_MAX_ND][RKDG_MAX_ND];     // reference inverse mass
+  double B[RKDG_MAX_NFPE][RKDG_MAX_NQF][RKDG_MAX_ND];   // traces at face points
+  double wf[RKDG_MAX_NQF];                   // face rule weights
+  int perm[RKDG_MAX_PERM][RKDG_MAX_NQF];     // elem1 point -> elem2 point
+  double Bl[RKDG_MAX_NFPE][RKDG_MAX_NQL][RKDG_MAX_ND];  // limiter face points
+  double Bv[RKDG_MAX_NV][RKDG_MAX_ND];       // element vertices
+  double wmean[RKDG_MAX_ND];                 // cell-mean weights (sum = 1)
+  // 1D tables for the sum-factorised tensor kernels
+  double l1d[RKDG_MAX_NQF][8];   // 1D basis at 1D face-rule points  [a][j]
+  double w1d[8];                 // 1D face-rule weights
+  double lend[2][8];             // 1D basis at 0 and 1
+  double d1[8][8];               // d1[j][m] = w_m l_j'(x_m) (collocated volume)
+  double minv1[8][8];            // 1D reference inverse mass (exact)
+  double lquad[2][8];            // 1D basis at the 2 limiter GL points
+};
+
+// Boundary condition slot.
+struct BCSlot {
+  int type;
+  double state[5];
+};
+
+// Per-element face table entry codes (fcode): bits 0-2 local face of the
+// other element, bit 3 = 1 if this element is the face's Elem2, bits 4..
+// permutation id.  fnbr: neighbour element id, -1 = boundary face with no
+// boundary integrator, <= -2 : boundary condition slot (-2 - fnbr).
+struct RhsParams {
+  int ne;
+  long long ndofs;
+  const int* fnbr;      // [nfpe][ne]
+  const int* fcode;     // [nfpe][ne]
+  const void* fgeo;     // [nfpe][dim+1][ne] elem1-outward unit normal, |J_f|
+  const void* egeo;     // [dim*dim+1][ne]   adj(J) (row r, col d), 1/det J
+  const RefTables* tab;
+  double gamma, covolume;
+  int rs, avg;
+  int faces_only;       // 1: face terms only (A.Mult for the initial dt)
+  BCSlot bc[RKDG_MAX_BC];
+  unsigned long long* mcs;  // atomicMax target, bits of a non-negative double
+  int* err;                 // [0] status (first writer wins), [1] element
+};
+
+// Stage epilogue.
+// mode 0: write the plain right-hand side y = k (FP64) to out64.
+// mode 1: Runge-Kutta combination  out = base + sum_j cprev[j] kprev[j] + ccur k.
+//   FP64 path: base/out64 are double; out32 optionally receives a float copy.
+//   FP32-bulk path: the conserved state is a float pair (hi, lo) (basehi,
+//   baselo); an intermediate stage writes its combination as float to out32
+//   (the next stage input), the final stage (final_stage = 1) updates (hi, lo)
+//   in double-single arithmetic (out32 = hi, outlo = lo).
+// kout (optional) stores k itself for later stages; means (optional) receives
+// the FP64 cell means of the result [neq][ne].
+template <typename R>
+struct EpiParams {
+  int mode;
+  int final_stage;
+  int nprev;
+  double* out64;
+  float* out32;
+  float* outlo;
+  R* kout;
+  const double* base;
+  const float* basehi;
+  const float* baselo;
+  const R* kprev[3];
+  double cprev[3];
+  float cprev_hi[3], cprev_lo[3];
+  double ccur;
+  float ccur_hi, ccur_lo;
+  double* means;
+};
+
+struct LimParams {
+  int ne;
+  long long ndofs;
+  const int* fnbr;
+  const RefTables* tab;
+  const double* means;  // [neq][ne]
+  double gamma, covolume;
+  int limiter, indicator, function, last_hope, quirks;
+};
+
+}  // namespace rkdg

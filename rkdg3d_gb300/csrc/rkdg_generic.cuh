@@ -1,0 +1,488 @@
+// Generic (dense reference-operator) element kernels: one thread per element.
+//
+// Used for every supported (geometry, order) pair; hexahedra additionally
+// have sum-factorised kernels (rkdg_hex.cuh).  Reference operators live in
+// shared memory, converted to the arithmetic type R.  The right-hand side of
+// one element is the reference's FE_Evolution::Mult restricted to that
+// element (fe_evolution.cpp:102-216): every face of the element computes the
+// numerical flux at the face points with the arguments ordered (Elem1,
+// Elem2, Elem1-outward normal) exactly as FaceIntegrator::AssembleFaceVector
+// (face_integrator.cpp:11-276), so the two elements of a face obtain
+// bit-identical fluxes and the scheme stays conservative to round-off
+// without atomics.
+#pragma once
+
+#include "rkdg_common.h"
+#include "rkdg_physics.cuh"
+
+namespace rkdg {
+
+// ---- double-single (float pair) helpers for the FP32-bulk path --------------
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void ds_add(float& hi, float& lo, float bh, float bl) {
+  float s, e;
+  two_sum(hi, bh, s, e);
+  e += lo + bl;
+  hi = s + e;
+  lo = e - (hi - s);
+}
+// (ch, cl) * k as a float pair
+__device__ __forceinline__ void ds_mul_f(float ch, float cl, float k, float& ph, float& pl) {
+  ph = ch * k;
+  pl = fmaf(ch, k, -ph) + cl * k;
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
+  if (!(v > 0.0)) return;
+  atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// Block-wide max of a per-thread wave speed, committed with one atomicMax per
+// block (the MPI_Allreduce(MAX) of main.cpp:543 on one device).
+template <typename R>
+__device__ __forceinline__ void block_max_commit(R v, unsigned long long* dst) {
+  double vd = (double)v;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) vd = fmax(vd, __shfl_xor_sync(0xffffffffu, vd, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ double redd[32];
+  if (lane == 0) redd[w] = vd;
+  __syncthreads();
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    double x = lane < nw ? redd[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (lane == 0) atomic_max_nonneg(dst, x);
+  }
+}
+
+__device__ __forceinline__ void flag_error(int* err, int code, int where) {
+  if (atomicCAS(&err[0], 0, code) == 0) err[1] = where;
+}
+
+// Epilogue for one element and one equation: y[i], i < ND.
+template <int ND, typename R>
+__device__ __forceinline__ void epilogue(const EpiParams<R>& ep, long long base_idx,
+                                         const R* y, const R* wmean, int ne, int e, int k) {
+  if (ep.mode == 0) {
+#pragma unroll
+    for (int i = 0; i < ND; ++i) ep.out64[base_idx + i] = (double)y[i];
+    return;
+  }
+  if constexpr (std::is_same<R, double>::value) {
+    double m = 0.0;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      const long long idx = base_idx + i;
+      double v = ep.base ? ep.base[idx] : 0.0;
+      for (int j = 0; j < ep.nprev; ++j) v += ep.cprev[j] * ep.kprev[j][idx];
+      v += ep.ccur * y[i];
+      if (ep.kout) ep.kout[idx] = y[i];
+      if (ep.out64) ep.out64[idx] = v;
+      if (ep.out32) ep.out32[idx] = (float)v;
+      m += wmean[i] * v;
+    }
+    if (ep.means) ep.means[(long long)k * ne + e] = m;
+  } else {
+    float mh = 0.0f, ml = 0.0f;
+    if (!ep.final_stage) {
+#pragma unroll
+      for (int i = 0; i < ND; ++i) {
+        const long long idx = base_idx + i;
+        float inc = ep.baselo[idx];
+        for (int j = 0; j < ep.nprev; ++j) inc = fmaf(ep.cprev_hi[j], ep.kprev[j][idx], inc);
+        inc = fmaf(ep.ccur_hi, y[i], inc);
+        const float v = ep.basehi[idx] + inc;
+        if (ep.kout) ep.kout[idx] = y[i];
+        ep.out32[idx] = v;
+        float ph, pl;
+        ds_mul_f(wmean[i], 0.0f, v, ph, pl);
+        ds_add(mh, ml, ph, pl);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < ND; ++i) {
+        const long long idx = base_idx + i;
+        float sh = 0.0f, sl = 0.0f, ph, pl;
+        for (int j = 0; j < ep.nprev; ++j) {
+          ds_mul_f(ep.cprev_hi[j], ep.cprev_lo[j], ep.kprev[j][idx], ph, pl);
+          ds_add(sh, sl, ph, pl);
+        }
+        ds_mul_f(ep.ccur_hi, ep.ccur_lo, y[i], ph, pl);
+        ds_add(sh, sl, ph, pl);
+        float h = ep.basehi[idx], l = ep.baselo[idx];
+        ds_add(h, l, sh, sl);
+        ep.out32[idx] = h;
+        ep.outlo[idx] = l;
+        ds_mul_f(wmean[i], 0.0f, h, ph, pl);
+        ds_add(mh, ml, ph, pl);
+        ds_add(mh, ml, wmean[i] * l, 0.0f);
+      }
+    }
+    if (ep.means) ep.means[(long long)k * ne + e] = (double)mh + (double)ml;
+  }
+}
+
+// ---- right-hand side --------------------------------------------------------
+template <int G, int P, typename R>
+__global__ void __launch_bounds__(128)
+    k_rhs_generic(const RhsParams prm, const R* __restrict__ u, const EpiParams<R> ep) {
+  using E = El<G, P>;
+  constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NFPE = E::NFPE, NQF = E::NQF;
+  __shared__ R sB[NFPE][NQF][ND];
+  __shared__ R sD[DIM][ND][ND];
+  __shared__ R sMinv[ND][ND];
+  __shared__ R sW[NQF];
+  __shared__ R sWm[ND];
+  __shared__ unsigned char sPerm[RKDG_MAX_PERM][NQF];
+  const RefTables* T = prm.tab;
+  for (int t = threadIdx.x; t < NFPE * NQF * ND; t += blockDim.x) {
+    const int s = t % ND, q = (t / ND) % NQF, lf = t / (ND * NQF);
+    sB[lf][q][s] = (R)T->B[lf][q][s];
+  }
+  for (int t = threadIdx.x; t < DIM * ND * ND; t += blockDim.x) {
+    const int m = t % ND, j = (t / ND) % ND, r = t / (ND * ND);
+    sD[r][j][m] = (R)T->D[r][j][m];
+  }
+  for (int t = threadIdx.x; t < ND * ND; t += blockDim.x) sMinv[t / ND][t % ND] = (R)T->Minv[t / ND][t % ND];
+  for (int t = threadIdx.x; t < NQF; t += blockDim.x) sW[t] = (R)T->wf[t];
+  for (int t = threadIdx.x; t < ND; t += blockDim.x) sWm[t] = (R)T->wmean[t];
+  for (int t = threadIdx.x; t < RKDG_MAX_PERM * NQF; t += blockDim.x)
+    sPerm[t / NQF][t % NQF] = (unsigned char)T->perm[t / NQF][t % NQF];
+  __syncthreads();
+
+  const int ne = prm.ne;
+  const long long NDa = prm.ndofs;
+  const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  R lmax = R(0);
+  if (e < ne) {
+    R acc[NEQ][ND];
+#pragma unroll
+    for (int k = 0; k < NEQ; ++k)
+#pragma unroll
+      for (int s = 0; s < ND; ++s) acc[k][s] = R(0);
+    const R* fg = (const R*)prm.fgeo;
+    for (int lf = 0; lf < NFPE; ++lf) {
+      const int nb = prm.fnbr[lf * ne + e];
+      if (nb == -1) continue;
+      const int code = prm.fcode[lf * ne + e];
+      R n[DIM];
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) n[c] = fg[(long long)(lf * (DIM + 1) + c) * ne + e];
+      const R jac = fg[(long long)(lf * (DIM + 1) + DIM) * ne + e];
+      const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
+      int e1 = e, lf1 = lf, e2 = nb, lf2 = lfo;
+      if (nb >= 0 && side) {
+        e1 = nb;
+        lf1 = lfo;
+        e2 = e;
+        lf2 = lf;
+      }
+      const R sg = side ? R(1) : R(-1);
+      for (int q = 0; q < NQF; ++q) {
+        const int q2 = sPerm[pid][q];
+        R s1[NEQ], s2[NEQ];
+        const R* B1 = sB[lf1][q];
+#pragma unroll
+        for (int k = 0; k < NEQ; ++k) {
+          const R* uk = u + k * NDa + (long long)e1 * ND;
+          R v = R(0);
+#pragma unroll
+          for (int s = 0; s < ND; ++s) v += uk[s] * B1[s];
+          s1[k] = v;
+        }
+        if (nb >= 0) {
+          const R* B2 = sB[lf2][q2];
+#pragma unroll
+          for (int k = 0; k < NEQ; ++k) {
+            const R* uk = u + k * NDa + (long long)e2 * ND;
+            R v = R(0);
+#pragma unroll
+            for (int s = 0; s < ND; ++s) v += uk[s] * B2[s];
+            s2[k] = v;
+          }
+        } else {
+          const BCSlot& bc = prm.bc[-2 - nb];
+          right_state<DIM>(bc.type, bc.state, s1, s2, n);
+        }
+        R F[NEQ];
+        R sp = riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg);
+        if (sp < R(0)) {
+          flag_error(prm.err, 2, e);
+          sp = R(0);
+        }
+        lmax = fmax(lmax, sp);
+        const R* Bo = sB[lf][side ? q2 : q];
+        const R wq = sW[q];
+#pragma unroll
+        for (int k = 0; k < NEQ; ++k) {
+          const R t = sg * (F[k] * wq) * jac;
+#pragma unroll
+          for (int s = 0; s < ND; ++s) acc[k][s] += t * Bo[s];
+        }
+      }
+    }
+    if (!prm.faces_only) {
+      const R* eg = (const R*)prm.egeo;
+      R adj[DIM][DIM];
+#pragma unroll
+      for (int r = 0; r < DIM; ++r)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) adj[r][d] = eg[(long long)(r * DIM + d) * ne + e];
+      const R idet = eg[(long long)(DIM * DIM) * ne + e];
+#pragma unroll
+      for (int m = 0; m < ND; ++m) {
+        R st[NEQ];
+#pragma unroll
+        for (int k = 0; k < NEQ; ++k) st[k] = u[k * NDa + (long long)e * ND + m];
+        R F[NEQ][DIM];
+        const R sp = flux_and_speed<DIM>(st, F, gamma, cov);
+        lmax = fmax(lmax, sp);
+#pragma unroll
+        for (int k = 0; k < NEQ; ++k)
+#pragma unroll
+          for (int r = 0; r < DIM; ++r) {
+            R G = R(0);
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) G += adj[r][d] * F[k][d];
+#pragma unroll
+            for (int j = 0; j < ND; ++j) acc[k][j] += sD[r][j][m] * G;
+          }
+      }
+#pragma unroll
+      for (int k = 0; k < NEQ; ++k) {
+        R y[ND];
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+          R v = R(0);
+#pragma unroll
+          for (int j = 0; j < ND; ++j) v += sMinv[i][j] * acc[k][j];
+          y[i] = v * idet;
+        }
+        epilogue<ND, R>(ep, k * NDa + (long long)e * ND, y, sWm, ne, e, k);
+      }
+    }
+  }
+  block_max_commit<R>(lmax, prm.mcs);
+}
+
+// ---- limiter ------------------------------------------------------------------
+// Limiter::update for one element (limiter.cpp:22-94): stencil = the element
+// and its face neighbours (ElementToElementTable, limiter.cpp:115-123), the
+// BJ-family indicator at the order-2 points of its interior faces
+// (indicator_bj.cpp:88-200, updateYMin 15-86), then LimiterMultiplier::limit
+// (limiter_multiplier.cpp:12-99, including the nd-fold application of the
+// density factor, quirks Q4/Q5, and the last-hope vertex check) or
+// LimiterFinDiff::limit (limiter_findiff.cpp:3-33, last equation only, Q6).
+// The update reads only this element's values and the cell means, so it is
+// done in place.  DS = true: the values are a float pair (u = hi, ulo = lo)
+// and the multiplier update runs in double-single arithmetic.
+template <int G, int P, typename R, bool DS>
+__global__ void __launch_bounds__(128)
+    k_limit_generic(const LimParams prm, R* __restrict__ u, float* __restrict__ ulo) {
+  using E = El<G, P>;
+  constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NFPE = E::NFPE, NQL = E::NQL, NV = E::NV;
+  __shared__ R sBl[NFPE][NQL][ND];
+  __shared__ R sBv[NV][ND];
+  const RefTables* T = prm.tab;
+  for (int t = threadIdx.x; t < NFPE * NQL * ND; t += blockDim.x) {
+    const int s = t % ND, q = (t / ND) % NQL, lf = t / (ND * NQL);
+    sBl[lf][q][s] = (R)T->Bl[lf][q][s];
+  }
+  for (int t = threadIdx.x; t < NV * ND; t += blockDim.x) sBv[t / ND][t % ND] = (R)T->Bv[t / ND][t % ND];
+  __syncthreads();
+  const int ne = prm.ne;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const long long NDa = prm.ndofs;
+  const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+  R el[NEQ][ND];
+  float lo[DS ? NEQ : 1][DS ? ND : 1];
+#pragma unroll
+  for (int k = 0; k < NEQ; ++k)
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      el[k][j] = u[k * NDa + (long long)e * ND + j];
+      if constexpr (DS) lo[k][j] = ulo[k * NDa + (long long)e * ND + j];
+    }
+  R um[NEQ];
+  float umh[NEQ], uml[NEQ];
+#pragma unroll
+  for (int k = 0; k < NEQ; ++k) {
+    const double m = prm.means[(long long)k * ne + e];
+    um[k] = (R)m;
+    umh[k] = (float)m;
+    uml[k] = (float)(m - (double)umh[k]);
+  }
+  R minValue;
+  R elind[NEQ];
+  if (prm.indicator == 0) {
+    minValue = R(1);
+#pragma unroll
+    for (int k = 0; k < NEQ; ++k) elind[k] = R(1);
+  } else if (prm.indicator == 1) {
+    minValue = R(0);
+#pragma unroll
+    for (int k = 0; k < NEQ; ++k) elind[k] = R(0);
+  } else {
+    R mI[NEQ], MI[NEQ], yMin[NEQ];
+#pragma unroll
+    for (int k = 0; k < NEQ; ++k) {
+      mI[k] = um[k] < R(1e9) ? um[k] : R(1e9);
+      MI[k] = um[k] > R(-1e9) ? um[k] : R(-1e9);
+      yMin[k] = R(1e9);
+    }
+    for (int lf = 0; lf < NFPE; ++lf) {
+      const int nb = prm.fnbr[lf * ne + e];
+      if (nb < 0) continue;
+#pragma unroll
+      for (int k = 0; k < NEQ; ++k) {
+        const R v = (R)prm.means[(long long)k * ne + nb];
+        mI[k] = v < mI[k] ? v : mI[k];
+        MI[k] = v > MI[k] ? v : MI[k];
+      }
+    }
+    for (int lf = 0; lf < NFPE; ++lf) {
+      const int nb = prm.fnbr[lf * ne + e];
+      if (nb < 0) continue;  // only interior faces carry indicator points
+#pragma unroll
+      for (int q = 0; q < NQL; ++q) {
+#pragma unroll
+        for (int k = 0; k < NEQ; ++k) {
+          R v = R(0);
+#pragma unroll
+          for (int j = 0; j < ND; ++j) {
+            v += el[k][j] * sBl[lf][q][j];
+            if constexpr (DS) v += lo[k][j] * sBl[lf][q][j];
+          }
+          const R diff = v - um[k];
+          R y;
+          if (diff > R(1e-3))
+            y = (MI[k] - um[k]) / diff;
+          else if (diff < R(-1e-3))
+            y = (mI[k] - um[k]) / diff;
+          else
+            y = R(1);
+          if (prm.function == 0) {
+            yMin[k] = y < yMin[k] ? y : yMin[k];
+            yMin[k] = yMin[k] > R(1) ? R(1) : yMin[k];
+          } else if (prm.function == 1) {
+            const R yc = (y * y + R(2) * y) / (y * y + y + R(2));
+            yMin[k] = yc < yMin[k] ? yc : yMin[k];
+          } else {
+            const R ys = R(1.5);
+            const R yr = y / ys;
+            const R yc = y < R(1) ? y + (R(3) - R(2) * ys) * yr * yr + (ys - R(2)) * yr * yr * yr : R(1);
+            yMin[k] = yc < yMin[k] ? yc : yMin[k];
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NEQ; ++k) elind[k] = yMin[k];
+    minValue = yMin[0];
+  }
+  if (prm.limiter == 1) {
+    const int reps = (prm.quirks & 1) ? 1 : ND;
+#pragma unroll
+    for (int k = 0; k < NEQ; ++k)
+      for (int r = 0; r < reps; ++r)
+#pragma unroll
+        for (int j = 0; j < ND; ++j) {
+          if constexpr (DS) {
+            float h = (float)el[k][j], l = lo[k][j];
+            ds_add(h, l, -umh[k], -uml[k]);
+            float ph, pl;
+            ds_mul_f(h, l, (float)minValue, ph, pl);
+            ds_add(ph, pl, umh[k], uml[k]);
+            el[k][j] = (R)ph;
+            lo[k][j] = pl;
+          } else {
+            el[k][j] = um[k] + minValue * (el[k][j] - um[k]);
+          }
+        }
+    if (prm.last_hope) {
+      for (int v = 0; v < NV; ++v) {
+        R fv[NEQ];
+#pragma unroll
+        for (int k = 0; k < NEQ; ++k) {
+          R s = R(0);
+#pragma unroll
+          for (int j = 0; j < ND; ++j) {
+            s += el[k][j] * sBv[v][j];
+            if constexpr (DS) s += lo[k][j] * sBv[v][j];
+          }
+          fv[k] = s;
+        }
+        if (!state_is_physical<DIM>(fv, gamma, cov)) {
+#pragma unroll
+          for (int k = 0; k < NEQ; ++k)
+#pragma unroll
+            for (int j = 0; j < ND; ++j) {
+              if constexpr (DS) {
+                el[k][j] = (R)umh[k];
+                lo[k][j] = uml[k];
+              } else {
+                el[k][j] = um[k];
+              }
+            }
+        }
+      }
+    }
+  } else {
+    const bool totalInd = elind[NEQ - 1] < R(0.999);
+    if (totalInd) {
+#pragma unroll
+      for (int k = 0; k < NEQ; ++k)
+#pragma unroll
+        for (int j = 0; j < ND; ++j) {
+          if constexpr (DS) {
+            el[k][j] = (R)umh[k];
+            lo[k][j] = uml[k];
+          } else {
+            el[k][j] = um[k];
+          }
+        }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NEQ; ++k)
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      u[k * NDa + (long long)e * ND + j] = el[k][j];
+      if constexpr (DS) ulo[k * NDa + (long long)e * ND + j] = lo[k][j];
+    }
+}
+
+// ---- cell means (Averager::computeMeanValues, averager.cpp:84-109) -----------
+// GridFunction::GetElementAverages = (int u) / (int 1); for affine elements the
+// Jacobian cancels and the weights are the reference integrals of the basis
+// functions normalised to sum 1.  lo (optional) is the low word of a float pair.
+template <int G, int P, typename T>
+__global__ void k_means_generic(int ne, long long ndofs, const RefTables* tab,
+                                const T* __restrict__ u, const float* __restrict__ ulo,
+                                double* __restrict__ means) {
+  using E = El<G, P>;
+  constexpr int ND = E::ND, NEQ = E::NEQ;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+#pragma unroll
+  for (int k = 0; k < NEQ; ++k) {
+    double m = 0.0;
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      double v = (double)u[k * ndofs + (long long)e * ND + j];
+      if (ulo) v += (double)ulo[k * ndofs + (long long)e * ND + j];
+      m += tab->wmean[j] * v;
+    }
+    means[(long long)k * ne + e] = m;
+  }
+}
+
+}  // namespace rkdg

@@ -1,0 +1,1024 @@
+// Host side of the GB300 RKDG C ABI (include/rkdg_gpu.h).
+//
+// Owns the device tables that replace MFEM's face/element transformations,
+// the Runge-Kutta stage orchestration of ExplicitRKLimitedSolver::Step
+// (rk_explicit_limited.cpp:30-82) and the time loop of main.cpp:467-553,
+// 701-733.  All arithmetic on the hot path runs in the CUDA kernels; this file
+// only builds tables, sizes buffers and enqueues launches.
+#include "rkdg_gpu.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "rkdg_common.h"
+#include "rkdg_launch.h"
+#include "rkdg_refelem.h"
+
+using rkdg::BCSlot;
+using rkdg::EpiParams;
+using rkdg::LimParams;
+using rkdg::RefTables;
+using rkdg::RhsParams;
+
+struct rkdg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  long long err_where = -1;
+  long long launches = 0;
+  // physics and scheme
+  int rs = RKDG_RS_RUSANOV, avg = RKDG_AVG_TRRS;
+  double gamma = 1.4, cov = 0.0, gasR = 1.0;
+  std::map<int, BCSlot> bcs;
+  int lim = RKDG_LIM_FINDIFF, ind = RKDG_IND_NOWHERE, fun = RKDG_FUN_MICHALAK, last_hope = 1,
+      quirks = 0;
+  int s = 3;
+  std::vector<double> a{1.0, 0.25, 0.25}, b{1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0}, c{1.0, 0.5};
+  int precision = RKDG_FP64;
+  // mesh (host copies)
+  bool has_mesh = false;
+  int dim = 0, geom = 0, p = 0, ne = 0, nd = 0, neq = 0, nfpe = 0, nvpe = 0;
+  long long ndofs = 0;
+  RefTables tab;
+  std::vector<int> h_fnbr, h_fattr, h_fcode;
+  std::vector<double> h_fgeo, h_egeo, h_wdet, h_nodes;
+  double hmin = 0.0;
+  // device tables
+  RefTables* d_tab = nullptr;
+  int* d_fnbr = nullptr;
+  int* d_fcode = nullptr;
+  double* d_fgeo64 = nullptr;
+  float* d_fgeo32 = nullptr;
+  double* d_egeo64 = nullptr;
+  float* d_egeo32 = nullptr;
+  double* d_wdet = nullptr;
+  unsigned long long* d_mcs = nullptr;  // 8 slots
+  int* d_err = nullptr;                 // 2 ints
+  double* d_means = nullptr;
+  double* d_partial = nullptr;
+  // scratch state buffers
+  double* d_k64[4] = {nullptr, nullptr, nullptr, nullptr};
+  float* d_k32[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* d_y64[2] = {nullptr, nullptr};
+  float* d_y32[2] = {nullptr, nullptr};
+  float* d_xh = nullptr;
+  float* d_xl = nullptr;
+  unsigned long long* h_mcs = nullptr;  // pinned
+  int* h_err = nullptr;                 // pinned
+
+  bool limiter_active() const { return !(lim == RKDG_LIM_FINDIFF && ind == RKDG_IND_NOWHERE); }
+};
+
+namespace {
+
+int fail(rkdg_ctx* c, int code, const std::string& msg, long long where = -1) {
+  if (c) {
+    c->err = msg;
+    c->err_where = where;
+  }
+  return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                              \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? RKDG_ERR_ALLOC : RKDG_ERR_CUDA, \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+  } while (0)
+
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+template <typename T>
+cudaError_t dalloc(T*& p, size_t n) {
+  dfree(p);
+  if (n == 0) return cudaSuccess;
+  return cudaMalloc((void**)&p, n * sizeof(T));
+}
+
+void free_mesh(rkdg_ctx* c) {
+  dfree(c->d_tab);
+  dfree(c->d_fnbr);
+  dfree(c->d_fcode);
+  dfree(c->d_fgeo64);
+  dfree(c->d_fgeo32);
+  dfree(c->d_egeo64);
+  dfree(c->d_egeo32);
+  dfree(c->d_wdet);
+  dfree(c->d_means);
+  dfree(c->d_partial);
+  for (auto& p : c->d_k64) dfree(p);
+  for (auto& p : c->d_k32) dfree(p);
+  for (auto& p : c->d_y64) dfree(p);
+  for (auto& p : c->d_y32) dfree(p);
+  dfree(c->d_xh);
+  dfree(c->d_xl);
+  c->has_mesh = false;
+}
+
+int nvpe_of(int geom) { return geom == 2 ? 3 : (geom == 3 ? 4 : 8); }
+int nfpe_of(int geom) { return geom == 2 ? 3 : (geom == 3 ? 4 : 6); }
+
+// Minimum singular value of a dim x dim matrix (row-major).
+double min_singular(int dim, const double* J) {
+  if (dim == 2) {
+    const double s1 = J[0] * J[0] + J[1] * J[1] + J[2] * J[2] + J[3] * J[3];
+    const double d = J[0] * J[3] - J[1] * J[2];
+    const double disc = std::sqrt(std::max(0.0, s1 * s1 - 4.0 * d * d));
+    return std::sqrt(std::max(0.0, 0.5 * (s1 - disc)));
+  }
+  double M[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double v = 0;
+      for (int k = 0; k < 3; ++k) v += J[k * 3 + i] * J[k * 3 + j];
+      M[i * 3 + j] = v;
+    }
+  // smallest eigenvalue of the symmetric matrix M by Jacobi rotations
+  double A[9];
+  std::memcpy(A, M, sizeof A);
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    double off = A[1] * A[1] + A[2] * A[2] + A[5] * A[5];
+    if (off < 1e-300) break;
+    for (int pq = 0; pq < 3; ++pq) {
+      const int pi = pq == 2 ? 1 : 0, qi = pq == 0 ? 1 : 2;
+      const double apq = A[pi * 3 + qi];
+      if (std::fabs(apq) < 1e-300) continue;
+      const double th = 0.5 * (A[qi * 3 + qi] - A[pi * 3 + pi]) / apq;
+      const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+      const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+      for (int k = 0; k < 3; ++k) {  // columns
+        const double akp = A[k * 3 + pi], akq = A[k * 3 + qi];
+        A[k * 3 + pi] = cs * akp - sn * akq;
+        A[k * 3 + qi] = sn * akp + cs * akq;
+      }
+      for (int k = 0; k < 3; ++k) {  // rows
+        const double apk = A[pi * 3 + k], aqk = A[qi * 3 + k];
+        A[pi * 3 + k] = cs * apk - sn * aqk;
+        A[qi * 3 + k] = sn * apk + cs * aqk;
+      }
+    }
+  }
+  const double lmin = std::min(A[0], std::min(A[4], A[8]));
+  return std::sqrt(std::max(0.0, lmin));
+}
+
+int refresh_fnbr(rkdg_ctx* c) {
+  if (!c->has_mesh) return RKDG_OK;
+  std::map<int, int> slot;
+  int k = 0;
+  for (auto& kv : c->bcs) slot[kv.first] = k++;
+  std::vector<int> f(c->h_fnbr);
+  for (size_t i = 0; i < f.size(); ++i)
+    if (f[i] < 0) {
+      auto it = slot.find(c->h_fattr[i]);
+      f[i] = it == slot.end() ? -1 : -2 - it->second;
+    }
+  CUDA_TRY(c, cudaMemcpy(c->d_fnbr, f.data(), f.size() * sizeof(int), cudaMemcpyHostToDevice));
+  return RKDG_OK;
+}
+
+RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
+  RhsParams P;
+  std::memset(&P, 0, sizeof P);
+  P.ne = c->ne;
+  P.ndofs = c->ndofs;
+  P.fnbr = c->d_fnbr;
+  P.fcode = c->d_fcode;
+  P.fgeo = prec == 0 ? (const void*)c->d_fgeo64 : (const void*)c->d_fgeo32;
+  P.egeo = prec == 0 ? (const void*)c->d_egeo64 : (const void*)c->d_egeo32;
+  P.tab = c->d_tab;
+  P.gamma = c->gamma;
+  P.covolume = c->cov;
+  P.rs = c->rs;
+  P.avg = c->avg;
+  P.faces_only = faces_only;
+  int k = 0;
+  for (auto& kv : c->bcs) P.bc[k++] = kv.second;
+  P.mcs = c->d_mcs + slot;
+  P.err = c->d_err;
+  return P;
+}
+
+LimParams lim_params(rkdg_ctx* c) {
+  LimParams L;
+  std::memset(&L, 0, sizeof L);
+  L.ne = c->ne;
+  L.ndofs = c->ndofs;
+  L.fnbr = c->d_fnbr;
+  L.tab = c->d_tab;
+  L.means = c->d_means;
+  L.gamma = c->gamma;
+  L.covolume = c->cov;
+  L.limiter = c->lim;
+  L.indicator = c->ind;
+  L.function = c->fun;
+  L.last_hope = c->last_hope;
+  L.quirks = c->quirks;
+  return L;
+}
+
+int ensure_scratch(rkdg_ctx* c) {
+  const size_t n = (size_t)c->ndofs * c->neq;
+  const int nk = std::max(c->s - 1, 0);
+  if (c->precision == RKDG_FP64) {
+    for (int i = 0; i < 4; ++i) {
+      if (i < nk && !c->d_k64[i]) CUDA_TRY(c, dalloc(c->d_k64[i], n));
+      if (i >= nk) dfree(c->d_k64[i]);
+    }
+    for (auto& p : c->d_k32) dfree(p);
+    for (int i = 0; i < 2; ++i)
+      if (!c->d_y64[i]) CUDA_TRY(c, dalloc(c->d_y64[i], n));
+    for (auto& p : c->d_y32) dfree(p);
+    dfree(c->d_xh);
+    dfree(c->d_xl);
+  } else {
+    for (int i = 0; i < 4; ++i) {
+      if (i < nk && !c->d_k32[i]) CUDA_TRY(c, dalloc(c->d_k32[i], n));
+      if (i >= nk) dfree(c->d_k32[i]);
+    }
+    for (auto& p : c->d_k64) dfree(p);
+    for (int i = 0; i < 2; ++i)
+      if (!c->d_y32[i]) CUDA_TRY(c, dalloc(c->d_y32[i], n));
+    dfree(c->d_y64[1]);
+    if (!c->d_y64[0]) CUDA_TRY(c, dalloc(c->d_y64[0], n));  // FP64 scratch for API calls
+    if (!c->d_xh) CUDA_TRY(c, dalloc(c->d_xh, n));
+    if (!c->d_xl) CUDA_TRY(c, dalloc(c->d_xl, n));
+  }
+  return RKDG_OK;
+}
+
+int check_device_error(rkdg_ctx* c) {
+  if (c->h_err[0] != 0) {
+    const int code = c->h_err[0];
+    char msg[128];
+    snprintf(msg, sizeof msg, "non-physical state in the Riemann solver at element %d",
+             c->h_err[1]);
+    CUDA_TRY(c, cudaMemsetAsync(c->d_err, 0, 2 * sizeof(int), c->stream));
+    return fail(c, code == 2 ? RKDG_ERR_UNPHYSICAL : RKDG_ERR_CUDA, msg, c->h_err[1]);
+  }
+  return RKDG_OK;
+}
+
+// Enqueue one Runge-Kutta step on the FP64 state x (no host synchronisation).
+int enqueue_step64(rkdg_ctx* c, double* x, double dt) {
+  const int s = c->s;
+  const bool lim = c->limiter_active();
+  const long long n = c->ndofs * c->neq;
+  for (int i = 0; i < s; ++i) {
+    const double* in;
+    if (i == 0) {
+      if (s == 1) {
+        CUDA_TRY(c, cudaMemcpyAsync(c->d_y64[0], x, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                    c->stream));
+        in = c->d_y64[0];
+      } else {
+        in = x;
+      }
+    } else {
+      in = c->d_y64[i % 2];
+    }
+    CUDA_TRY(c, cudaMemsetAsync(c->d_mcs + i, 0, sizeof(unsigned long long), c->stream));
+    EpiParams<double> ep;
+    std::memset(&ep, 0, sizeof ep);
+    ep.mode = 1;
+    ep.base = x;
+    double* out;
+    if (i < s - 1) {
+      const int row = (i + 1) * i / 2;  // MFEM packing: coefficients of y_{i+1}
+      for (int j = 0; j < i; ++j) {
+        ep.kprev[j] = c->d_k64[j];
+        ep.cprev[j] = c->a[row + j] * dt;
+      }
+      ep.nprev = i;
+      ep.ccur = c->a[row + i] * dt;
+      ep.kout = c->d_k64[i];
+      out = c->d_y64[(i + 1) % 2];
+    } else {
+      for (int j = 0; j < s - 1; ++j) {
+        ep.kprev[j] = c->d_k64[j];
+        ep.cprev[j] = c->b[j] * dt;
+      }
+      ep.nprev = s - 1;
+      ep.ccur = c->b[s - 1] * dt;
+      out = x;
+    }
+    ep.out64 = out;
+    ep.means = lim ? c->d_means : nullptr;
+    RhsParams P = rhs_params(c, 0, 0, i);
+    CUDA_TRY(c, rkdg::launch_rhs(c->geom, c->p, 0, P, in, &ep, c->stream));
+    c->launches++;
+    if (lim) {
+      LimParams L = lim_params(c);
+      CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 0, L, out, nullptr, c->stream));
+      c->launches++;
+    }
+  }
+  return RKDG_OK;
+}
+
+void split_coef(double v, float& hi, float& lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+// Enqueue one step on the float-pair state (d_xh, d_xl).
+int enqueue_step32(rkdg_ctx* c, double dt) {
+  const int s = c->s;
+  const bool lim = c->limiter_active();
+  const long long n = c->ndofs * c->neq;
+  for (int i = 0; i < s; ++i) {
+    const float* in;
+    if (i == 0) {
+      if (s == 1) {
+        CUDA_TRY(c, rkdg::launch_copy_f(n, c->d_xh, c->d_y32[0], c->stream));
+        c->launches++;
+        in = c->d_y32[0];
+      } else {
+        in = c->d_xh;
+      }
+    } else {
+      in = c->d_y32[i % 2];
+    }
+    CUDA_TRY(c, cudaMemsetAsync(c->d_mcs + i, 0, sizeof(unsigned long long), c->stream));
+    EpiParams<float> ep;
+    std::memset(&ep, 0, sizeof ep);
+    ep.mode = 1;
+    ep.basehi = c->d_xh;
+    ep.baselo = c->d_xl;
+    if (i < s - 1) {
+      const int row = (i + 1) * i / 2;
+      for (int j = 0; j < i; ++j) {
+        ep.kprev[j] = c->d_k32[j];
+        split_coef(c->a[row + j] * dt, ep.cprev_hi[j], ep.cprev_lo[j]);
+      }
+      ep.nprev = i;
+      split_coef(c->a[row + i] * dt, ep.ccur_hi, ep.ccur_lo);
+      ep.kout = c->d_k32[i];
+      ep.out32 = c->d_y32[(i + 1) % 2];
+      ep.final_stage = 0;
+    } else {
+      for (int j = 0; j < s - 1; ++j) {
+        ep.kprev[j] = c->d_k32[j];
+        split_coef(c->b[j] * dt, ep.cprev_hi[j], ep.cprev_lo[j]);
+      }
+      ep.nprev = s - 1;
+      split_coef(c->b[s - 1] * dt, ep.ccur_hi, ep.ccur_lo);
+      ep.out32 = c->d_xh;
+      ep.outlo = c->d_xl;
+      ep.final_stage = 1;
+    }
+    ep.means = lim ? c->d_means : nullptr;
+    RhsParams P = rhs_params(c, 1, 0, i);
+    CUDA_TRY(c, rkdg::launch_rhs(c->geom, c->p, 1, P, in, &ep, c->stream));
+    c->launches++;
+    if (lim) {
+      LimParams L = lim_params(c);
+      if (i < s - 1)
+        CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 1, L, c->d_y32[(i + 1) % 2], nullptr, c->stream));
+      else
+        CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 2, L, c->d_xh, c->d_xl, c->stream));
+      c->launches++;
+    }
+  }
+  return RKDG_OK;
+}
+
+int read_mcs(rkdg_ctx* c, int slot, double* out) {
+  CUDA_TRY(c, cudaMemcpyAsync(c->h_mcs, c->d_mcs + slot, sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(c->h_err, c->d_err, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                              c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  int st = check_device_error(c);
+  if (st) return st;
+  if (out) {
+    double v;
+    unsigned long long bits = c->h_mcs[0];
+    std::memcpy(&v, &bits, sizeof v);
+    *out = v;
+  }
+  return RKDG_OK;
+}
+
+#define NEED_MESH(c)                                              \
+  do {                                                            \
+    if (!(c)) return RKDG_ERR_INVALID;                            \
+    if (!(c)->has_mesh) return fail(c, RKDG_ERR_NOMESH, "no mesh"); \
+    cudaSetDevice((c)->device);                                   \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int rkdg_create(rkdg_ctx** out, int device) {
+  if (!out) return RKDG_ERR_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return RKDG_ERR_NOT_FOUND;
+  if (device < 0 || device >= n) return RKDG_ERR_INVALID;
+  rkdg_ctx* c = new rkdg_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc((void**)&c->d_mcs, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc((void**)&c->d_err, 2 * sizeof(int)) != cudaSuccess ||
+      cudaMallocHost((void**)&c->h_mcs, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMallocHost((void**)&c->h_err, 2 * sizeof(int)) != cudaSuccess ||
+      cudaMemset(c->d_err, 0, 2 * sizeof(int)) != cudaSuccess) {
+    delete c;
+    return RKDG_ERR_CUDA;
+  }
+  c->own_stream = true;
+  *out = c;
+  return RKDG_OK;
+}
+
+int rkdg_destroy(rkdg_ctx* c) {
+  if (!c) return RKDG_ERR_INVALID;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  free_mesh(c);
+  dfree(c->d_mcs);
+  dfree(c->d_err);
+  if (c->h_mcs) cudaFreeHost(c->h_mcs);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return RKDG_OK;
+}
+
+const char* rkdg_last_error(rkdg_ctx* c, long long* where) {
+  if (!c) return "null context";
+  if (where) *where = c->err_where;
+  return c->err.c_str();
+}
+
+int rkdg_set_stream(rkdg_ctx* c, void* st) {
+  if (!c) return RKDG_ERR_INVALID;
+  cudaSetDevice(c->device);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  if (st) {
+    c->stream = (cudaStream_t)st;
+    c->own_stream = false;
+  } else {
+    CUDA_TRY(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->own_stream = true;
+  }
+  return RKDG_OK;
+}
+
+int rkdg_synchronize(rkdg_ctx* c) {
+  if (!c) return RKDG_ERR_INVALID;
+  cudaSetDevice(c->device);
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return RKDG_OK;
+}
+
+int rkdg_set_physics(rkdg_ctx* c, int rsolver, int averaging, double gamma, double covolume,
+                     double gas_constant) {
+  if (!c) return RKDG_ERR_INVALID;
+  if (rsolver < 0 || rsolver > 3 || averaging < 0 || averaging > 1 || !(gamma > 1.0) ||
+      covolume < 0.0)
+    return fail(c, RKDG_ERR_INVALID, "invalid physics parameters");
+  c->rs = rsolver;
+  c->avg = averaging;
+  c->gamma = gamma;
+  c->cov = covolume;
+  c->gasR = gas_constant;
+  return RKDG_OK;
+}
+
+int rkdg_set_bc(rkdg_ctx* c, int attr, int type, const double* state) {
+  if (!c) return RKDG_ERR_INVALID;
+  if (type < 0 || type > 4 || attr < 1) return fail(c, RKDG_ERR_INVALID, "invalid boundary condition");
+  if ((type == RKDG_BC_FIXED_ROTATED || type == RKDG_BC_SUPERSONIC_INLET) && !state)
+    return fail(c, RKDG_ERR_INVALID, "fixed-state boundary needs a state");
+  if (!c->bcs.count(attr) && (int)c->bcs.size() >= RKDG_MAX_BC)
+    return fail(c, RKDG_ERR_INVALID, "too many boundary attributes");
+  BCSlot bc;
+  std::memset(&bc, 0, sizeof bc);
+  bc.type = type;
+  if (state)
+    for (int i = 0; i < 5; ++i) bc.state[i] = (i < (c->has_mesh ? c->neq : 5)) ? state[i] : 0.0;
+  c->bcs[attr] = bc;
+  if (c->has_mesh) {
+    cudaSetDevice(c->device);
+    return refresh_fnbr(c);
+  }
+  return RKDG_OK;
+}
+
+int rkdg_set_limiter(rkdg_ctx* c, int limiter, int indicator, int function, int last_hope,
+                     int quirk_flags) {
+  if (!c) return RKDG_ERR_INVALID;
+  if (limiter < 0 || limiter > 1 || indicator < 0 || indicator > 2 || function < 0 || function > 2)
+    return fail(c, RKDG_ERR_INVALID, "invalid limiter configuration");
+  c->lim = limiter;
+  c->ind = indicator;
+  c->fun = function;
+  c->last_hope = last_hope ? 1 : 0;
+  c->quirks = quirk_flags;
+  return RKDG_OK;
+}
+
+int rkdg_set_tableau(rkdg_ctx* c, int s, const double* a, const double* b, const double* cc) {
+  if (!c) return RKDG_ERR_INVALID;
+  if (s < 1 || s > 4 || !b || (s > 1 && !a)) return fail(c, RKDG_ERR_INVALID, "invalid tableau");
+  c->s = s;
+  c->a.assign(a ? a : b, (a ? a : b) + s * (s - 1) / 2);
+  c->b.assign(b, b + s);
+  if (cc)
+    c->c.assign(cc, cc + std::max(s - 1, 0));
+  else
+    c->c.assign(std::max(s - 1, 0), 0.0);
+  if (c->has_mesh) {
+    cudaSetDevice(c->device);
+    return ensure_scratch(c);
+  }
+  return RKDG_OK;
+}
+
+int rkdg_set_precision(rkdg_ctx* c, int precision) {
+  if (!c) return RKDG_ERR_INVALID;
+  if (precision != RKDG_FP64 && precision != RKDG_FP32_BULK)
+    return fail(c, RKDG_ERR_INVALID, "invalid precision");
+  c->precision = precision;
+  if (c->has_mesh) {
+    cudaSetDevice(c->device);
+    return ensure_scratch(c);
+  }
+  return RKDG_OK;
+}
+
+int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
+  if (!c || !m) return RKDG_ERR_INVALID;
+  cudaSetDevice(c->device);
+  const int dim = m->dim, geom = m->geom, p = m->order, ne = m->num_elements;
+  if (!((dim == 2 && (geom == RKDG_GEOM_TRIANGLE || geom == RKDG_GEOM_SQUARE)) ||
+        (dim == 3 && geom == RKDG_GEOM_CUBE)))
+    return fail(c, RKDG_ERR_UNSUPPORTED, "unsupported geometry / dimension");
+  if (!rkdg::generic_supported(geom, p))
+    return fail(c, RKDG_ERR_UNSUPPORTED, "unsupported polynomial order for this geometry");
+  if (ne <= 0 || !m->elem_vertices || !m->elem_coords || m->num_bdr < 0 ||
+      (m->num_bdr > 0 && (!m->bdr_vertices || !m->bdr_attr)))
+    return fail(c, RKDG_ERR_INVALID, "invalid mesh description");
+  free_mesh(c);
+  RefTables T;
+  std::vector<rkdg::FacePoint> fpts;
+  if (!rkdg::build_ref_tables(geom, p, T, &fpts))
+    return fail(c, RKDG_ERR_UNSUPPORTED, "reference tables exceed the supported sizes");
+  const int nvpe = nvpe_of(geom), nfpe = nfpe_of(geom), nvpf = dim == 2 ? 2 : 4;
+  const int gs = rkdg::geom_slot(geom);
+  const int nd = T.nd, neq = dim + 2;
+  c->dim = dim;
+  c->geom = geom;
+  c->p = p;
+  c->ne = ne;
+  c->nd = nd;
+  c->neq = neq;
+  c->nfpe = nfpe;
+  c->nvpe = nvpe;
+  c->ndofs = (long long)ne * nd;
+  // ---- element geometry (affine elements) ----
+  c->h_egeo.assign((size_t)(dim * dim + 1) * ne, 0.0);
+  c->h_wdet.assign(ne, 0.0);
+  c->h_nodes.assign((size_t)dim * c->ndofs, 0.0);
+  const double refvol = geom == 2 ? 0.5 : 1.0;
+  double hmin = 1e300;
+  std::vector<double> Jall((size_t)ne * 9);
+  for (int e = 0; e < ne; ++e) {
+    const double* X = m->elem_coords + (size_t)e * nvpe * dim;
+    double col[3][3] = {{0}};
+    const int vi[3] = {1, geom == 2 ? 2 : 3, 4};
+    for (int r = 0; r < dim; ++r)
+      for (int i = 0; i < dim; ++i) col[r][i] = X[vi[r] * dim + i] - X[i];
+    double scale = 0;
+    for (int r = 0; r < dim; ++r)
+      for (int i = 0; i < dim; ++i) scale = std::max(scale, std::fabs(col[r][i]));
+    for (int v = 0; v < nvpe; ++v) {
+      const double* rv = rkdg::kRefVert[gs][v];
+      for (int i = 0; i < dim; ++i) {
+        double pred = X[i];
+        for (int r = 0; r < dim; ++r) pred += rv[r] * col[r][i];
+        if (std::fabs(pred - X[v * dim + i]) > 1e-9 * scale)
+          return fail(c, RKDG_ERR_UNSUPPORTED, "non-affine element (only affine elements are supported)", e);
+      }
+    }
+    double J[9] = {0};
+    for (int i = 0; i < dim; ++i)
+      for (int r = 0; r < dim; ++r) J[i * dim + r] = col[r][i];
+    double det, adj[9];
+    if (dim == 2) {
+      det = J[0] * J[3] - J[1] * J[2];
+      adj[0] = J[3];
+      adj[1] = -J[1];
+      adj[2] = -J[2];
+      adj[3] = J[0];
+    } else {
+      adj[0] = J[4] * J[8] - J[5] * J[7];
+      adj[1] = J[2] * J[7] - J[1] * J[8];
+      adj[2] = J[1] * J[5] - J[2] * J[4];
+      adj[3] = J[5] * J[6] - J[3] * J[8];
+      adj[4] = J[0] * J[8] - J[2] * J[6];
+      adj[5] = J[2] * J[3] - J[0] * J[5];
+      adj[6] = J[3] * J[7] - J[4] * J[6];
+      adj[7] = J[1] * J[6] - J[0] * J[7];
+      adj[8] = J[0] * J[4] - J[1] * J[3];
+      det = J[0] * adj[0] + J[1] * adj[3] + J[2] * adj[6];
+    }
+    if (!(det > 0.0)) return fail(c, RKDG_ERR_INVALID, "inverted or degenerate element", e);
+    for (int rd = 0; rd < dim * dim; ++rd) c->h_egeo[(size_t)rd * ne + e] = adj[rd];
+    c->h_egeo[(size_t)(dim * dim) * ne + e] = 1.0 / det;
+    c->h_wdet[e] = det * refvol;
+    double Jp[9];
+    std::memcpy(Jp, J, sizeof Jp);
+    if (geom == 2) {  // relative to the equilateral reference triangle
+      const double A[4] = {1.0, -1.0 / std::sqrt(3.0), 0.0, 2.0 / std::sqrt(3.0)};
+      for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) Jp[i * 2 + j] = J[i * 2] * A[j] + J[i * 2 + 1] * A[2 + j];
+    }
+    hmin = std::min(hmin, min_singular(dim, Jp));
+    std::memcpy(&Jall[(size_t)e * 9], J, sizeof J);
+  }
+  c->hmin = hmin;
+  {
+    rkdg::Basis B(geom, p);
+    for (int e = 0; e < ne; ++e) {
+      const double* X = m->elem_coords + (size_t)e * nvpe * dim;
+      const double* J = &Jall[(size_t)e * 9];
+      for (int j = 0; j < nd; ++j)
+        for (int i = 0; i < dim; ++i) {
+          double v = X[i];
+          for (int r = 0; r < dim; ++r) v += J[i * dim + r] * B.nodes[j * dim + r];
+          c->h_nodes[(size_t)i * c->ndofs + (long long)e * nd + j] = v;
+        }
+    }
+  }
+  // ---- faces ----
+  struct Side {
+    int e = -1, lf = -1;
+  };
+  struct FaceRec {
+    Side s1, s2;
+  };
+  std::map<std::array<int, 4>, int> key2f;
+  std::vector<FaceRec> faces;
+  auto face_key = [&](const int* ids) {
+    std::array<int, 4> k = {-1, -1, -1, -1};
+    for (int i = 0; i < nvpf; ++i) k[i] = ids[i];
+    for (int i = 1; i < nvpf; ++i)
+      for (int j = i; j > 0 && k[j - 1] > k[j]; --j) std::swap(k[j - 1], k[j]);
+    return k;
+  };
+  for (int e = 0; e < ne; ++e)
+    for (int lf = 0; lf < nfpe; ++lf) {
+      int ids[4];
+      for (int k = 0; k < nvpf; ++k)
+        ids[k] = m->elem_vertices[(size_t)e * nvpe + rkdg::kFaceVert[gs][lf][k]];
+      auto key = face_key(ids);
+      auto it = key2f.find(key);
+      if (it == key2f.end()) {
+        key2f[key] = (int)faces.size();
+        FaceRec f;
+        f.s1 = {e, lf};
+        faces.push_back(f);
+      } else {
+        FaceRec& f = faces[it->second];
+        if (f.s2.e >= 0) return fail(c, RKDG_ERR_INVALID, "non-manifold face", e);
+        f.s2 = {e, lf};
+      }
+    }
+  std::map<std::array<int, 4>, int> bkey;
+  for (int i = 0; i < m->num_bdr; ++i) bkey[face_key(m->bdr_vertices + (size_t)i * nvpf)] = m->bdr_attr[i];
+  c->h_fnbr.assign((size_t)nfpe * ne, -1);
+  c->h_fattr.assign((size_t)nfpe * ne, 0);
+  c->h_fcode.assign((size_t)nfpe * ne, 0);
+  c->h_fgeo.assign((size_t)nfpe * (dim + 1) * ne, 0.0);
+  std::map<std::vector<int>, int> perm_ids;
+  {
+    std::vector<int> id(T.nqf);
+    for (int q = 0; q < T.nqf; ++q) id[q] = q;
+    perm_ids[id] = 0;
+    for (int q = 0; q < T.nqf; ++q) T.perm[0][q] = q;
+  }
+  auto fp_of = [&](int lf, int q) -> const rkdg::FacePoint& { return fpts[(size_t)lf * T.nqf + q]; };
+  for (auto& kv : key2f) {
+    const FaceRec& f = faces[kv.second];
+    const int e1 = f.s1.e, lf1 = f.s1.lf;
+    const double* X = m->elem_coords + (size_t)e1 * nvpe * dim;
+    const int* fv = rkdg::kFaceVert[gs][lf1];
+    double nor[3];
+    if (dim == 2) {
+      const double jx = X[fv[1] * 2] - X[fv[0] * 2], jy = X[fv[1] * 2 + 1] - X[fv[0] * 2 + 1];
+      nor[0] = jy;
+      nor[1] = -jx;
+    } else {
+      double ds[3], dt[3];
+      for (int i = 0; i < 3; ++i) {
+        ds[i] = X[fv[1] * 3 + i] - X[fv[0] * 3 + i];
+        dt[i] = X[fv[3] * 3 + i] - X[fv[0] * 3 + i];
+      }
+      nor[0] = ds[1] * dt[2] - ds[2] * dt[1];
+      nor[1] = ds[2] * dt[0] - ds[0] * dt[2];
+      nor[2] = ds[0] * dt[1] - ds[1] * dt[0];
+    }
+    double nm = 0;
+    for (int i = 0; i < dim; ++i) nm += nor[i] * nor[i];
+    nm = std::sqrt(nm);
+    const double inv = 1.0 / nm;
+    double nh[3];
+    for (int i = 0; i < dim; ++i) nh[i] = nor[i] * inv;
+    auto put_geo = [&](int e, int lf) {
+      for (int i = 0; i < dim; ++i) c->h_fgeo[(size_t)(lf * (dim + 1) + i) * ne + e] = nh[i];
+      c->h_fgeo[(size_t)(lf * (dim + 1) + dim) * ne + e] = nm;
+    };
+    put_geo(e1, lf1);
+    if (f.s2.e < 0) {
+      auto bit = bkey.find(kv.first);
+      c->h_fattr[(size_t)lf1 * ne + e1] = bit == bkey.end() ? 0 : bit->second;
+      c->h_fnbr[(size_t)lf1 * ne + e1] = -1;
+      continue;
+    }
+    const int e2 = f.s2.e, lf2 = f.s2.lf;
+    put_geo(e2, lf2);
+    // point permutation: e1 canonical point q -> e2 canonical point on lf2
+    std::vector<int> pm(T.nqf, -1);
+    int ids1[4];
+    for (int k = 0; k < nvpf; ++k) ids1[k] = m->elem_vertices[(size_t)e1 * nvpe + fv[k]];
+    for (int q = 0; q < T.nqf; ++q) {
+      const rkdg::FacePoint& P1 = fp_of(lf1, q);
+      double N[4];
+      if (dim == 2) {
+        N[0] = 1 - P1.s[0];
+        N[1] = P1.s[0];
+      } else {
+        N[0] = (1 - P1.s[0]) * (1 - P1.s[1]);
+        N[1] = P1.s[0] * (1 - P1.s[1]);
+        N[2] = P1.s[0] * P1.s[1];
+        N[3] = (1 - P1.s[0]) * P1.s[1];
+      }
+      double xi2[3] = {0, 0, 0};
+      for (int k = 0; k < nvpf; ++k) {
+        int lv = -1;
+        for (int mm = 0; mm < nvpf; ++mm) {
+          const int v2 = rkdg::kFaceVert[gs][lf2][mm];
+          if (m->elem_vertices[(size_t)e2 * nvpe + v2] == ids1[k]) lv = v2;
+        }
+        if (lv < 0) return fail(c, RKDG_ERR_INVALID, "inconsistent face vertices", e2);
+        for (int i = 0; i < dim; ++i) xi2[i] += N[k] * rkdg::kRefVert[gs][lv][i];
+      }
+      for (int q2 = 0; q2 < T.nqf; ++q2) {
+        const rkdg::FacePoint& P2 = fp_of(lf2, q2);
+        double d = 0;
+        for (int i = 0; i < dim; ++i) d = std::max(d, std::fabs(P2.xi[i] - xi2[i]));
+        if (d < 1e-10) pm[q] = q2;
+      }
+      if (pm[q] < 0) return fail(c, RKDG_ERR_INVALID, "face points do not match", e2);
+    }
+    int pid;
+    auto pit = perm_ids.find(pm);
+    if (pit == perm_ids.end()) {
+      pid = (int)perm_ids.size();
+      if (pid >= RKDG_MAX_PERM) return fail(c, RKDG_ERR_UNSUPPORTED, "too many face orientations");
+      perm_ids[pm] = pid;
+      for (int q = 0; q < T.nqf; ++q) T.perm[pid][q] = pm[q];
+    } else {
+      pid = pit->second;
+    }
+    c->h_fnbr[(size_t)lf1 * ne + e1] = e2;
+    c->h_fnbr[(size_t)lf2 * ne + e2] = e1;
+    c->h_fcode[(size_t)lf1 * ne + e1] = lf2 | (0 << 3) | (pid << 4);
+    c->h_fcode[(size_t)lf2 * ne + e2] = lf1 | (1 << 3) | (pid << 4);
+  }
+  T.nperm = (int)perm_ids.size();
+  c->tab = T;
+  // ---- upload ----
+  const size_t nf = (size_t)nfpe * ne;
+  CUDA_TRY(c, dalloc(c->d_tab, 1));
+  CUDA_TRY(c, cudaMemcpy(c->d_tab, &c->tab, sizeof(RefTables), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, dalloc(c->d_fnbr, nf));
+  CUDA_TRY(c, dalloc(c->d_fcode, nf));
+  CUDA_TRY(c, cudaMemcpy(c->d_fcode, c->h_fcode.data(), nf * sizeof(int), cudaMemcpyHostToDevice));
+  std::vector<float> f32(c->h_fgeo.begin(), c->h_fgeo.end());
+  CUDA_TRY(c, dalloc(c->d_fgeo64, c->h_fgeo.size()));
+  CUDA_TRY(c, dalloc(c->d_fgeo32, c->h_fgeo.size()));
+  CUDA_TRY(c, cudaMemcpy(c->d_fgeo64, c->h_fgeo.data(), c->h_fgeo.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->d_fgeo32, f32.data(), f32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  std::vector<float> e32(c->h_egeo.begin(), c->h_egeo.end());
+  CUDA_TRY(c, dalloc(c->d_egeo64, c->h_egeo.size()));
+  CUDA_TRY(c, dalloc(c->d_egeo32, c->h_egeo.size()));
+  CUDA_TRY(c, cudaMemcpy(c->d_egeo64, c->h_egeo.data(), c->h_egeo.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->d_egeo32, e32.data(), e32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, dalloc(c->d_wdet, (size_t)ne));
+  CUDA_TRY(c, cudaMemcpy(c->d_wdet, c->h_wdet.data(), ne * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, dalloc(c->d_means, (size_t)neq * ne));
+  CUDA_TRY(c, dalloc(c->d_partial, (size_t)neq * 1024));
+  c->has_mesh = true;
+  int st = refresh_fnbr(c);
+  if (st) return st;
+  return ensure_scratch(c);
+}
+
+int rkdg_sizes(rkdg_ctx* c, long long* ndofs, int* nd, int* neq) {
+  if (!c) return RKDG_ERR_INVALID;
+  if (!c->has_mesh) return fail(c, RKDG_ERR_NOMESH, "no mesh");
+  if (ndofs) *ndofs = c->ndofs;
+  if (nd) *nd = c->nd;
+  if (neq) *neq = c->neq;
+  return RKDG_OK;
+}
+
+int rkdg_node_coords_host(rkdg_ctx* c, double* out) {
+  if (!c || !out) return RKDG_ERR_INVALID;
+  if (!c->has_mesh) return fail(c, RKDG_ERR_NOMESH, "no mesh");
+  std::memcpy(out, c->h_nodes.data(), c->h_nodes.size() * sizeof(double));
+  return RKDG_OK;
+}
+
+int rkdg_hmin(rkdg_ctx* c, double* hmin) {
+  if (!c || !hmin) return RKDG_ERR_INVALID;
+  if (!c->has_mesh) return fail(c, RKDG_ERR_NOMESH, "no mesh");
+  *hmin = c->hmin;
+  return RKDG_OK;
+}
+
+int rkdg_rhs(rkdg_ctx* c, const double* x, double* y, double* mcs_out) {
+  NEED_MESH(c);
+  if (!x || !y) return fail(c, RKDG_ERR_INVALID, "null state pointer");
+  CUDA_TRY(c, cudaMemsetAsync(c->d_mcs, 0, sizeof(unsigned long long), c->stream));
+  const long long n = c->ndofs * c->neq;
+  if (c->precision == RKDG_FP64) {
+    EpiParams<double> ep;
+    std::memset(&ep, 0, sizeof ep);
+    ep.mode = 0;
+    ep.out64 = y;
+    RhsParams P = rhs_params(c, 0, 0, 0);
+    CUDA_TRY(c, rkdg::launch_rhs(c->geom, c->p, 0, P, x, &ep, c->stream));
+    c->launches++;
+  } else {
+    CUDA_TRY(c, rkdg::launch_to_float(n, x, c->d_y32[0], c->stream));
+    EpiParams<float> ep;
+    std::memset(&ep, 0, sizeof ep);
+    ep.mode = 0;
+    ep.out64 = y;
+    RhsParams P = rhs_params(c, 1, 0, 0);
+    CUDA_TRY(c, rkdg::launch_rhs(c->geom, c->p, 1, P, c->d_y32[0], &ep, c->stream));
+    c->launches += 2;
+  }
+  return read_mcs(c, 0, mcs_out);
+}
+
+int rkdg_face_speed(rkdg_ctx* c, const double* x, double* mcs_out) {
+  NEED_MESH(c);
+  if (!x) return fail(c, RKDG_ERR_INVALID, "null state pointer");
+  CUDA_TRY(c, cudaMemsetAsync(c->d_mcs, 0, sizeof(unsigned long long), c->stream));
+  EpiParams<double> ep;
+  std::memset(&ep, 0, sizeof ep);
+  RhsParams P = rhs_params(c, 0, 1, 0);
+  CUDA_TRY(c, rkdg::launch_rhs(c->geom, c->p, 0, P, x, &ep, c->stream));
+  c->launches++;
+  return read_mcs(c, 0, mcs_out);
+}
+
+int rkdg_cell_means(rkdg_ctx* c, const double* x, double* means) {
+  NEED_MESH(c);
+  if (!x || !means) return fail(c, RKDG_ERR_INVALID, "null pointer");
+  CUDA_TRY(c, rkdg::launch_means(c->geom, c->p, 0, c->ne, c->ndofs, c->d_tab, x, nullptr, means, c->stream));
+  c->launches++;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return RKDG_OK;
+}
+
+int rkdg_limit(rkdg_ctx* c, double* x) {
+  NEED_MESH(c);
+  if (!x) return fail(c, RKDG_ERR_INVALID, "null state pointer");
+  if (!c->limiter_active()) return RKDG_OK;
+  CUDA_TRY(c, rkdg::launch_means(c->geom, c->p, 0, c->ne, c->ndofs, c->d_tab, x, nullptr, c->d_means, c->stream));
+  LimParams L = lim_params(c);
+  CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 0, L, x, nullptr, c->stream));
+  c->launches += 2;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return RKDG_OK;
+}
+
+int rkdg_step(rkdg_ctx* c, double* x, double dt, double* next_mcs) {
+  NEED_MESH(c);
+  if (!x) return fail(c, RKDG_ERR_INVALID, "null state pointer");
+  int st = ensure_scratch(c);
+  if (st) return st;
+  const long long n = c->ndofs * c->neq;
+  if (c->precision == RKDG_FP64) {
+    st = enqueue_step64(c, x, dt);
+  } else {
+    CUDA_TRY(c, rkdg::launch_split(n, x, c->d_xh, c->d_xl, c->stream));
+    st = enqueue_step32(c, dt);
+    if (!st) CUDA_TRY(c, rkdg::launch_join(n, c->d_xh, c->d_xl, x, c->stream));
+    c->launches += 2;
+  }
+  if (st) return st;
+  return read_mcs(c, c->s - 1, next_mcs);
+}
+
+int rkdg_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0, int dt_mode,
+             int max_steps, int* steps_out, double* t_out, double* dt_out, double* sum_dt_out) {
+  NEED_MESH(c);
+  if (!x || dt_mode < 0 || dt_mode > 2) return fail(c, RKDG_ERR_INVALID, "invalid run arguments");
+  int st = ensure_scratch(c);
+  if (st) return st;
+  const long long n = c->ndofs * c->neq;
+  double dt = dt0;
+  const double denom = 2.0 * c->p + 1.0;
+  if (dt_mode != 2) {
+    double mcs = 0;
+    st = rkdg_face_speed(c, x, &mcs);
+    if (st) return st;
+    if (!(mcs > 0)) return fail(c, RKDG_ERR_INVALID, "zero wave speed: cannot form a CFL dt");
+    dt = cfl * c->hmin / mcs / denom;
+  }
+  if (!(dt > 0)) return fail(c, RKDG_ERR_INVALID, "non-positive dt");
+  const bool fp32 = c->precision != RKDG_FP64;
+  if (fp32) {
+    CUDA_TRY(c, rkdg::launch_split(n, x, c->d_xh, c->d_xl, c->stream));
+    c->launches++;
+  }
+  double t = 0.0, sum_dt = 0.0;
+  int ti = 0;
+  bool done = false;
+  while (!done) {
+    const double dt_real = std::min(dt, t_end - t);
+    st = fp32 ? enqueue_step32(c, dt_real) : enqueue_step64(c, x, dt_real);
+    if (st) return st;
+    sum_dt += dt_real;
+    if (dt_mode == 0) {
+      double mcs = 0;
+      st = read_mcs(c, c->s - 1, &mcs);
+      if (st) return st;
+      dt = cfl * c->hmin / mcs / denom;
+    }
+    t += dt;
+    ti++;
+    done = (t >= t_end - 1e-8 * dt);
+    if (max_steps > 0 && ti >= max_steps) break;
+  }
+  if (fp32) {
+    CUDA_TRY(c, rkdg::launch_join(n, c->d_xh, c->d_xl, x, c->stream));
+    c->launches++;
+  }
+  st = read_mcs(c, c->s - 1, nullptr);
+  if (st) return st;
+  if (steps_out) *steps_out = ti;
+  if (t_out) *t_out = t;
+  if (dt_out) *dt_out = dt;
+  if (sum_dt_out) *sum_dt_out = sum_dt;
+  return RKDG_OK;
+}
+
+int rkdg_totals(rkdg_ctx* c, const double* x, double* totals) {
+  NEED_MESH(c);
+  if (!x || !totals) return fail(c, RKDG_ERR_INVALID, "null pointer");
+  const int nb = 256;
+  CUDA_TRY(c, rkdg::launch_totals(c->nd, c->neq, c->ne, c->ndofs, c->d_tab, c->d_wdet, x, c->d_partial, nb, c->stream));
+  c->launches++;
+  std::vector<double> part((size_t)c->neq * nb);
+  CUDA_TRY(c, cudaMemcpyAsync(part.data(), c->d_partial, part.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < c->neq; ++k) {
+    long double s = 0;
+    for (int b = 0; b < nb; ++b) s += part[(size_t)k * nb + b];
+    totals[k] = (double)s;
+  }
+  return RKDG_OK;
+}
+
+int rkdg_riemann_batch(rkdg_ctx* c, int n, const double* u1, const double* u2, const double* nor,
+                       double* flux, double* speed) {
+  if (!c) return RKDG_ERR_INVALID;
+  if (!c->has_mesh) return fail(c, RKDG_ERR_NOMESH, "no mesh (the dimension comes from the mesh)");
+  cudaSetDevice(c->device);
+  if (n < 0 || (n > 0 && (!u1 || !u2 || !nor || !flux || !speed)))
+    return fail(c, RKDG_ERR_INVALID, "invalid Riemann batch arguments");
+  CUDA_TRY(c, rkdg::launch_riemann_batch(c->dim, c->precision == RKDG_FP64 ? 0 : 1, n, u1, u2, nor, flux,
+                                         speed, c->gamma, c->cov, c->rs, c->avg, c->stream));
+  c->launches++;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return RKDG_OK;
+}
+
+long long rkdg_kernel_launches(rkdg_ctx* c) { return c ? c->launches : -1; }
+
+}  // extern "C"

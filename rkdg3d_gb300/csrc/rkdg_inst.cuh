@@ -1,0 +1,57 @@
+// Explicit instantiation helpers for the generic kernels (one translation
+// unit per geometry keeps the build parallel).
+#pragma once
+
+#include "rkdg_generic.cuh"
+#include "rkdg_launch.h"
+
+namespace rkdg {
+
+constexpr int kGenericBlock = 128;
+
+template <int G, int P>
+cudaError_t launch_rhs_t(int prec, const RhsParams& prm, const void* u, const void* ep,
+                         cudaStream_t st) {
+  const int grid = (prm.ne + kGenericBlock - 1) / kGenericBlock;
+  if (prec == 0)
+    k_rhs_generic<G, P, double><<<grid, kGenericBlock, 0, st>>>(
+        prm, (const double*)u, *(const EpiParams<double>*)ep);
+  else
+    k_rhs_generic<G, P, float><<<grid, kGenericBlock, 0, st>>>(
+        prm, (const float*)u, *(const EpiParams<float>*)ep);
+  return cudaGetLastError();
+}
+
+template <int G, int P>
+cudaError_t launch_limit_t(int mode, const LimParams& prm, void* u, float* ulo, cudaStream_t st) {
+  const int grid = (prm.ne + kGenericBlock - 1) / kGenericBlock;
+  if (mode == 0)
+    k_limit_generic<G, P, double, false><<<grid, kGenericBlock, 0, st>>>(prm, (double*)u, nullptr);
+  else if (mode == 1)
+    k_limit_generic<G, P, float, false><<<grid, kGenericBlock, 0, st>>>(prm, (float*)u, nullptr);
+  else
+    k_limit_generic<G, P, float, true><<<grid, kGenericBlock, 0, st>>>(prm, (float*)u, ulo);
+  return cudaGetLastError();
+}
+
+template <int G, int P>
+cudaError_t launch_means_t(int mode, int ne, long long ndofs, const RefTables* tab, const void* u,
+                           const float* ulo, double* means, cudaStream_t st) {
+  const int grid = (ne + kGenericBlock - 1) / kGenericBlock;
+  if (mode == 0)
+    k_means_generic<G, P, double><<<grid, kGenericBlock, 0, st>>>(ne, ndofs, tab, (const double*)u,
+                                                                  nullptr, means);
+  else
+    k_means_generic<G, P, float><<<grid, kGenericBlock, 0, st>>>(
+        ne, ndofs, tab, (const float*)u, mode == 2 ? ulo : nullptr, means);
+  return cudaGetLastError();
+}
+
+#define RKDG_INSTANTIATE(G, P)                                                                 \
+  template cudaError_t launch_rhs_t<G, P>(int, const RhsParams&, const void*, const void*,     \
+                                          cudaStream_t);                                       \
+  template cudaError_t launch_limit_t<G, P>(int, const LimParams&, void*, float*, cudaStream_t); \
+  template cudaError_t launch_means_t<G, P>(int, int, long long, const RefTables*, const void*, \
+                                            const float*, double*, cudaStream_t);
+
+}  // namespace rkdg

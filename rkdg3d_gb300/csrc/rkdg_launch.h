@@ -1,0 +1,45 @@
+// Kernel launchers (host-callable), implemented in the .cu files.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "rkdg_common.h"
+
+namespace rkdg {
+
+bool generic_supported(int geom, int p);
+// prec: 0 = FP64, 1 = FP32.  ep points to EpiParams<double> or EpiParams<float>.
+cudaError_t launch_rhs(int geom, int p, int prec, const RhsParams& prm, const void* u,
+                       const void* ep, cudaStream_t st);
+// mode: 0 = double in place, 1 = float in place, 2 = float pair (u = hi, ulo = lo)
+cudaError_t launch_limit(int geom, int p, int mode, const LimParams& prm, void* u, float* ulo,
+                         cudaStream_t st);
+// mode: 0 = double, 1 = float, 2 = float pair
+cudaError_t launch_means(int geom, int p, int mode, int ne, long long ndofs,
+                         const RefTables* tab, const void* u, const float* ulo, double* means,
+                         cudaStream_t st);
+
+cudaError_t launch_riemann_batch(int dim, int prec, int n, const double* u1, const double* u2,
+                                 const double* nor, double* flux, double* speed, double gamma,
+                                 double covolume, int rs, int avg, cudaStream_t st);
+cudaError_t launch_split(long long n, const double* x, float* hi, float* lo, cudaStream_t st);
+cudaError_t launch_join(long long n, const float* hi, const float* lo, double* x,
+                        cudaStream_t st);
+cudaError_t launch_to_float(long long n, const double* x, float* y, cudaStream_t st);
+cudaError_t launch_copy_f(long long n, const float* x, float* y, cudaStream_t st);
+// per-block partial sums of sum_e w_e * sum_j wmean_j u[k][e][j]  -> partial[k][block]
+cudaError_t launch_totals(int nd, int neq, int ne, long long ndofs, const RefTables* tab,
+                          const double* wdet, const double* u, double* partial, int nblocks,
+                          cudaStream_t st);
+
+// Template launch helpers shared by the per-geometry translation units.
+template <int G, int P>
+cudaError_t launch_rhs_t(int prec, const RhsParams& prm, const void* u, const void* ep,
+                         cudaStream_t st);
+template <int G, int P>
+cudaError_t launch_limit_t(int mode, const LimParams& prm, void* u, float* ulo, cudaStream_t st);
+template <int G, int P>
+cudaError_t launch_means_t(int mode, int ne, long long ndofs, const RefTables* tab, const void* u,
+                           const float* ulo, double* means, cudaStream_t st);
+
+}  // namespace rkdg

@@ -1,0 +1,342 @@
+// Device-side Euler physics and approximate Riemann solvers (sm_103a).
+//
+// Pointwise restatement of src/physics/physics.cpp and src/riemannsolvers/
+// for compile-time dimension DIM and arithmetic type R (double for the plain
+// FP64 path, float for the FP32-bulk path).  In the FP32 path the pressure is
+// recovered in FP64 whenever internal energy loses more than three digits to
+// cancellation (near vacuum / strong shocks).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+namespace rkdg {
+
+template <typename R>
+__device__ __forceinline__ R rsqrt_(R x) {
+  return sqrt(x);
+}
+
+// ComputePressure (physics.cpp:101-112), covolume EoS.
+template <int DIM, typename R>
+__device__ __forceinline__ R pressure(const R* s, R gamma, R b) {
+  const R den = s[0];
+  R v2 = R(0);
+#pragma unroll
+  for (int d = 0; d < DIM; d++) v2 += s[1 + d] * s[1 + d];
+  v2 /= den;
+  const R ie = s[1 + DIM] - R(0.5) * v2;
+  if constexpr (std::is_same<R, float>::value) {
+    if (fabsf(ie) < 1e-3f * fabsf(s[1 + DIM])) {
+      double v2d = 0.0;
+#pragma unroll
+      for (int d = 0; d < DIM; d++) v2d += (double)s[1 + d] * (double)s[1 + d];
+      v2d /= (double)den;
+      return (float)(((double)gamma - 1.0) * ((double)s[1 + DIM] - 0.5 * v2d) /
+                     (1.0 - (double)den * (double)b));
+    }
+  }
+  return (gamma - R(1)) * ie / (R(1) - den * b);
+}
+
+// ComputeSoundSpeed (physics.cpp:134-140)
+template <int DIM, typename R>
+__device__ __forceinline__ R sound_speed_p(const R* s, R p, R gamma, R b) {
+  const R den = s[0];
+  return sqrt(gamma * p / den / (R(1) - den * b));
+}
+
+// StateIsPhysical (physics.cpp:6-50): covolume-aware pressure.
+template <int DIM, typename R>
+__device__ __forceinline__ bool state_is_physical(const R* s, R gamma, R b) {
+  const R den = s[0];
+  const R e = s[1 + DIM];
+  if (den < R(0) || den != den) return false;
+  if (e <= R(0) || e != e) return false;
+  const R p = pressure<DIM>(s, gamma, b);
+  if (p <= R(0) || p != p) return false;
+  return true;
+}
+
+// StateIsPhysicalSay (physics.cpp:53-97): perfect-gas pressure (quirk Q10).
+template <int DIM, typename R>
+__device__ __forceinline__ bool state_is_physical_say(const R* s, R gamma) {
+  const R den = s[0];
+  const R e = s[1 + DIM];
+  if (den < R(0) || den != den) return false;
+  if (e <= R(0) || e != e) return false;
+  R v2 = R(0);
+#pragma unroll
+  for (int i = 0; i < DIM; i++) v2 += s[1 + i] * s[1 + i];
+  v2 /= den;
+  const R p = (gamma - R(1)) * (e - R(0.5) * v2);
+  if (p <= R(0) || p != p) return false;
+  return true;
+}
+
+// ComputeMaxCharSpeed (physics.cpp:252-266)
+template <int DIM, typename R>
+__device__ __forceinline__ R max_char_speed(const R* s, R gamma, R b) {
+  const R den = s[0];
+  R v2 = R(0);
+#pragma unroll
+  for (int d = 0; d < DIM; d++) v2 += s[1 + d] * s[1 + d];
+  v2 /= den;
+  const R p = pressure<DIM>(s, gamma, b);
+  const R c = sound_speed_p<DIM>(s, p, gamma, b);
+  return sqrt(v2 / den) + c;
+}
+
+// ComputeFlux (physics.cpp:143-168): F[k][d]; also returns |u|+c at the node
+// (FE_Evolution::GetFlux, fe_evolution.cpp:219-245).
+template <int DIM, typename R>
+__device__ __forceinline__ R flux_and_speed(const R* s, R F[DIM + 2][DIM], R gamma, R b) {
+  const R den = s[0];
+  const R inv = R(1) / den;
+  R v2 = R(0);
+#pragma unroll
+  for (int d = 0; d < DIM; d++) v2 += s[1 + d] * s[1 + d];
+  const R pres = pressure<DIM>(s, gamma, b);
+#pragma unroll
+  for (int d = 0; d < DIM; d++) {
+    F[0][d] = s[1 + d];
+#pragma unroll
+    for (int i = 0; i < DIM; i++) F[1 + i][d] = s[1 + i] * s[1 + d] * inv;
+    F[1 + d][d] += pres;
+  }
+  const R H = (s[1 + DIM] + pres) * inv;
+#pragma unroll
+  for (int d = 0; d < DIM; d++) F[1 + DIM][d] = s[1 + d] * H;
+  const R c = sqrt(gamma * pres * inv / (R(1) - den * b));
+  return sqrt(v2 * inv * inv) + c;
+}
+
+// ComputeFluxDotN (physics.cpp:171-195)
+template <int DIM, typename R>
+__device__ __forceinline__ void flux_dot_n(const R* s, const R* n, R* fn, R p) {
+  const R den = s[0];
+  R dvn = R(0);
+#pragma unroll
+  for (int d = 0; d < DIM; d++) dvn += s[1 + d] * n[d];
+  fn[0] = dvn;
+#pragma unroll
+  for (int d = 0; d < DIM; d++) fn[1 + d] = dvn * s[1 + d] / den + p * n[d];
+  const R H = (s[1 + DIM] + p) / den;
+  fn[1 + DIM] = dvn * H;
+}
+
+// ComputeFluxF (physics.cpp:198-231): x-flux of a rotated state.
+template <int DIM, typename R>
+__device__ __forceinline__ void flux_F(const R* s, R* f, R p) {
+  f[0] = s[1];
+  f[1] = s[1] * s[1] / s[0] + p;
+#pragma unroll
+  for (int d = 1; d < DIM; d++) f[d + 1] = s[1] * s[d + 1] / s[0];
+  const R H = (s[1 + DIM] + p) / s[0];
+  f[1 + DIM] = s[1] * H;
+}
+
+// RiemannSolver::Rotate / InverseRotate (rs_basic.cpp:11-67), including the
+// degenerate branch at |cos psi| <= 1e-6 (quirk Q14).
+template <int DIM, typename R>
+__device__ __forceinline__ void rotate(R* s, const R* n) {
+  R* m = s + 1;
+  if constexpr (DIM == 2) {
+    const R mx = n[0] * m[0] + n[1] * m[1];
+    const R my = -n[1] * m[0] + n[0] * m[1];
+    m[0] = mx;
+    m[1] = my;
+  } else {
+    const R sp = n[2];
+    const R cp = sqrt(R(1) - sp * sp);
+    const bool ok = fabs(cp) > R(1e-6);
+    const R st = ok ? n[1] / cp : R(1);
+    const R ct = ok ? n[0] / cp : R(0);
+    const R mx = cp * ct * m[0] + cp * st * m[1] + sp * m[2];
+    const R my = -st * m[0] + ct * m[1];
+    const R mz = -sp * ct * m[0] - sp * st * m[1] + cp * m[2];
+    m[0] = mx;
+    m[1] = my;
+    m[2] = mz;
+  }
+}
+template <int DIM, typename R>
+__device__ __forceinline__ void inverse_rotate(R* s, const R* n) {
+  R* m = s + 1;
+  if constexpr (DIM == 2) {
+    const R mx = n[0] * m[0] - n[1] * m[1];
+    const R my = n[1] * m[0] + n[0] * m[1];
+    m[0] = mx;
+    m[1] = my;
+  } else {
+    const R sp = n[2];
+    const R cp = sqrt(R(1) - sp * sp);
+    const bool ok = fabs(cp) > R(1e-6);
+    const R st = ok ? n[1] / cp : R(1);
+    const R ct = ok ? n[0] / cp : R(0);
+    const R mx = cp * ct * m[0] - st * m[1] - sp * ct * m[2];
+    const R my = cp * st * m[0] + ct * m[1] - sp * st * m[2];
+    const R mz = sp * m[0] + cp * m[2];
+    m[0] = mx;
+    m[1] = my;
+    m[2] = mz;
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ R powr(R a, R e) {
+  return pow(a, e);
+}
+
+// Wave-speed estimates on rotated states: TRRS ComputeToroCharSpeeds
+// (physics.cpp:309-350) or Einfeldt ComputeEinfeldtCharSpeeds (269-296).
+// Only lambda[0] and lambda[dim+1] are used by the solvers.
+template <int DIM, typename R>
+__device__ __forceinline__ void wave_speeds(const R* s1, const R* s2, R p1, R p2, R gamma, R b,
+                                            int avg, R& SL, R& SR) {
+  const R cL = sound_speed_p<DIM>(s1, p1, gamma, b);
+  const R cR = sound_speed_p<DIM>(s2, p2, gamma, b);
+  if (avg == 1) {
+    const R ruL = s1[1], ruR = s2[1];
+    const R uL = ruL / s1[0], uR = ruR / s2[0];
+    const R sL = sqrt(s1[0]), sR = sqrt(s2[0]);
+    const R sum = sL + sR;
+    const R eta2 = R(0.5) * sL * sR / ((sL + sR) * (sL + sR));
+    const R uav = (ruL / sL + ruR / sR) / sum;
+    const R cav = sqrt((sL * cL * cL + sR * cR * cR) / sum + eta2 * (uR - uL) * (uR - uL));
+    SL = uav - cav;
+    SR = uav + cav;
+    return;
+  }
+  const R uL = s1[1] / s1[0], uR = s2[1] / s2[0];
+  const R z = R(0.5) * (gamma - R(1)) / gamma;
+  const R pStar = powr(
+      (cL + cR - R(0.5) * (gamma - R(1)) * (uR - uL)) / (cL / powr(p1, z) + cR / powr(p2, z)),
+      R(1) / z);
+  const R qL = pStar > p1 ? sqrt(R(1) + R(0.5) * (gamma + R(1)) * (pStar / p1 - R(1)) / gamma)
+                          : R(1);
+  const R qR = pStar > p2 ? sqrt(R(1) + R(0.5) * (gamma + R(1)) * (pStar / p2 - R(1)) / gamma)
+                          : R(1);
+  SL = uL - qL * cL;
+  SR = uR + qR * cR;
+}
+
+// RiemannSolver*::Eval (rs_rusanov.cpp:6-40, rs_llf.cpp:6-37, rs_hll.cpp:6-50,
+// rs_hllc.cpp:71-161).  s1, s2 are working copies (rotated in place, as the
+// reference does through const_cast); n is the unit normal from side 1 to
+// side 2.  Returns the solver's wave speed, or -1 for a non-physical state.
+template <int DIM, typename R>
+__device__ __forceinline__ R riemann(R* s1, R* s2, const R* n, R* flux, R gamma, R b, int rs,
+                                     int avg) {
+  constexpr int NEQ = DIM + 2;
+  if (!state_is_physical_say<DIM>(s1, gamma)) return R(-1);
+  if (!state_is_physical_say<DIM>(s2, gamma)) return R(-1);
+  if (rs == 0) {
+    const R p1 = pressure<DIM>(s1, gamma, b);
+    const R p2 = pressure<DIM>(s2, gamma, b);
+    R v1 = R(0), v2 = R(0);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      v1 += s1[1 + d] * s1[1 + d];
+      v2 += s2[1 + d] * s2[1 + d];
+    }
+    const R e1 = sqrt(v1 / s1[0] / s1[0]) + sound_speed_p<DIM>(s1, p1, gamma, b);
+    const R e2 = sqrt(v2 / s2[0] / s2[0]) + sound_speed_p<DIM>(s2, p2, gamma, b);
+    const R maxE = e1 > e2 ? e1 : e2;
+    R f1[NEQ], f2[NEQ];
+    flux_dot_n<DIM>(s1, n, f1, p1);
+    flux_dot_n<DIM>(s2, n, f2, p2);
+    R nm = R(0);
+#pragma unroll
+    for (int i = 0; i < DIM; i++) nm += n[i] * n[i];
+    nm = sqrt(nm);
+#pragma unroll
+    for (int i = 0; i < NEQ; i++)
+      flux[i] = R(0.5) * (f1[i] + f2[i]) / nm - R(0.5) * maxE * (s2[i] - s1[i]);
+    return maxE;
+  }
+  rotate<DIM>(s1, n);
+  rotate<DIM>(s2, n);
+  const R p1 = pressure<DIM>(s1, gamma, b);
+  const R p2 = pressure<DIM>(s2, gamma, b);
+  R f1[NEQ], f2[NEQ];
+  flux_F<DIM>(s1, f1, p1);
+  flux_F<DIM>(s2, f2, p2);
+  R SL, SR;
+  wave_speeds<DIM>(s1, s2, p1, p2, gamma, b, avg, SL, SR);
+  R ret;
+  if (rs == 1) {
+    const R maxE = fmax(fabs(SL), fabs(SR));
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) flux[i] = R(0.5) * (f1[i] + f2[i]) - R(0.5) * maxE * (s2[i] - s1[i]);
+    ret = maxE;
+  } else if (rs == 2) {
+    const R maxE = fmax(fabs(SL), fabs(SR));
+    if (SL >= R(0)) {
+#pragma unroll
+      for (int i = 0; i < NEQ; ++i) flux[i] = f1[i];
+    } else if (SR <= R(0)) {
+#pragma unroll
+      for (int i = 0; i < NEQ; ++i) flux[i] = f2[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < NEQ; ++i)
+        flux[i] = (SR * f1[i] - SL * f2[i] + SL * SR * (s2[i] - s1[i])) / (SR - SL);
+    }
+    ret = maxE;
+  } else {
+    const R maxE = SL > SR ? SL : SR;
+    if (SL >= R(0)) {
+#pragma unroll
+      for (int i = 0; i < NEQ; ++i) flux[i] = f1[i];
+    } else if (SR <= R(0)) {
+#pragma unroll
+      for (int i = 0; i < NEQ; ++i) flux[i] = f2[i];
+    } else {
+      const R cL = SL - s1[1] / s1[0];
+      const R cR = SR - s2[1] / s2[0];
+      const R sStar = (p2 - p1 + s1[1] * cL - s2[1] * cR) / (s1[0] * cL - s2[0] * cR);
+      const bool left = sStar > R(0);
+      const R* st = left ? s1 : s2;
+      const R* fK = left ? f1 : f2;
+      const R pK = left ? p1 : p2;
+      const R SK = left ? SL : SR;
+      const R cK = left ? cL : cR;
+      const R rhoL = st[0];
+      const R extra = SK * (pK + rhoL * cK * (sStar - st[1] / st[0]));
+      const R inv = R(1) / (SK - sStar);
+#pragma unroll
+      for (int i = 0; i < NEQ; ++i) {
+        const R Di = (i == 1) ? R(1) : ((i == DIM + 1) ? sStar : R(0));
+        flux[i] = (sStar * (st[i] * SK - fK[i]) + Di * extra) * inv;
+      }
+    }
+    ret = maxE;
+  }
+  inverse_rotate<DIM>(flux, n);
+  return ret;
+}
+
+// computeRightState of the boundary integrators.
+template <int DIM, typename R>
+__device__ __forceinline__ void right_state(int type, const double* st, const R* s1, R* s2,
+                                            const R* n) {
+  constexpr int NEQ = DIM + 2;
+#pragma unroll
+  for (int i = 0; i < NEQ; ++i) s2[i] = s1[i];
+  if (type == 0 || type == 4) {  // slip / wall
+    rotate<DIM>(s2, n);
+    s2[1] = -s2[1];
+    inverse_rotate<DIM>(s2, n);
+  } else if (type == 2) {  // fixed state in the rotated frame (quirk Q12)
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) s2[i] = (R)st[i];
+    inverse_rotate<DIM>(s2, n);
+  } else if (type == 3) {  // supersonic inlet, global frame
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) s2[i] = (R)st[i];
+  }
+}
+
+}  // namespace rkdg

@@ -1,0 +1,180 @@
+"""GPU parity against the CPU oracle through the C ABI (FP64 path).
+
+Tolerance: per-RHS normwise relative L1 error <= 1e-12 (the plain FP64 path
+contract); limiter and step parity <= 1e-12; full runs <= 1e-9 (thousands of
+limited stages with data-dependent branches).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle.refcpu import Oracle
+from rkdg3d_gb300 import cases
+from rkdg3d_gb300 import mesh as M
+from rkdg3d_gb300.solver import (AVG_EINFELDT, AVG_TRRS, BC_FIXED_ROTATED, BC_OPEN, BC_SLIP,
+                                 BC_SUPERSONIC_INLET, FUN_BJ, FUN_MICHALAK, FUN_VENKATAKRISHNAN,
+                                 IND_BJ, IND_EVERYWHERE, IND_NOWHERE, LIM_FINDIFF, LIM_MULTI,
+                                 RS_HLL, RS_HLLC, RS_LLF, RS_RUSANOV, TABLEAU_REFERENCE_RK3,
+                                 TABLEAU_SSPRK3, Context)
+from tests.helpers import periodic_case, random_state, rel_l1, walled_case
+
+pytestmark = pytest.mark.gpu
+
+RHS_TOL = 1e-12
+
+
+def pair(case):
+    ctx = Context(case.mesh, case.order, device=0)
+    cases.configure_context(case, ctx)
+    orc = Oracle(case.mesh, case.order)
+    cases.configure_oracle(case, orc)
+    return ctx, orc
+
+
+def dev(x):
+    return torch.tensor(x, dtype=torch.float64, device="cuda:0")
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("rs", [RS_RUSANOV, RS_LLF, RS_HLL, RS_HLLC])
+@pytest.mark.parametrize("avg", [AVG_TRRS, AVG_EINFELDT])
+@pytest.mark.parametrize("cov", [0.0, 0.01])
+def test_riemann_batch(cuda, dim, rs, avg, cov):
+    case = periodic_case(M.GEOM_CUBE if dim == 3 else M.GEOM_SQUARE, 3, 1, rs, avg, covolume=cov)
+    ctx, orc = pair(case)
+    rng = np.random.default_rng(dim * 100 + rs * 10 + avg)
+    n = 4096
+    neq = dim + 2
+
+    def states():
+        rho = rng.uniform(0.2, 2.0, n)
+        vel = rng.uniform(-2, 2, (dim, n))
+        p = rng.uniform(0.1, 3.0, n)
+        return cases.conservative([rho, *vel, p], 1.4, cov).reshape(neq, n).T.copy()
+
+    u1, u2 = states(), states()
+    nor = rng.normal(size=(n, dim))
+    nor[: n // 8] = 0.0
+    nor[: n // 8, dim - 1] = np.where(rng.uniform(size=n // 8) < 0.5, -1.0, 1.0)  # axis normals
+    nor /= np.linalg.norm(nor, axis=1, keepdims=True)
+    f_ref, s_ref = orc.riemann(u1, u2, nor)
+    flux = torch.empty((n, neq), dtype=torch.float64, device="cuda")
+    sp = torch.empty(n, dtype=torch.float64, device="cuda")
+    ctx.riemann_batch(dev(u1), dev(u2), dev(nor), flux, sp)
+    f = flux.cpu().numpy()
+    s = sp.cpu().numpy()
+    assert np.all((s < 0) == (s_ref < 0))
+    ok = s_ref >= 0
+    assert np.allclose(s[ok], s_ref[ok], rtol=1e-12, atol=1e-13)
+    scale = np.abs(f_ref[ok]).max(axis=1, keepdims=True) + 1e-300
+    assert np.abs(f[ok] - f_ref[ok]).max() / scale.max() < 1e-12
+    assert (np.abs(f[ok] - f_ref[ok]) / scale).max() < 1e-11
+
+
+@pytest.mark.parametrize("rs", [RS_RUSANOV, RS_LLF, RS_HLL, RS_HLLC])
+@pytest.mark.parametrize("geom,order,n", [(M.GEOM_SQUARE, 1, 6), (M.GEOM_SQUARE, 2, 5),
+                                          (M.GEOM_SQUARE, 3, 4), (M.GEOM_CUBE, 1, 3),
+                                          (M.GEOM_CUBE, 2, 3)])
+def test_rhs_periodic(cuda, rs, geom, order, n):
+    case = periodic_case(geom, n, order, rs, AVG_TRRS)
+    ctx, orc = pair(case)
+    x = random_state(ctx.node_coords(), seed=rs)
+    y_ref, m_ref = orc.rhs(x)
+    y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    m = ctx.rhs(dev(x), y)
+    assert rel_l1(y.cpu().numpy(), y_ref) < RHS_TOL
+    assert abs(m - m_ref) <= 1e-13 * m_ref
+
+
+@pytest.mark.parametrize("geom,order,n", [(M.GEOM_SQUARE, 1, 5), (M.GEOM_SQUARE, 2, 4),
+                                          (M.GEOM_TRIANGLE, 1, 5), (M.GEOM_TRIANGLE, 2, 4),
+                                          (M.GEOM_CUBE, 1, 3), (M.GEOM_CUBE, 2, 2)])
+@pytest.mark.parametrize("bc", [BC_SLIP, BC_OPEN, BC_FIXED_ROTATED, BC_SUPERSONIC_INLET])
+@pytest.mark.parametrize("rs,avg", [(RS_HLLC, AVG_EINFELDT), (RS_HLL, AVG_TRRS), (RS_RUSANOV, 0)])
+def test_rhs_walls(cuda, geom, order, n, bc, rs, avg):
+    case = walled_case(geom, n, order, rs, avg, covolume=0.005, bc=bc)
+    dim = case.dim
+    if bc in (BC_FIXED_ROTATED, BC_SUPERSONIC_INLET):
+        st = cases.supersonic_inlet_state(1.1, 0.3, -0.2, 0.1, 0.9, 1.4, dim)
+        case.bcs = [(a, bc, st) for a, _, _ in case.bcs]
+    ctx, orc = pair(case)
+    x = random_state(ctx.node_coords(), b=0.005, seed=7)
+    y_ref, m_ref = orc.rhs(x)
+    y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    m = ctx.rhs(dev(x), y)
+    assert rel_l1(y.cpu().numpy(), y_ref) < RHS_TOL
+    assert abs(m - m_ref) <= 1e-13 * abs(m_ref)
+
+
+def test_node_coords_match_oracle(cuda):
+    for geom, order in [(M.GEOM_SQUARE, 2), (M.GEOM_TRIANGLE, 2), (M.GEOM_CUBE, 2)]:
+        case = walled_case(geom, 3, order, RS_RUSANOV)
+        ctx, orc = pair(case)
+        assert np.allclose(ctx.node_coords(), orc.node_coords(), rtol=0, atol=1e-14)
+        assert abs(ctx.hmin() - orc.hmin()) < 1e-12
+
+
+def _limited_sod_state(orc, case, steps=30):
+    x = cases.project(case, orc.node_coords())
+    for _ in range(steps):
+        x, _ = orc.step(x, 4e-4)
+    return x
+
+
+@pytest.mark.parametrize("lim,ind,fun", [(LIM_MULTI, IND_BJ, FUN_BJ), (LIM_MULTI, IND_BJ, FUN_MICHALAK),
+                                         (LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN),
+                                         (LIM_FINDIFF, IND_BJ, FUN_MICHALAK),
+                                         (LIM_MULTI, IND_NOWHERE, FUN_MICHALAK),
+                                         (LIM_MULTI, IND_EVERYWHERE, FUN_MICHALAK)])
+def test_limiter_parity(cuda, lim, ind, fun):
+    case = cases.sod(nx=60, ny=3)
+    case.limiter = (lim, ind, fun, 1, 0)
+    ctx, orc = pair(case)
+    x = _limited_sod_state(orc, case)
+    means_ref = orc.means(x)
+    md = torch.empty(ctx.neq * ctx.ne, dtype=torch.float64, device="cuda")
+    ctx.cell_means(dev(x), md)
+    assert rel_l1(md.cpu().numpy(), means_ref) < 1e-14
+    xl_ref = orc.limit(x)
+    xd = dev(x)
+    ctx.limit(xd)
+    assert rel_l1(xd.cpu().numpy(), xl_ref) < 1e-12
+
+
+@pytest.mark.parametrize("tab", [TABLEAU_SSPRK3, TABLEAU_REFERENCE_RK3])
+def test_step_parity_sod(cuda, tab):
+    case = cases.sod(nx=60, ny=3, tableau=tab)
+    ctx, orc = pair(case)
+    x = _limited_sod_state(orc, case, steps=5)
+    x_ref, m_ref = orc.step(x, 3e-4)
+    xd = dev(x)
+    m = ctx.step(xd, 3e-4)
+    assert rel_l1(xd.cpu().numpy(), x_ref) < 1e-12
+    assert abs(m - m_ref) <= 1e-12 * m_ref
+
+
+def test_full_run_sod(cuda):
+    """Full limited run: density field at t_end equals the oracle's."""
+    case = cases.sod(nx=100, ny=4, t_end=0.1)
+    ctx, orc = pair(case)
+    x0 = cases.project(case, orc.node_coords())
+    x_ref, info_ref = orc.run(x0, case.t_end, case.cfl)
+    xd = dev(x0)
+    info = ctx.run(xd, case.t_end, case.cfl)
+    assert info["steps"] == info_ref["steps"]
+    nd = orc.ndofs
+    rho = xd.cpu().numpy()[:nd]
+    assert rel_l1(rho, x_ref[:nd]) < 1e-9
+    assert rel_l1(xd.cpu().numpy(), x_ref) < 1e-9
+
+
+def test_conservation_periodic_hex(cuda):
+    case = periodic_case(M.GEOM_CUBE, 4, 2, RS_HLLC)
+    case.tableau = TABLEAU_SSPRK3
+    ctx, _ = pair(case)
+    x = dev(random_state(ctx.node_coords(), seed=3, amp=0.1, vel=0.2))
+    t0 = ctx.totals(x)
+    for _ in range(10):
+        ctx.step(x, 2e-3)
+    t1 = ctx.totals(x)
+    assert np.all(np.abs(t1 - t0) <= 1e-13 * np.abs(t0).max())

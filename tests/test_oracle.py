@@ -1,0 +1,190 @@
+"""CPU tests of the oracle (no GPU): known-answer physics checks, MFEM-
+semantics restatements and the committed golden vectors."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle.refcpu import Oracle
+from rkdg3d_gb300 import cases
+from rkdg3d_gb300 import mesh as M
+from rkdg3d_gb300.solver import (AVG_EINFELDT, AVG_TRRS, BC_SLIP, FUN_MICHALAK, IND_BJ,
+                                 LIM_FINDIFF, LIM_MULTI, IND_NOWHERE, RS_HLL, RS_HLLC, RS_LLF,
+                                 RS_RUSANOV, TABLEAU_SSPRK3)
+from tests import exact_riemann
+from tests.golden.make_golden import golden_cases, initial_state
+from tests.helpers import periodic_case, random_state, rel_l1, walled_case
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
+
+
+def _oracle(case):
+    o = Oracle(case.mesh, case.order)
+    cases.configure_oracle(case, o)
+    return o
+
+
+def _flux(u, n, gamma=1.4, b=0.0):
+    dim = n.shape[-1]
+    rho = u[:, 0]
+    m = u[:, 1:1 + dim]
+    E = u[:, 1 + dim]
+    p = (gamma - 1) * (E - 0.5 * (m * m).sum(1) / rho) / (1 - rho * b)
+    mn = (m * n).sum(1)
+    out = np.zeros_like(u)
+    out[:, 0] = mn
+    out[:, 1:1 + dim] = mn[:, None] * m / rho[:, None] + p[:, None] * n
+    out[:, 1 + dim] = mn * (E + p) / rho
+    return out
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("rs", [RS_RUSANOV, RS_LLF, RS_HLL, RS_HLLC])
+@pytest.mark.parametrize("avg", [AVG_TRRS, AVG_EINFELDT])
+def test_riemann_consistency(dim, rs, avg):
+    """F(u, u, n) = F(u).n for every solver (face flux consistency)."""
+    case = periodic_case(M.GEOM_CUBE if dim == 3 else M.GEOM_SQUARE, 3, 1, rs, avg)
+    o = _oracle(case)
+    rng = np.random.default_rng(1)
+    n = 500
+    u = cases.conservative([rng.uniform(0.3, 2, n), *rng.uniform(-1, 1, (dim, n)),
+                            rng.uniform(0.2, 2, n)], 1.4, 0.0).reshape(dim + 2, n).T.copy()
+    nor = rng.normal(size=(n, dim))
+    nor /= np.linalg.norm(nor, axis=1, keepdims=True)
+    f, s = o.riemann(u, u.copy(), nor)
+    if rs != RS_HLLC:  # HLLC returns max(SL, SR), negative in supersonic reverse flow (Q2)
+        assert np.all(s > 0)
+    assert np.allclose(f, _flux(u, nor), rtol=1e-11, atol=1e-12)
+
+
+@pytest.mark.parametrize("rs", [RS_RUSANOV, RS_LLF, RS_HLL, RS_HLLC])
+def test_riemann_rotation_invariance_2d(rs):
+    """Rotating the frame rotates the momentum flux and leaves the rest."""
+    o = _oracle(periodic_case(M.GEOM_SQUARE, 3, 1, rs))
+    rng = np.random.default_rng(2)
+    n = 300
+    mk = lambda: cases.conservative([rng.uniform(0.3, 2, n), *rng.uniform(-1, 1, (2, n)),
+                                     rng.uniform(0.2, 2, n)], 1.4, 0.0).reshape(4, n).T.copy()
+    u1, u2 = mk(), mk()
+    nor = rng.normal(size=(n, 2))
+    nor /= np.linalg.norm(nor, axis=1, keepdims=True)
+    th = 0.7
+    R = np.array([[np.cos(th), -np.sin(th)], [np.sin(th), np.cos(th)]])
+    rot = lambda u: np.concatenate([u[:, :1], u[:, 1:3] @ R.T, u[:, 3:]], 1)
+    f, _ = o.riemann(u1, u2, nor)
+    fr, _ = o.riemann(rot(u1), rot(u2), nor @ R.T)
+    assert np.allclose(fr, rot(f), rtol=1e-10, atol=1e-11)
+
+
+@pytest.mark.parametrize("geom,order", [(M.GEOM_SQUARE, 1), (M.GEOM_SQUARE, 2),
+                                        (M.GEOM_TRIANGLE, 1), (M.GEOM_TRIANGLE, 2),
+                                        (M.GEOM_CUBE, 1), (M.GEOM_CUBE, 2)])
+@pytest.mark.parametrize("rs", [RS_RUSANOV, RS_HLLC])
+def test_free_stream_rest_state(geom, order, rs):
+    """A uniform state at rest in a slip-walled box has a zero right-hand side."""
+    case = walled_case(geom, 3, order, rs, bc=BC_SLIP)
+    o = _oracle(case)
+    X = o.node_coords()
+    one = np.ones(X.shape[1])
+    x = cases.conservative([1.3 * one] + [0 * one] * case.dim + [0.8 * one], 1.4, 0.0)
+    y, _ = o.rhs(x)
+    assert np.abs(y).max() < 1e-11
+
+
+@pytest.mark.parametrize("geom,order", [(M.GEOM_SQUARE, 1), (M.GEOM_SQUARE, 3), (M.GEOM_CUBE, 2)])
+def test_free_stream_periodic_uniform_flow(geom, order):
+    case = periodic_case(geom, 3, order, RS_HLLC)
+    o = _oracle(case)
+    X = o.node_coords()
+    one = np.ones(X.shape[1])
+    x = cases.conservative([one] + [0.3 * one] * case.dim + [one], 1.4, 0.0)
+    y, _ = o.rhs(x)
+    assert np.abs(y).max() < 1e-11
+
+
+@pytest.mark.parametrize("geom,order", [(M.GEOM_SQUARE, 2), (M.GEOM_CUBE, 1)])
+def test_discrete_conservation(geom, order):
+    """sum_e sum_j (int phi_j) dU_j/dt = 0 on a periodic mesh."""
+    case = periodic_case(geom, 4, order, RS_HLL)
+    o = _oracle(case)
+    x = random_state(o.node_coords(), seed=5, amp=0.1, vel=0.2)
+    y, _ = o.rhs(x)
+    d = o.totals(y)
+    assert np.abs(d).max() < 1e-13 * np.abs(o.totals(x)).max() * 1e2
+
+
+def test_gl_nodes_and_triangle_nodes():
+    """Node positions of DG_FECollection's Gauss-Legendre bases."""
+    m = M.quad_grid(1, 1)
+    o = Oracle(m, 1)
+    X = o.node_coords()
+    g = 0.5 * (1 - 1 / np.sqrt(3))
+    assert np.allclose(sorted(set(np.round(X[0], 14))), [g, 1 - g])
+    t = M.tri_grid(1, 1)
+    o = Oracle(t, 1)
+    X = o.node_coords()[:, :3]   # first triangle (0,0),(1,0),(1,1): x = xi + eta, y = eta
+    op = np.array([g, 1 - g])
+    w = 2 * op[0] + op[1]
+    ref = np.array([[op[0] / w, op[0] / w], [op[1] / w, op[0] / w], [op[0] / w, op[1] / w]])
+    phys = np.stack([ref[:, 0] + ref[:, 1], ref[:, 1]], 0)
+    assert np.allclose(X, phys, atol=1e-14)
+
+
+def test_sod_against_exact_solution():
+    """Q1 Sod (200 x 4, HLLC, limited) density is close to the exact solution."""
+    case = cases.sod(nx=200, ny=4, rsolver=RS_HLLC, averaging=AVG_TRRS, function=FUN_MICHALAK,
+                     tableau=TABLEAU_SSPRK3, t_end=0.2)
+    o = _oracle(case)
+    X = o.node_coords()
+    x0 = cases.project(case, X)
+    x, info = o.run(x0, case.t_end, case.cfl)
+    t = info["sum_dt"]
+    rho = x[:o.ndofs]
+    ex = exact_riemann.sample(X[0], t, 0.5, (1.0, 0.0, 1.0), (0.125, 0.0, 0.1))[0]
+    l1 = np.mean(np.abs(rho - ex))
+    assert l1 < 0.01, l1
+    assert np.all(rho > 0.1) and np.all(rho < 1.05)
+
+
+def test_sod_totals_conserved():
+    case = cases.sod(nx=50, ny=2, t_end=0.05)
+    o = _oracle(case)
+    x0 = cases.project(case, o.node_coords())
+    t0 = o.totals(x0)
+    x, _ = o.run(x0, case.t_end, case.cfl)
+    t1 = o.totals(x)
+    # mass and energy fluxes through the open ends are zero before the waves arrive
+    assert abs(t1[0] - t0[0]) < 1e-14 and abs(t1[3] - t0[3]) < 1e-14
+
+
+def test_limiter_nowhere_findiff_is_identity():
+    case = cases.sod(nx=20, ny=2)
+    case.limiter = (LIM_FINDIFF, IND_NOWHERE, FUN_MICHALAK, 1, 0)
+    o = _oracle(case)
+    x = random_state(o.node_coords(), seed=2)
+    assert np.array_equal(o.limit(x), x)
+
+
+def test_limiter_keeps_means():
+    case = cases.sod(nx=30, ny=2)
+    case.limiter = (LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 0)
+    o = _oracle(case)
+    x = random_state(o.node_coords(), seed=4)
+    m0 = o.means(x)
+    m1 = o.means(o.limit(x))
+    assert np.allclose(m0, m1, rtol=1e-13, atol=1e-14)
+
+
+@pytest.mark.parametrize("name", list(golden_cases()))
+def test_golden_vectors(name):
+    g = np.load(GOLDEN)
+    case, seed, dt = golden_cases()[name]
+    o = _oracle(case)
+    x = initial_state(case, o, seed)
+    assert np.array_equal(x, g[f"{name}/x"])
+    y, mcs = o.rhs(x)
+    assert rel_l1(y, g[f"{name}/rhs"]) < 1e-14
+    assert mcs == pytest.approx(g[f"{name}/mcs"][0], rel=1e-15)
+    assert rel_l1(o.limit(x), g[f"{name}/limited"]) < 1e-14
+    xs, _ = o.step(x, dt)
+    assert rel_l1(xs, g[f"{name}/step"]) < 1e-14
