@@ -1,0 +1,354 @@
+"""Benchmark: DOF-stage updates/s of the RKDG hot path on one GB300.
+
+Workload (one GPU): the 3D periodic acoustic pulse on a 64^3 hexahedral mesh,
+DG Q2 (27 nodes x 5 variables per element, N = 35,389,440 unknowns), Rusanov
+flux, no limiter, SSP-RK3 with dt fixed from CFL 0.2 at t = 0.  One bench
+"step" is one Runge-Kutta step (3 stages) over the whole mesh; the metric is
+N x stages / second.  Inputs are larger than L2 (the FP64 state alone is
+283 MB), so no L2 flush is needed between steps.
+
+Arms:
+  default            this implementation: FP32-bulk path (value) next to the
+                     plain FP64 path, error of the former against the latter,
+                     roofline of the stage kernel, end-to-end number through
+                     the C ABI with host buffers, and the CPU oracle timed on
+                     the host cores (cpu_baseline).
+  --impl reference   the reference's CPU algorithm (the FP64 oracle, all
+                     host threads) on the same workload, bounded sample.
+
+Multi-GPU (torchrun, N > 1): replicas only — every rank solves its own copy,
+no collective on the data path; value = total units / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-stage updates/s, mixed vs plain FP64 on 1 GB300 at <=1e-6 rel L1 err"
+UNIT = "DOF-stage updates/s"
+STAGES = 3
+
+
+def workload_config(case, n_elem_side):
+    return {
+        "workload": f"periodic acoustic pulse {n_elem_side}^3 hex Q2 (27 nodes x 5 vars), Rusanov, "
+                    "no limiter, SSP-RK3, dt fixed from CFL 0.2",
+        "elements": case.mesh.num_elements,
+        "unknowns": None,
+        "stages_per_step": STAGES,
+        "l2_policy": "inputs larger than L2 (FP64 state 283 MB > 129 MB L2); no flush",
+    }
+
+
+def algorithmic_bytes_per_step(N, ne, precision):
+    """Bytes one SSP-RK3 step must move at stored widths:
+    FP32-bulk: stage 0 reads x_hi, x_lo, writes k0, y1 (16N); stage 1 reads
+    y1, x_hi, x_lo, k0, writes k1, y2 (24N); stage 2 reads y2, k0, k1, x_hi,
+    x_lo, writes x_hi, x_lo (28N).  FP64: stage 0 reads x, writes k0, y1
+    (24N); stage 1 reads y1, x, k0, writes k1, y2 (40N); stage 2 reads y2, x,
+    k0, k1, writes x (40N).  Plus per stage the element and face tables."""
+    if precision == "fp32":
+        state = 68 * N
+        tables = ne * (10 * 4 + 6 * (4 * 4 + 4 + 4))
+    else:
+        state = 104 * N
+        tables = ne * (10 * 8 + 6 * (4 * 8 + 4 + 4))
+    return state + STAGES * tables
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                smax.append(float(parts[2].split()[0]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl != "reference" else "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier_max(val, world):
+    if world == 1:
+        return val
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([val], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.barrier()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def oracle_rate(case, x0, dt, steps, threads):
+    """Reference CPU algorithm (FP64 oracle) on the full mesh for `steps`
+    Runge-Kutta steps; returns (rate, seconds)."""
+    from oracle import refcpu
+    refcpu.set_threads(threads)
+    orc = refcpu.Oracle(case.mesh, case.order)
+    from rkdg3d_gb300 import cases
+    cases.configure_oracle(case, orc)
+    x = x0.copy()
+    t0 = time.perf_counter()
+    x, _ = orc.run(x, 1e30, dt0=dt, dt_mode=2, max_steps=steps)
+    sec = time.perf_counter() - t0
+    return orc.n * STAGES * steps / sec, sec
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from rkdg3d_gb300 import cases
+    case = cases.pulse3d(n=args.n, order=2, steps=args.steps, cfl=0.2)
+    from oracle import refcpu
+    orc = refcpu.Oracle(case.mesh, case.order)
+    cases.configure_oracle(case, orc)
+    x0 = cases.project(case, orc.node_coords())
+    dt = 0.2 * orc.hmin() / orc.face_speed(x0) / 5.0
+    threads = os.cpu_count() or 1
+    # bounded sample: a one-step probe sizes the timed sample to ~60 s
+    _, probe = oracle_rate(case, x0, dt, 1, threads)
+    for _ in range(max(0, min(args.warmup, 1) - 1)):
+        oracle_rate(case, x0, dt, 1, threads)
+    ksteps = int(max(1, min(args.steps, 60.0 // max(probe, 1e-3))))
+    rate, sec = oracle_rate(case, x0, dt, ksteps, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / ksteps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": dict(workload_config(case, args.n), unknowns=orc.n),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{ksteps} full RK steps of the {args.n}^3 mesh (FP64 oracle, "
+                                   f"restatement of the reference CPU path; reference not buildable)"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    from rkdg3d_gb300 import cases
+    from rkdg3d_gb300.solver import FP32_BULK, FP64, Context
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    case = cases.pulse3d(n=args.n, order=2, steps=args.steps, cfl=0.2)
+    stream = torch.cuda.current_stream(dev)
+
+    def make(prec):
+        ctx = Context(case.mesh, case.order, device=local, precision=prec)
+        cases.configure_context(case, ctx)
+        ctx.set_stream(stream.cuda_stream)
+        return ctx
+
+    ctx32 = make(FP32_BULK)
+    X = ctx32.node_coords()
+    x0 = cases.project(case, X)
+    N = ctx32.n
+    x0d = torch.tensor(x0, dtype=torch.float64, device=dev)
+    mcs = ctx32.face_speed(x0d)
+    dt = case.cfl * ctx32.hmin() / mcs / (2 * case.order + 1)
+
+    def timed_run(ctx, steps, warm):
+        assert steps > 0
+        x = x0d.clone()
+        if warm > 0:
+            ctx.run(x, 1e30, dt0=dt, dt_mode=2, max_steps=warm)
+        torch.cuda.synchronize(dev)
+        x = x0d.clone()
+        l0 = ctx.launches()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.run(x, 1e30, dt0=dt, dt_mode=2, max_steps=steps)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return x, e0.elapsed_time(e1) / 1e3, ctx.launches() - l0
+
+    # FP32-bulk (the headline) with clocks sampled during the timed region
+    with ClockSampler(local) as clk:
+        x32, sec32, launches = timed_run(ctx32, args.steps, args.warmup)
+    clocks = clk.summary()
+    sec32 = barrier_max(sec32, world)
+    value = world * N * STAGES * args.steps / sec32
+
+    # plain FP64 path on a shorter window (it runs at the FP64 issue rate)
+    ctx64 = make(FP64)
+    k64 = max(1, min(args.steps, args.fp64_steps))
+    x64, sec64, _ = timed_run(ctx64, k64, min(args.warmup, 3))
+    value64 = world * N * STAGES * k64 / barrier_max(sec64, world)
+    # error of the FP32-bulk path against the FP64 path after the same steps
+    x32b, _, _ = timed_run(ctx32, k64, 0)
+    a = x32b.cpu().numpy()
+    b = x64.cpu().numpy()
+    nd = ctx32.ndofs
+    rho_a, rho_b = a[:nd], b[:nd]
+    E_a, E_b = a[-nd:], b[-nd:]
+    err = {
+        "steps_compared": k64,
+        "rho_rel_l1": float(np.abs(rho_a - rho_b).sum() / np.abs(rho_b).sum()),
+        "rho_linf": float(np.abs(rho_a - rho_b).max()),
+        "E_rel_l1": float(np.abs(E_a - E_b).sum() / np.abs(E_b).sum()),
+        "E_linf": float(np.abs(E_a - E_b).max()),
+    }
+    del ctx64
+
+    # end to end through the C ABI from pinned host memory
+    xh = torch.tensor(x0, dtype=torch.float64).pin_memory()
+    out = torch.empty_like(xh).pin_memory()
+    xd = torch.empty(N, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    xd.copy_(xh, non_blocking=True)
+    ctx32.run(xd, 1e30, dt0=dt, dt_mode=2, max_steps=args.steps)
+    out.copy_(xd, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    sec_e2e = barrier_max(time.perf_counter() - t0, world)
+    e2e = {"value": world * N * STAGES * args.steps / sec_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": 8 * N / args.steps, "d2h_bytes_per_step": 8 * N / args.steps,
+           "note": "state uploaded once and downloaded once per job of `steps` RK steps; "
+                   "call = rkdg_run through the ctypes C ABI"}
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    bps = algorithmic_bytes_per_step(N, ctx32.ne, "fp32")
+    ms_step = 1e3 * sec32 / args.steps
+    achieved = bps / (ms_step / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": args.traffic_per_launch,
+            "peak_source": peak_src, "kernel": "k_rhs_hex_sf (stage kernel)",
+            "algorithmic_bytes_per_launch": bps / STAGES}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        try:
+            _, probe = oracle_rate(case, x0, dt, 1, threads)
+            ks = int(max(1, min(5, 20.0 // max(probe, 1e-3))))
+            rate, sec = oracle_rate(case, x0, dt, ks, threads)
+            cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"{ks} RK steps of the full {args.n}^3 mesh, FP64 oracle "
+                             f"({sec:.1f} s)"}
+        except Exception as exc:  # pragma: no cover
+            cpu = {"value": None, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"failed: {exc}"}
+
+    if rank == 0:
+        cfg = workload_config(case, args.n)
+        cfg["unknowns"] = N
+        cfg["precision"] = "fp32-bulk (float-pair conserved state)"
+        cfg["parallelism"] = f"replicas x{world}"
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": cfg,
+            "fp64": {"value": value64, "unit": UNIT, "steps": k64,
+                     "ms_per_step": 1e3 * sec64 / k64, "speedup_mixed_vs_fp64": value / value64},
+            "error_vs_fp64": err,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=64, help="elements per side")
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--traffic-per-launch", type=float, default=None,
+                    help="DRAM bytes per stage launch from an ncu capture (profiles/)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -54,6 +54,12 @@ struct RefTables {
   double d1[8][8];               // d1[j][m] = w_m l_j'(x_m) (collocated volume)
   double minv1[8][8];            // 1D reference inverse mass (exact)
   double lquad[2][8];            // 1D basis at the 2 limiter GL points
+  double w1[8];                  // 1D GL node weights
+  // hexahedra: per local face, normal axis and side, and the tensor trace
+  // weights B2[lf][q][i0*n1+i1] = l(a_q, i0) l(b_q, i1) on the face's two
+  // tangential axes (ascending axis order)
+  int fax[RKDG_MAX_NFPE], fside[RKDG_MAX_NFPE];
+  double B2[RKDG_MAX_NFPE][RKDG_MAX_NQF][9];
 };
 
 // Boundary condition slot.

@@ -969,6 +969,9 @@ int rkdg_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0, int d
       st = read_mcs(c, c->s - 1, &mcs);
       if (st) return st;
       dt = cfl * c->hmin / mcs / denom;
+      // The reference loops forever on a non-finite or vanishing dt; stop instead.
+      if (!std::isfinite(dt) || !(dt > 1e-14 * std::max(t_end, 1.0)))
+        return fail(c, RKDG_ERR_UNPHYSICAL, "non-finite or vanishing CFL time step", ti);
     }
     t += dt;
     ti++;

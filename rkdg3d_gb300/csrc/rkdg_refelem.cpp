@@ -385,6 +385,28 @@ bool build_ref_tables(int geom, int p, RefTables& T, std::vector<FacePoint>* fpt
       Pts l2 = seg_rule(2);
       for (int a = 0; a < 2; ++a)
         for (int j = 0; j < B.n1; ++j) T.lquad[a][j] = lag(B.x1, j, l2.x[a]);
+      for (int j = 0; j < B.n1; ++j) T.w1[j] = gw[j];
+    }
+    if (geom == 5) {
+      // tensor trace tables of the hexahedron faces
+      for (int lf = 0; lf < nfpe; ++lf) {
+        double xi0[3], xi1[3];
+        face_to_elem(geom, lf, &f.x[0], xi0);
+        face_to_elem(geom, lf, &f.x[(f.n - 1) * 2], xi1);
+        int nax = 0;
+        for (int i = 0; i < 3; ++i)
+          if (std::fabs(xi0[i] - xi1[i]) < 1e-14) nax = i;
+        T.fax[lf] = nax;
+        T.fside[lf] = xi0[nax] > 0.5 ? 1 : 0;
+        const int t0 = nax == 0 ? 1 : 0, t1 = nax == 2 ? 1 : 2;
+        for (int q = 0; q < f.n; ++q) {
+          double xi[3];
+          face_to_elem(geom, lf, &f.x[q * 2], xi);
+          for (int i0 = 0; i0 < B.n1; ++i0)
+            for (int i1 = 0; i1 < B.n1; ++i1)
+              T.B2[lf][q][i0 * B.n1 + i1] = lag(B.x1, i0, xi[t0]) * lag(B.x1, i1, xi[t1]);
+        }
+      }
     }
   }
   // limiter face points (order 2) and vertices

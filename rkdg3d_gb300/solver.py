@@ -220,6 +220,8 @@ class Context:
 
     def run(self, x, t_end: float, cfl: float = 0.3, dt0: float = 0.0, dt_mode: int = 0,
             max_steps: int = 0) -> dict:
+        if max_steps <= 0 and not (t_end < 1e20):
+            raise ValueError("run() needs a finite t_end or max_steps > 0")
         steps = C.c_int()
         t = C.c_double()
         dt = C.c_double()
