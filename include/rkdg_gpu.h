@@ -103,6 +103,11 @@ int rkdg_set_limiter(rkdg_ctx* ctx, int limiter, int indicator, int function,
 int rkdg_set_tableau(rkdg_ctx* ctx, int s, const double* a, const double* b,
                      const double* c);
 int rkdg_set_precision(rkdg_ctx* ctx, int precision);
+/* Kernel tuning knobs (no counterpart in the reference; used by the
+ * autotuner).  RKDG_TUNE_HEX_KERNEL: 0 default, 1 warp per element,
+ * 2 five-lane team per element (hexahedra). */
+enum { RKDG_TUNE_HEX_KERNEL = 1 };
+int rkdg_set_tuning(rkdg_ctx* ctx, int key, int value);
 
 /* ---- queries ------------------------------------------------------------ */
 /* NDofs (scalar nodes), nodes per element, number of equations. */
@@ -148,6 +153,25 @@ int rkdg_totals(rkdg_ctx* ctx, const double* x_dev, double* totals_host);
  * flux [n][neq], speed [n] (-1 where the reference returns -1). */
 int rkdg_riemann_batch(rkdg_ctx* ctx, int n, const double* u1, const double* u2,
                        const double* nor, double* flux, double* speed);
+/* ---- batched independent problems ----------------------------------------
+ * Many independent solves (different meshes, states and EoS constants) in one
+ * context: the mesh passed to rkdg_upload_mesh is the disjoint union of the
+ * problems' meshes, problem p owning elements [elem_offsets[p],
+ * elem_offsets[p+1]).  Riemann solver, limiter, tableau and boundary
+ * conditions are shared; gamma and covolume are per problem.  There is no
+ * counterpart in the reference, which runs one problem per process; each
+ * problem follows the reference's single-problem semantics (main.cpp:467-733)
+ * with its own h_min, CFL dt and time. */
+int rkdg_batch_setup(rkdg_ctx* ctx, int nprob, const int* elem_offsets,
+                     const double* gamma, const double* covolume);
+/* Advance every problem to t_end (dt_mode as rkdg_run, per problem).  With
+ * use_graph != 0 the whole multi-step solve is one CUDA-graph launch: the RK
+ * step is captured once as the body of a device-controlled while node and the
+ * loop ends on the device when the last problem finishes.  Host outputs
+ * (arrays of nprob, may be NULL): steps, booked t, integrated time. */
+int rkdg_batch_run(rkdg_ctx* ctx, double* x_dev, double t_end, double cfl, double dt0,
+                   int dt_mode, int max_steps, int use_graph, int* steps_out,
+                   double* t_out, double* sum_dt_out);
 /* Number of kernels this context launched since creation (instrumentation). */
 long long rkdg_kernel_launches(rkdg_ctx* ctx);
 

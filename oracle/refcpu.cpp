@@ -1484,7 +1484,7 @@ int ref_run(ref_ctx* c, double* x, double t_end, double cfl, double dt0, int dt_
     if (st) return st;
     sum_dt += dt_real;
     if (dt_mode == 0) dt = cfl * hmin / mcs / (2 * c->p + 1);
-    if (!std::isfinite(dt) || !(dt > 1e-14 * std::max(t_end, 1.0))) {
+    if (!std::isfinite(dt) || !(dt > 0.0) || (t_end < 1e20 && dt < 1e-14 * t_end)) {
       c->err = "non-finite or vanishing CFL time step";
       return REF_ERR_UNPHYSICAL;
     }

@@ -30,6 +30,7 @@ _SIGS = [
     ("rkdg_set_limiter", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("rkdg_set_tableau", C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
     ("rkdg_set_precision", C.c_int, [_vp, C.c_int]),
+    ("rkdg_set_tuning", C.c_int, [_vp, C.c_int, C.c_int]),
     ("rkdg_sizes", C.c_int, [_vp, C.POINTER(C.c_longlong), _ip, _ip]),
     ("rkdg_node_coords_host", C.c_int, [_vp, _dp]),
     ("rkdg_hmin", C.c_int, [_vp, _dp]),
@@ -42,6 +43,9 @@ _SIGS = [
                            _ip, _dp, _dp, _dp]),
     ("rkdg_totals", C.c_int, [_vp, _vp, _dp]),
     ("rkdg_riemann_batch", C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    ("rkdg_batch_setup", C.c_int, [_vp, C.c_int, _ip, _dp, _dp]),
+    ("rkdg_batch_run", C.c_int, [_vp, _vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                 C.c_int, _ip, _dp, _dp]),
     ("rkdg_kernel_launches", C.c_longlong, [_vp]),
 ]
 

@@ -154,6 +154,83 @@ def double_mach(nx=1024, ny=256, order=1, jitter=0.2, seed=0, t_end=0.2, cfl=0.2
                 ic=ic)
 
 
+@dataclass
+class BatchCase:
+    """Independent 2D Riemann problems solved together (one context)."""
+    cases: list
+    mesh: M.Mesh
+    offsets: np.ndarray
+    gammas: np.ndarray
+    covolumes: np.ndarray
+    order: int
+    t_end: float
+    cfl: float
+
+    def project(self, coords: np.ndarray) -> np.ndarray:
+        """byNODES state of the union mesh from each problem's own IC."""
+        nd = (self.order + 1) ** 2
+        parts = []
+        for p, c in enumerate(self.cases):
+            e0, e1 = self.offsets[p], self.offsets[p + 1]
+            parts.append(project(c, coords[:, e0 * nd:e1 * nd]).reshape(4, -1))
+        return np.concatenate(parts, axis=1).ravel()
+
+
+def union_mesh(meshes) -> M.Mesh:
+    ev, ec, bv, ba = [], [], [], []
+    voff = 0
+    for m in meshes:
+        ev.append(m.elem_vertices + voff)
+        ec.append(m.elem_coords)
+        bv.append(m.bdr_vertices + voff)
+        ba.append(m.bdr_attr)
+        voff += int(max(m.elem_vertices.max(), m.bdr_vertices.max() if m.bdr_vertices.size else 0)) + 1
+    return M.Mesh(meshes[0].dim, meshes[0].geom, np.concatenate(ev).astype(np.int32),
+                  np.concatenate(ec), np.concatenate(bv).astype(np.int32),
+                  np.concatenate(ba).astype(np.int32))
+
+
+def batched_riemann(nprob=256, nmin=100, nmax=2000, seed=0, order=1, t_end=0.15, cfl=0.3,
+                    covolume=0.001, tableau=TABLEAU_SSPRK3) -> BatchCase:
+    """Uneven batch of 2D Riemann problems: problem i on an N_i x 4 quad mesh
+    over [0,1] x [0, 4/N_i], N_i ~ U{nmin..nmax}; rho, p ~ U[0.1,1] and
+    u ~ U[-0.5,0.5] on each side, interface ~ U[0.3,0.7]; the first half
+    perfect gas (gamma 1.4), the second half covolume b.  HLLC + Einfeldt,
+    Multi limiter with the Michalak indicator, slip walls, open ends.  All
+    draws come from numpy.random.default_rng(seed) in the order N, rho_L,
+    rho_R, p_L, p_R, u_L, u_R, interface."""
+    rng = np.random.default_rng(seed)
+    N = rng.integers(nmin, nmax + 1, size=nprob)
+    rl, rr, pl, pr = rng.uniform(0.1, 1.0, (4, nprob))
+    ul, ur = rng.uniform(-0.5, 0.5, (2, nprob))
+    xi = rng.uniform(0.3, 0.7, nprob)
+    gam = np.full(nprob, 1.4)
+    cov = np.where(np.arange(nprob) < nprob // 2, 0.0, covolume)
+    cs = []
+    for p in range(nprob):
+        mesh = M.quad_grid(int(N[p]), 4, 0.0, 1.0, 0.0, 4.0 / N[p])
+
+        def ic(x, p=p):
+            left = x[0] < xi[p]
+            z = np.zeros_like(x[0])
+            return (np.where(left, rl[p], rr[p]), np.where(left, ul[p], ur[p]), z,
+                    np.where(left, pl[p], pr[p]))
+
+        cs.append(Case(f"riemann{p}", mesh, order, RS_HLLC, AVG_EINFELDT, gamma=gam[p],
+                       covolume=cov[p],
+                       bcs=[(1, BC_SLIP, None), (3, BC_SLIP, None), (2, BC_OPEN, None),
+                            (4, BC_OPEN, None)],
+                       limiter=(LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 0), tableau=tableau,
+                       t_end=t_end, cfl=cfl, ic=ic))
+    offs = np.concatenate([[0], np.cumsum([c.mesh.num_elements for c in cs])]).astype(np.int32)
+    return BatchCase(cs, union_mesh([c.mesh for c in cs]), offs, gam, cov, order, t_end, cfl)
+
+
+def configure_batch(bc: BatchCase, ctx) -> None:
+    configure_context(bc.cases[0], ctx)
+    ctx.batch_setup(bc.offsets, bc.gammas, bc.covolumes)
+
+
 def configure_oracle(case: Case, oracle) -> None:
     oracle.set_physics(case.rsolver, case.averaging, case.gamma, case.covolume, 1.0)
     for attr, t, st in case.bcs:

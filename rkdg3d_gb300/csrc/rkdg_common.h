@@ -60,6 +60,9 @@ struct RefTables {
   // tangential axes (ascending axis order)
   int fax[RKDG_MAX_NFPE], fside[RKDG_MAX_NFPE];
   double B2[RKDG_MAX_NFPE][RKDG_MAX_NQF][9];
+  // canonical face point q -> tensor index a + nq1*b (a along the lower
+  // tangential axis, b along the upper one)
+  int fab[RKDG_MAX_NFPE][RKDG_MAX_NQF];
 };
 
 // Boundary condition slot.
@@ -86,6 +89,14 @@ struct RhsParams {
   BCSlot bc[RKDG_MAX_BC];
   unsigned long long* mcs;  // atomicMax target, bits of a non-negative double
   int* err;                 // [0] status (first writer wins), [1] element
+  // batched independent problems (null when the context holds one problem):
+  // element -> problem, per-problem EoS constants, active flags and one
+  // max-speed slot per problem
+  const int* prob;
+  const double* pgamma;
+  const double* pcov;
+  const int* pactive;
+  unsigned long long* pmcs;
 };
 
 // Stage epilogue.
@@ -116,6 +127,10 @@ struct EpiParams {
   double ccur;
   float ccur_hi, ccur_lo;
   double* means;
+  // batched problems: when pdt is set, cprev/ccur hold the unscaled tableau
+  // coefficients and are multiplied by the problem's dt (pdt[prob[e]])
+  const int* prob;
+  const double* pdt;
 };
 
 struct LimParams {
@@ -126,6 +141,25 @@ struct LimParams {
   const double* means;  // [neq][ne]
   double gamma, covolume;
   int limiter, indicator, function, last_hope, quirks;
+  const int* prob;      // batched problems (or null)
+  const double* pgamma;
+  const double* pcov;
+  const int* pactive;
+};
+
+// Device-side time control of batched problems (one entry per problem).
+struct BatchState {
+  double t_end, cfl, denom;
+  int nprob, dt_mode, max_steps;
+  const double* hmin;   // [nprob]
+  double* dt;           // [nprob] dt of the reference bookkeeping
+  double* dtr;          // [nprob] dt_real used by the current step
+  double* t;            // [nprob]
+  double* sum_dt;       // [nprob]
+  int* active;          // [nprob]
+  int* steps;           // [nprob]
+  int* nactive;         // [1]
+  const unsigned long long* mcs_last;  // [nprob] max speed of the last stage
 };
 
 }  // namespace rkdg

@@ -1,6 +1,9 @@
-// Hexahedra: sum-factorised right-hand side kernels (rkdg_hex.cuh) plus the
-// generic limiter and cell-mean kernels.
+// Hexahedra: register-resident team kernels (rkdg_hex_team.cuh) for the
+// right-hand side, the warp-per-element sum-factorised kernel
+// (rkdg_hex.cuh) for the FP64 path, plus the generic limiter and cell-mean
+// kernels.
 #include "rkdg_hex.cuh"
+#include "rkdg_hex_team.cuh"
 #include "rkdg_inst.cuh"
 
 namespace rkdg {
@@ -22,19 +25,36 @@ static cudaError_t launch_hex_sf(const RhsParams& prm, const R* u, const EpiPara
   return cudaGetLastError();
 }
 
+template <int P, typename R>
+static cudaError_t launch_hex_team(const RhsParams& prm, const R* u, const EpiParams<R>& ep,
+                                   cudaStream_t st) {
+  using S = TeamSize<P>;
+  const size_t smem = S::template smem_bytes<R>();
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_rhs_hex_team<P, R>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  const int grid = (prm.ne + S::EPB - 1) / S::EPB;
+  k_rhs_hex_team<P, R><<<grid, S::THREADS, smem, st>>>(prm, u, ep);
+  return cudaGetLastError();
+}
+
 template <>
 cudaError_t launch_rhs_t<5, 1>(int prec, const RhsParams& prm, const void* u, const void* ep,
                                cudaStream_t st) {
   if (prec == 0)
-    return launch_hex_sf<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st);
-  return launch_hex_sf<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+    return launch_hex_team<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st);
+  return launch_hex_team<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
 }
 template <>
 cudaError_t launch_rhs_t<5, 2>(int prec, const RhsParams& prm, const void* u, const void* ep,
                                cudaStream_t st) {
   if (prec == 0)
     return launch_hex_sf<2, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st);
-  return launch_hex_sf<2, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+  return launch_hex_team<2, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
 }
 
 template cudaError_t launch_limit_t<5, 1>(int, const LimParams&, void*, float*, cudaStream_t);
@@ -43,5 +63,26 @@ template cudaError_t launch_means_t<5, 1>(int, int, long long, const RefTables*,
                                           const float*, double*, cudaStream_t);
 template cudaError_t launch_means_t<5, 2>(int, int, long long, const RefTables*, const void*,
                                           const float*, double*, cudaStream_t);
+
+// Both hexahedral right-hand-side kernels, selectable for tests (0 = default
+// choice above, 1 = warp-per-element sum factorisation, 2 = team kernel).
+cudaError_t launch_hex_variant(int variant, int p, int prec, const RhsParams& prm, const void* u,
+                               const void* ep, cudaStream_t st) {
+  if (variant == 1) {
+    if (p == 1)
+      return prec == 0 ? launch_hex_sf<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)
+                       : launch_hex_sf<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+    return prec == 0 ? launch_hex_sf<2, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)
+                     : launch_hex_sf<2, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+  }
+  if (variant == 2) {
+    if (p == 1)
+      return prec == 0 ? launch_hex_team<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)
+                       : launch_hex_team<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+    return prec == 0 ? launch_hex_team<2, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)
+                     : launch_hex_team<2, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+  }
+  return p == 1 ? launch_rhs_t<5, 1>(prec, prm, u, ep, st) : launch_rhs_t<5, 2>(prec, prm, u, ep, st);
+}
 
 }  // namespace rkdg

@@ -65,10 +65,35 @@ __device__ __forceinline__ void flag_error(int* err, int code, int where) {
   if (atomicCAS(&err[0], 0, code) == 0) err[1] = where;
 }
 
-// Epilogue for one element and one equation: y[i], i < ND.
+// Per-problem max wave speed for batched problems: elements of one problem
+// are contiguous, so a warp holds a few contiguous runs; a segmented shuffle
+// reduction leaves each run's max in its first lane, which commits it.
+__device__ __forceinline__ void segmented_max_commit(double v, int pb,
+                                                     unsigned long long* pmcs) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const double o = __shfl_down_sync(0xffffffffu, v, off);
+    const int opb = __shfl_down_sync(0xffffffffu, pb, off);
+    if (lane + off < 32 && opb == pb) v = fmax(v, o);
+  }
+  const int prev = __shfl_up_sync(0xffffffffu, pb, 1);
+  if (pb >= 0 && (lane == 0 || prev != pb)) atomic_max_nonneg(&pmcs[pb], v);
+}
+
+// Split c*s (c a tableau coefficient, s a problem's dt) into a float pair.
+__device__ __forceinline__ void split_scaled(double c, double s, float& hi, float& lo) {
+  const double v = c * s;
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+// Epilogue for one element and one equation: y[i], i < ND.  dts scales the
+// coefficients of batched problems (1 otherwise).
 template <int ND, typename R>
 __device__ __forceinline__ void epilogue(const EpiParams<R>& ep, long long base_idx,
-                                         const R* y, const R* wmean, int ne, int e, int k) {
+                                         const R* y, const R* wmean, int ne, int e, int k,
+                                         double dts) {
   if (ep.mode == 0) {
 #pragma unroll
     for (int i = 0; i < ND; ++i) ep.out64[base_idx + i] = (double)y[i];
@@ -80,8 +105,8 @@ __device__ __forceinline__ void epilogue(const EpiParams<R>& ep, long long base_
     for (int i = 0; i < ND; ++i) {
       const long long idx = base_idx + i;
       double v = ep.base ? ep.base[idx] : 0.0;
-      for (int j = 0; j < ep.nprev; ++j) v += ep.cprev[j] * ep.kprev[j][idx];
-      v += ep.ccur * y[i];
+      for (int j = 0; j < ep.nprev; ++j) v += (ep.cprev[j] * dts) * ep.kprev[j][idx];
+      v += (ep.ccur * dts) * y[i];
       if (ep.kout) ep.kout[idx] = y[i];
       if (ep.out64) ep.out64[idx] = v;
       if (ep.out32) ep.out32[idx] = (float)v;
@@ -90,13 +115,25 @@ __device__ __forceinline__ void epilogue(const EpiParams<R>& ep, long long base_
     if (ep.means) ep.means[(long long)k * ne + e] = m;
   } else {
     float mh = 0.0f, ml = 0.0f;
+    float ch[3], cl[3], cch, ccl;
+    if (ep.pdt) {
+      for (int j = 0; j < ep.nprev; ++j) split_scaled(ep.cprev[j], dts, ch[j], cl[j]);
+      split_scaled(ep.ccur, dts, cch, ccl);
+    } else {
+      for (int j = 0; j < ep.nprev; ++j) {
+        ch[j] = ep.cprev_hi[j];
+        cl[j] = ep.cprev_lo[j];
+      }
+      cch = ep.ccur_hi;
+      ccl = ep.ccur_lo;
+    }
     if (!ep.final_stage) {
 #pragma unroll
       for (int i = 0; i < ND; ++i) {
         const long long idx = base_idx + i;
         float inc = ep.baselo[idx];
-        for (int j = 0; j < ep.nprev; ++j) inc = fmaf(ep.cprev_hi[j], ep.kprev[j][idx], inc);
-        inc = fmaf(ep.ccur_hi, y[i], inc);
+        for (int j = 0; j < ep.nprev; ++j) inc = fmaf(ch[j], ep.kprev[j][idx], inc);
+        inc = fmaf(cch, y[i], inc);
         const float v = ep.basehi[idx] + inc;
         if (ep.kout) ep.kout[idx] = y[i];
         ep.out32[idx] = v;
@@ -110,10 +147,10 @@ __device__ __forceinline__ void epilogue(const EpiParams<R>& ep, long long base_
         const long long idx = base_idx + i;
         float sh = 0.0f, sl = 0.0f, ph, pl;
         for (int j = 0; j < ep.nprev; ++j) {
-          ds_mul_f(ep.cprev_hi[j], ep.cprev_lo[j], ep.kprev[j][idx], ph, pl);
+          ds_mul_f(ch[j], cl[j], ep.kprev[j][idx], ph, pl);
           ds_add(sh, sl, ph, pl);
         }
-        ds_mul_f(ep.ccur_hi, ep.ccur_lo, y[i], ph, pl);
+        ds_mul_f(cch, ccl, y[i], ph, pl);
         ds_add(sh, sl, ph, pl);
         float h = ep.basehi[idx], l = ep.baselo[idx];
         ds_add(h, l, sh, sl);
@@ -158,10 +195,20 @@ __global__ void __launch_bounds__(128)
 
   const int ne = prm.ne;
   const long long NDa = prm.ndofs;
-  const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+  R gamma = (R)prm.gamma, cov = (R)prm.covolume;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   R lmax = R(0);
-  if (e < ne) {
+  bool live = e < ne;
+  int pb = -1;
+  double dts = 1.0;
+  if (live && prm.prob) {
+    pb = prm.prob[e];
+    live = prm.pactive[pb] != 0;
+    gamma = (R)prm.pgamma[pb];
+    cov = (R)prm.pcov[pb];
+    if (ep.pdt) dts = ep.pdt[pb];
+  }
+  if (live) {
     R acc[NEQ][ND];
 #pragma unroll
     for (int k = 0; k < NEQ; ++k)
@@ -265,11 +312,14 @@ __global__ void __launch_bounds__(128)
           for (int j = 0; j < ND; ++j) v += sMinv[i][j] * acc[k][j];
           y[i] = v * idet;
         }
-        epilogue<ND, R>(ep, k * NDa + (long long)e * ND, y, sWm, ne, e, k);
+        epilogue<ND, R>(ep, k * NDa + (long long)e * ND, y, sWm, ne, e, k, dts);
       }
     }
   }
-  block_max_commit<R>(lmax, prm.mcs);
+  if (prm.prob)
+    segmented_max_commit((double)lmax, live ? pb : -1, prm.pmcs);
+  else
+    block_max_commit<R>(lmax, prm.mcs);
 }
 
 // ---- limiter ------------------------------------------------------------------
@@ -301,7 +351,13 @@ __global__ void __launch_bounds__(128)
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   const long long NDa = prm.ndofs;
-  const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+  R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+  if (prm.prob) {
+    const int pb = prm.prob[e];
+    if (!prm.pactive[pb]) return;
+    gamma = (R)prm.pgamma[pb];
+    cov = (R)prm.pcov[pb];
+  }
   R el[NEQ][ND];
   float lo[DS ? NEQ : 1][DS ? ND : 1];
 #pragma unroll

@@ -88,6 +88,52 @@ __device__ __forceinline__ double epi_value(const EpiParams<R>& ep, long long id
   }
 }
 
+// Same epilogue, returning the combined value as a pair (hi, lo); lo is zero
+// except for the float-pair conserved state of the final stage.
+template <typename R>
+__device__ __forceinline__ void epi_value2(const EpiParams<R>& ep, long long idx, R y, R& hi,
+                                           R& lo) {
+  lo = R(0);
+  if (ep.mode == 0) {
+    ep.out64[idx] = (double)y;
+    hi = y;
+    return;
+  }
+  if constexpr (std::is_same<R, double>::value) {
+    double v = ep.base ? ep.base[idx] : 0.0;
+    for (int j = 0; j < ep.nprev; ++j) v += ep.cprev[j] * ep.kprev[j][idx];
+    v += ep.ccur * y;
+    if (ep.kout) ep.kout[idx] = y;
+    if (ep.out64) ep.out64[idx] = v;
+    if (ep.out32) ep.out32[idx] = (float)v;
+    hi = v;
+  } else {
+    if (!ep.final_stage) {
+      float inc = ep.baselo[idx];
+      for (int j = 0; j < ep.nprev; ++j) inc = fmaf(ep.cprev_hi[j], ep.kprev[j][idx], inc);
+      inc = fmaf(ep.ccur_hi, y, inc);
+      const float v = ep.basehi[idx] + inc;
+      if (ep.kout) ep.kout[idx] = y;
+      ep.out32[idx] = v;
+      hi = v;
+      return;
+    }
+    float sh = 0.0f, sl = 0.0f, ph, pl;
+    for (int j = 0; j < ep.nprev; ++j) {
+      ds_mul_f(ep.cprev_hi[j], ep.cprev_lo[j], ep.kprev[j][idx], ph, pl);
+      ds_add(sh, sl, ph, pl);
+    }
+    ds_mul_f(ep.ccur_hi, ep.ccur_lo, y, ph, pl);
+    ds_add(sh, sl, ph, pl);
+    float h = ep.basehi[idx], l = ep.baselo[idx];
+    ds_add(h, l, sh, sl);
+    ep.out32[idx] = h;
+    ep.outlo[idx] = l;
+    hi = h;
+    lo = l;
+  }
+}
+
 template <int P, typename R>
 __global__ void __launch_bounds__(256)
     k_rhs_hex_sf(const RhsParams prm, const R* __restrict__ u, const EpiParams<R> ep) {

@@ -1,0 +1,433 @@
+// Register-resident hexahedral right-hand side: a team of 5 lanes per element,
+// one lane per conserved variable.
+//
+// Every linear tensor operation of the DG right-hand side acts on one variable
+// at a time, so a lane keeps its variable's (p+1)^3 nodal values and
+// accumulators in registers and applies, with compile-time indices,
+//   * the contraction along each face normal and the interpolation to the
+//     (p+2)^2 face points (sum factorisation),
+//   * the lifting of the face fluxes (transposed tensor trace),
+//   * the collocated (phi, grad phi) operator one direction at a time,
+//   * the inverse of the exact mass matrix det J (M1 x M1 x M1) as three
+//     1D sweeps (fe_evolution.cpp:178-208).
+// Only the pointwise nonlinear work needs all five variables: the nodal Euler
+// flux (FE_Evolution::GetFlux, fe_evolution.cpp:219-245) and the numerical
+// flux at the face points (FaceIntegrator::AssembleFaceVector,
+// face_integrator.cpp:11-276, arguments ordered Elem1, Elem2, Elem1-outward
+// normal); the team spreads those points over its lanes and exchanges the
+// states through a small shared-memory buffer.  Six teams per warp, four warps
+// per CTA (24 elements); the CTA loads its elements' DOFs and applies the
+// Runge-Kutta epilogue with coalesced accesses.
+#pragma once
+
+#include "rkdg_common.h"
+#include "rkdg_generic.cuh"
+#include "rkdg_hex.cuh"
+#include "rkdg_physics.cuh"
+
+namespace rkdg {
+
+template <int P>
+struct TeamSize {
+  static constexpr int N1 = P + 1, NQ1 = P + 2, ND = N1 * N1 * N1, NQF = NQ1 * NQ1, NEQ = 5,
+                       NF2 = N1 * N1;
+  static constexpr int TPW = 6, WARPS = 4, EPB = TPW * WARPS, THREADS = 32 * WARPS;
+  // per team exchange: max(traces + fluxes, volume fluxes)
+  static constexpr int XF = 3 * NEQ * NQF, XV = 3 * NEQ * ND;
+  static constexpr int XCH = XF > XV ? XF : XV;
+  static constexpr int TAB = NQ1 * N1 + 2 * N1 + 2 * N1 * N1 + N1 + NQF;
+  static constexpr int TAB_AL = (TAB + 3) & ~3;
+  template <typename R>
+  static constexpr size_t smem_bytes() {
+    return sizeof(R) * (size_t)(TAB_AL + EPB * NEQ * ND + EPB * XCH);
+  }
+};
+
+// MFEM hexahedron local faces: normal axis and side.
+__host__ __device__ constexpr int hex_face_axis(int lf) {
+  return lf == 0 || lf == 5 ? 2 : (lf == 1 || lf == 3 ? 1 : 0);
+}
+__host__ __device__ constexpr int hex_face_side(int lf) {
+  return lf == 2 || lf == 3 || lf == 5 ? 1 : 0;
+}
+template <int N1>
+__host__ __device__ constexpr int hnode(int nax, int jn, int i0, int i1) {
+  return nax == 0 ? jn + N1 * (i0 + N1 * i1) : (nax == 1 ? i0 + N1 * (jn + N1 * i1) : i0 + N1 * (i1 + N1 * jn));
+}
+
+// Contraction of a register array along face LF's normal: v[i0*N1+i1].
+template <int P, int LF, typename R>
+__device__ __forceinline__ void team_contract(const R (&u)[(P + 1) * (P + 1) * (P + 1)],
+                                              const R* lend, R (&v)[(P + 1) * (P + 1)]) {
+  constexpr int N1 = P + 1, NAX = hex_face_axis(LF), SD = hex_face_side(LF);
+#pragma unroll
+  for (int i0 = 0; i0 < N1; ++i0)
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1) {
+      R s = R(0);
+#pragma unroll
+      for (int jn = 0; jn < N1; ++jn) s += lend[SD * N1 + jn] * u[hnode<N1>(NAX, jn, i0, i1)];
+      v[i0 * N1 + i1] = s;
+    }
+}
+
+// Same contraction reading the element's values from global memory.
+template <int P, int LF, typename R>
+__device__ __forceinline__ void team_contract_g(const R* __restrict__ ug, const R* lend,
+                                                R (&v)[(P + 1) * (P + 1)]) {
+  constexpr int N1 = P + 1, NAX = hex_face_axis(LF), SD = hex_face_side(LF);
+#pragma unroll
+  for (int i0 = 0; i0 < N1; ++i0)
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1) {
+      R s = R(0);
+#pragma unroll
+      for (int jn = 0; jn < N1; ++jn) s += lend[SD * N1 + jn] * __ldg(ug + hnode<N1>(NAX, jn, i0, i1));
+      v[i0 * N1 + i1] = s;
+    }
+}
+
+template <int P, typename R>
+__device__ __forceinline__ void team_contract_g_any(int lf, const R* __restrict__ ug, const R* lend,
+                                                    R (&v)[(P + 1) * (P + 1)]) {
+  switch (lf) {
+    case 0: team_contract_g<P, 0>(ug, lend, v); break;
+    case 1: team_contract_g<P, 1>(ug, lend, v); break;
+    case 2: team_contract_g<P, 2>(ug, lend, v); break;
+    case 3: team_contract_g<P, 3>(ug, lend, v); break;
+    case 4: team_contract_g<P, 4>(ug, lend, v); break;
+    default: team_contract_g<P, 5>(ug, lend, v); break;
+  }
+}
+
+// v (N1 x N1 on the face's tangential axes) -> values at the NQ1 x NQ1 face
+// points in tensor order a + NQ1*b, written to dst.
+template <int P, typename R>
+__device__ __forceinline__ void team_interp(const R (&v)[(P + 1) * (P + 1)], const R* l1d, R* dst) {
+  constexpr int N1 = P + 1, NQ1 = P + 2;
+  R w[NQ1][N1];
+#pragma unroll
+  for (int a = 0; a < NQ1; ++a)
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1) {
+      R s = R(0);
+#pragma unroll
+      for (int i0 = 0; i0 < N1; ++i0) s += l1d[a * N1 + i0] * v[i0 * N1 + i1];
+      w[a][i1] = s;
+    }
+#pragma unroll
+  for (int b = 0; b < NQ1; ++b)
+#pragma unroll
+    for (int a = 0; a < NQ1; ++a) {
+      R s = R(0);
+#pragma unroll
+      for (int i1 = 0; i1 < N1; ++i1) s += l1d[b * N1 + i1] * w[a][i1];
+      dst[a + NQ1 * b] = s;
+    }
+}
+
+// Lift face values f (tensor order) of face LF into the accumulators.
+template <int P, int LF, typename R>
+__device__ __forceinline__ void team_lift(const R* f, const R* l1d, const R* lend,
+                                          R (&acc)[(P + 1) * (P + 1) * (P + 1)]) {
+  constexpr int N1 = P + 1, NQ1 = P + 2, NAX = hex_face_axis(LF), SD = hex_face_side(LF);
+  R w[N1][NQ1];
+#pragma unroll
+  for (int i0 = 0; i0 < N1; ++i0)
+#pragma unroll
+    for (int b = 0; b < NQ1; ++b) {
+      R s = R(0);
+#pragma unroll
+      for (int a = 0; a < NQ1; ++a) s += l1d[a * N1 + i0] * f[a + NQ1 * b];
+      w[i0][b] = s;
+    }
+#pragma unroll
+  for (int i0 = 0; i0 < N1; ++i0)
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1) {
+      R s = R(0);
+#pragma unroll
+      for (int b = 0; b < NQ1; ++b) s += l1d[b * N1 + i1] * w[i0][b];
+#pragma unroll
+      for (int jn = 0; jn < N1; ++jn) acc[hnode<N1>(NAX, jn, i0, i1)] += lend[SD * N1 + jn] * s;
+    }
+}
+
+// One face of one element, for the team's variable k.
+template <int P, int LF, typename R>
+__device__ __forceinline__ void team_face(const RhsParams& prm, const R* __restrict__ ug, int e, int k,
+                                          int tl, R (&u)[(P + 1) * (P + 1) * (P + 1)],
+                                          R (&acc)[(P + 1) * (P + 1) * (P + 1)], R* xch,
+                                          const R* l1d, const R* lend, const R* wf,
+                                          const unsigned char (*perm)[(P + 2) * (P + 2)],
+                                          const int (*fab)[RKDG_MAX_NQF], R gamma, R cov,
+                                          R& lmax, unsigned mask) {
+  using S = TeamSize<P>;
+  constexpr int N1 = S::N1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ;
+  const int ne = prm.ne;
+  const long long NDa = prm.ndofs;
+  const int nb = prm.fnbr[LF * ne + e];
+  if (nb == -1) return;
+  R* To = xch;                 // [NEQ][NQF] own traces (tensor order)
+  R* Tn = To + NEQ * NQF;      // [NEQ][NQF] neighbour traces (its tensor order)
+  R* Fh = Tn + NEQ * NQF;      // [NEQ][NQF] lifted flux values (own tensor order)
+  {
+    R v[N1 * N1];
+    team_contract<P, LF>(u, lend, v);
+    team_interp<P>(v, l1d, To + k * NQF);
+  }
+  const int code = prm.fcode[LF * ne + e];
+  const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
+  if (nb >= 0) {
+    R v[N1 * N1];
+    team_contract_g_any<P>(lfo, ug + k * NDa + (long long)nb * ND, lend, v);
+    team_interp<P>(v, l1d, Tn + k * NQF);
+  }
+  __syncwarp(mask);
+  const R* fg = (const R*)prm.fgeo;
+  R n[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) n[c] = fg[(long long)(LF * 4 + c) * ne + e];
+  const R jac = fg[(long long)(LF * 4 + 3) * ne + e];
+  const R sg = side ? R(1) : R(-1);
+#pragma unroll
+  for (int rr = 0; rr < (NQF + NEQ - 1) / NEQ; ++rr) {
+    const int q = tl + NEQ * rr;
+    if (q < NQF) {
+      const int q2 = perm[pid][q];
+      R s1[NEQ], s2[NEQ];
+      int own = fab[LF][q];
+      if (nb >= 0) {
+        const int a1 = side ? fab[lfo][q] : fab[LF][q];
+        const int a2 = side ? fab[LF][q2] : fab[lfo][q2];
+        const R* T1 = side ? Tn : To;
+        const R* T2 = side ? To : Tn;
+#pragma unroll
+        for (int kk = 0; kk < NEQ; ++kk) {
+          s1[kk] = T1[kk * NQF + a1];
+          s2[kk] = T2[kk * NQF + a2];
+        }
+        if (side) own = a2;
+      } else {
+#pragma unroll
+        for (int kk = 0; kk < NEQ; ++kk) s1[kk] = To[kk * NQF + own];
+        const BCSlot& bc = prm.bc[-2 - nb];
+        right_state<3>(bc.type, bc.state, s1, s2, n);
+      }
+      R F[NEQ];
+      R sp = riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg);
+      if (sp < R(0)) {
+        flag_error(prm.err, 2, e);
+        sp = R(0);
+      }
+      lmax = fmax(lmax, sp);
+      const R wq = wf[q];
+#pragma unroll
+      for (int kk = 0; kk < NEQ; ++kk) Fh[kk * NQF + own] = sg * (F[kk] * wq) * jac;
+    }
+  }
+  __syncwarp(mask);
+  if (!prm.faces_only) team_lift<P, LF>(Fh + k * NQF, l1d, lend, acc);
+  __syncwarp(mask);
+}
+
+template <int P, typename R>
+__global__ void __launch_bounds__(128)
+    k_rhs_hex_team(const RhsParams prm, const R* __restrict__ u, const EpiParams<R> ep) {
+  using S = TeamSize<P>;
+  constexpr int N1 = S::N1, NQ1 = S::NQ1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, EPB = S::EPB;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ unsigned char sPerm[RKDG_MAX_PERM][NQF];
+  __shared__ int sFab[6][RKDG_MAX_NQF];
+  R* sm = reinterpret_cast<R*>(smraw);
+  R* tL1 = sm;                  // [NQ1][N1]
+  R* tLend = tL1 + NQ1 * N1;    // [2][N1]
+  R* tD1 = tLend + 2 * N1;      // [N1][N1]
+  R* tMinv = tD1 + N1 * N1;     // [N1][N1]
+  R* tW1 = tMinv + N1 * N1;     // [N1]
+  R* tWf = tW1 + N1;            // [NQF]
+  R* sU = sm + S::TAB_AL;       // [EPB][NEQ][ND]
+  R* sX = sU + EPB * NEQ * ND;  // [EPB][XCH]
+  const RefTables* T = prm.tab;
+  const int tid = threadIdx.x;
+  for (int t = tid; t < NQ1 * N1; t += blockDim.x) tL1[t] = (R)T->l1d[t / N1][t % N1];
+  for (int t = tid; t < 2 * N1; t += blockDim.x) tLend[t] = (R)T->lend[t / N1][t % N1];
+  for (int t = tid; t < N1 * N1; t += blockDim.x) {
+    tD1[t] = (R)T->d1[t / N1][t % N1];
+    tMinv[t] = (R)T->minv1[t / N1][t % N1];
+  }
+  for (int t = tid; t < N1; t += blockDim.x) tW1[t] = (R)T->w1[t];
+  for (int t = tid; t < NQF; t += blockDim.x) tWf[t] = (R)T->wf[t];
+  for (int t = tid; t < T->nperm * NQF; t += blockDim.x) sPerm[t / NQF][t % NQF] = (unsigned char)T->perm[t / NQF][t % NQF];
+  for (int t = tid; t < 6 * NQF; t += blockDim.x) sFab[t / NQF][t % NQF] = T->fab[t / NQF][t % NQF];
+
+  const int ne = prm.ne;
+  const long long NDa = prm.ndofs;
+  const int e0 = blockIdx.x * EPB;
+  const int nel = min(EPB, ne - e0);
+  for (int k = 0; k < NEQ; ++k)
+    for (int t = tid; t < nel * ND; t += blockDim.x)
+      sU[((t / ND) * NEQ + k) * ND + (t % ND)] = u[k * NDa + (long long)e0 * ND + t];
+  __syncthreads();
+
+  const int warp = tid >> 5, lane = tid & 31;
+  const int team = lane / NEQ, tl = lane - NEQ * team;
+  const int el = warp * S::TPW + team;  // element slot in the CTA
+  const bool act = team < S::TPW && el < nel;
+  // the five lanes of a team synchronise among themselves only (teams may
+  // skip different faces)
+  const unsigned mask = act ? (0x1Fu << (team * NEQ)) : 0u;
+  const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+  R lmax = R(0);
+  if (act) {
+    const int e = e0 + el;
+    const int k = tl;
+    R* xch = sX + el * S::XCH;
+    R uv[ND], acc[ND];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      uv[i] = sU[(el * NEQ + k) * ND + i];
+      acc[i] = R(0);
+    }
+    team_face<P, 0>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
+    team_face<P, 1>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
+    team_face<P, 2>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
+    team_face<P, 3>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
+    team_face<P, 4>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
+    team_face<P, 5>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
+    if (!prm.faces_only) {
+      // nodal fluxes: lane tl handles nodes tl, tl+5, ...; contravariant
+      // components of all variables go to the exchange buffer [3][NEQ][ND]
+      const R* eg = (const R*)prm.egeo;
+      R adj[3][3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) adj[r][d] = eg[(long long)(r * 3 + d) * ne + e];
+      const R idet = eg[(long long)9 * ne + e];
+#pragma unroll
+      for (int rr = 0; rr < (ND + NEQ - 1) / NEQ; ++rr) {
+        const int m = tl + NEQ * rr;
+        if (m < ND) {
+          R st[NEQ];
+#pragma unroll
+          for (int kk = 0; kk < NEQ; ++kk) st[kk] = sU[(el * NEQ + kk) * ND + m];
+          R F[NEQ][3];
+          lmax = fmax(lmax, flux_and_speed<3>(st, F, gamma, cov));
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int kk = 0; kk < NEQ; ++kk)
+              xch[(r * NEQ + kk) * ND + m] = adj[r][0] * F[kk][0] + adj[r][1] * F[kk][1] + adj[r][2] * F[kk][2];
+        }
+      }
+      __syncwarp(mask);
+      R g[ND];
+      // x direction
+#pragma unroll
+      for (int i = 0; i < ND; ++i) g[i] = xch[(0 * NEQ + k) * ND + i];
+#pragma unroll
+      for (int jz = 0; jz < N1; ++jz)
+#pragma unroll
+        for (int jy = 0; jy < N1; ++jy)
+#pragma unroll
+          for (int jx = 0; jx < N1; ++jx) {
+            R s = R(0);
+#pragma unroll
+            for (int m = 0; m < N1; ++m) s += tD1[jx * N1 + m] * g[m + N1 * (jy + N1 * jz)];
+            acc[jx + N1 * (jy + N1 * jz)] += tW1[jy] * tW1[jz] * s;
+          }
+#pragma unroll
+      for (int i = 0; i < ND; ++i) g[i] = xch[(1 * NEQ + k) * ND + i];
+#pragma unroll
+      for (int jz = 0; jz < N1; ++jz)
+#pragma unroll
+        for (int jy = 0; jy < N1; ++jy)
+#pragma unroll
+          for (int jx = 0; jx < N1; ++jx) {
+            R s = R(0);
+#pragma unroll
+            for (int m = 0; m < N1; ++m) s += tD1[jy * N1 + m] * g[jx + N1 * (m + N1 * jz)];
+            acc[jx + N1 * (jy + N1 * jz)] += tW1[jx] * tW1[jz] * s;
+          }
+#pragma unroll
+      for (int i = 0; i < ND; ++i) g[i] = xch[(2 * NEQ + k) * ND + i];
+#pragma unroll
+      for (int jz = 0; jz < N1; ++jz)
+#pragma unroll
+        for (int jy = 0; jy < N1; ++jy)
+#pragma unroll
+          for (int jx = 0; jx < N1; ++jx) {
+            R s = R(0);
+#pragma unroll
+            for (int m = 0; m < N1; ++m) s += tD1[jz * N1 + m] * g[jx + N1 * (jy + N1 * m)];
+            acc[jx + N1 * (jy + N1 * jz)] += tW1[jx] * tW1[jy] * s;
+          }
+      // inverse mass: x, y, z sweeps
+#pragma unroll
+      for (int jz = 0; jz < N1; ++jz)
+#pragma unroll
+        for (int jy = 0; jy < N1; ++jy)
+#pragma unroll
+          for (int jx = 0; jx < N1; ++jx) {
+            R s = R(0);
+#pragma unroll
+            for (int m = 0; m < N1; ++m) s += tMinv[jx * N1 + m] * acc[m + N1 * (jy + N1 * jz)];
+            g[jx + N1 * (jy + N1 * jz)] = s;
+          }
+#pragma unroll
+      for (int jz = 0; jz < N1; ++jz)
+#pragma unroll
+        for (int jy = 0; jy < N1; ++jy)
+#pragma unroll
+          for (int jx = 0; jx < N1; ++jx) {
+            R s = R(0);
+#pragma unroll
+            for (int m = 0; m < N1; ++m) s += tMinv[jy * N1 + m] * g[jx + N1 * (m + N1 * jz)];
+            acc[jx + N1 * (jy + N1 * jz)] = s;
+          }
+      __syncwarp(mask);
+#pragma unroll
+      for (int jz = 0; jz < N1; ++jz)
+#pragma unroll
+        for (int jy = 0; jy < N1; ++jy)
+#pragma unroll
+          for (int jx = 0; jx < N1; ++jx) {
+            R s = R(0);
+#pragma unroll
+            for (int m = 0; m < N1; ++m) s += tMinv[jz * N1 + m] * acc[jx + N1 * (jy + N1 * m)];
+            // the right-hand side replaces this variable's staged DOFs (the
+            // team's nodal fluxes have been formed already)
+            sU[(el * NEQ + k) * ND + jx + N1 * (jy + N1 * jz)] = s * idet;
+          }
+    }
+  }
+  __syncthreads();
+  if (!prm.faces_only) {
+    // coalesced Runge-Kutta epilogue over the CTA's elements; the combined
+    // state (hi, lo) is kept in shared memory when the limiter needs means
+    const bool need_means = ep.mode == 1 && ep.means;
+    for (int k = 0; k < NEQ; ++k)
+      for (int t = tid; t < nel * ND; t += blockDim.x) {
+        const int s = ((t / ND) * NEQ + k) * ND + (t % ND);
+        R hi, lo;
+        epi_value2<R>(ep, k * NDa + (long long)e0 * ND + t, sU[s], hi, lo);
+        if (need_means) {
+          sU[s] = hi;
+          sX[s] = lo;
+        }
+      }
+    if (need_means) {
+      __syncthreads();
+      // cell means of the combined state, one (element, variable) per thread
+      for (int t = tid; t < nel * NEQ; t += blockDim.x) {
+        double m = 0.0;
+        for (int i = 0; i < ND; ++i) m += T->wmean[i] * ((double)sU[t * ND + i] + (double)sX[t * ND + i]);
+        ep.means[(long long)(t % NEQ) * ne + e0 + t / NEQ] = m;
+      }
+    }
+  }
+  block_max_commit<R>(lmax, prm.mcs);
+}
+
+}  // namespace rkdg

@@ -44,6 +44,7 @@ struct rkdg_ctx {
   int s = 3;
   std::vector<double> a{1.0, 0.25, 0.25}, b{1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0}, c{1.0, 0.5};
   int precision = RKDG_FP64;
+  int hex_variant = 0;  // RKDG_TUNE_HEX_KERNEL
   // mesh (host copies)
   bool has_mesh = false;
   int dim = 0, geom = 0, p = 0, ne = 0, nd = 0, neq = 0, nfpe = 0, nvpe = 0;
@@ -74,6 +75,22 @@ struct rkdg_ctx {
   float* d_xl = nullptr;
   unsigned long long* h_mcs = nullptr;  // pinned
   int* h_err = nullptr;                 // pinned
+  std::vector<double> h_ehmin;          // per-element GetElementSize(i, 1)
+  // batched independent problems
+  int nprob = 0;
+  std::vector<int> h_poff;
+  int* d_prob = nullptr;
+  double* d_pgamma = nullptr;
+  double* d_pcov = nullptr;
+  double* d_phmin = nullptr;
+  double* d_pdt = nullptr;
+  double* d_pdtr = nullptr;
+  double* d_pt = nullptr;
+  double* d_psum = nullptr;
+  int* d_pactive = nullptr;
+  int* d_psteps = nullptr;
+  int* d_nactive = nullptr;
+  unsigned long long* d_pmcs = nullptr;  // [4][nprob]
 
   bool limiter_active() const { return !(lim == RKDG_LIM_FINDIFF && ind == RKDG_IND_NOWHERE); }
 };
@@ -126,6 +143,19 @@ void free_mesh(rkdg_ctx* c) {
   for (auto& p : c->d_y32) dfree(p);
   dfree(c->d_xh);
   dfree(c->d_xl);
+  dfree(c->d_prob);
+  dfree(c->d_pgamma);
+  dfree(c->d_pcov);
+  dfree(c->d_phmin);
+  dfree(c->d_pdt);
+  dfree(c->d_pdtr);
+  dfree(c->d_pt);
+  dfree(c->d_psum);
+  dfree(c->d_pactive);
+  dfree(c->d_psteps);
+  dfree(c->d_nactive);
+  dfree(c->d_pmcs);
+  c->nprob = 0;
   c->has_mesh = false;
 }
 
@@ -213,6 +243,14 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   return P;
 }
 
+void set_batch(rkdg_ctx* c, RhsParams& P, int slot) {
+  P.prob = c->d_prob;
+  P.pgamma = c->d_pgamma;
+  P.pcov = c->d_pcov;
+  P.pactive = c->d_pactive;
+  P.pmcs = c->d_pmcs + (size_t)slot * c->nprob;
+}
+
 LimParams lim_params(rkdg_ctx* c) {
   LimParams L;
   std::memset(&L, 0, sizeof L);
@@ -273,11 +311,31 @@ int check_device_error(rkdg_ctx* c) {
   return RKDG_OK;
 }
 
+LimParams lim_params_for(rkdg_ctx* c, bool batch) {
+  LimParams L = lim_params(c);
+  if (batch) {
+    L.prob = c->d_prob;
+    L.pgamma = c->d_pgamma;
+    L.pcov = c->d_pcov;
+    L.pactive = c->d_pactive;
+  }
+  return L;
+}
+
+cudaError_t zero_slot(rkdg_ctx* c, int i, bool batch) {
+  if (batch)
+    return cudaMemsetAsync(c->d_pmcs + (size_t)i * c->nprob, 0,
+                           (size_t)c->nprob * sizeof(unsigned long long), c->stream);
+  return cudaMemsetAsync(c->d_mcs + i, 0, sizeof(unsigned long long), c->stream);
+}
+
 // Enqueue one Runge-Kutta step on the FP64 state x (no host synchronisation).
-int enqueue_step64(rkdg_ctx* c, double* x, double dt) {
+// batch: every problem uses its own dt_real (d_pdtr) and EoS constants.
+int enqueue_step64(rkdg_ctx* c, double* x, double dt, bool batch = false) {
   const int s = c->s;
   const bool lim = c->limiter_active();
   const long long n = c->ndofs * c->neq;
+  if (batch) dt = 1.0;
   for (int i = 0; i < s; ++i) {
     const double* in;
     if (i == 0) {
@@ -291,11 +349,15 @@ int enqueue_step64(rkdg_ctx* c, double* x, double dt) {
     } else {
       in = c->d_y64[i % 2];
     }
-    CUDA_TRY(c, cudaMemsetAsync(c->d_mcs + i, 0, sizeof(unsigned long long), c->stream));
+    CUDA_TRY(c, zero_slot(c, i, batch));
     EpiParams<double> ep;
     std::memset(&ep, 0, sizeof ep);
     ep.mode = 1;
     ep.base = x;
+    if (batch) {
+      ep.prob = c->d_prob;
+      ep.pdt = c->d_pdtr;
+    }
     double* out;
     if (i < s - 1) {
       const int row = (i + 1) * i / 2;  // MFEM packing: coefficients of y_{i+1}
@@ -319,10 +381,11 @@ int enqueue_step64(rkdg_ctx* c, double* x, double dt) {
     ep.out64 = out;
     ep.means = lim ? c->d_means : nullptr;
     RhsParams P = rhs_params(c, 0, 0, i);
-    CUDA_TRY(c, rkdg::launch_rhs(c->geom, c->p, 0, P, in, &ep, c->stream));
+    if (batch) set_batch(c, P, i);
+    CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,0, P, in, &ep, c->stream));
     c->launches++;
     if (lim) {
-      LimParams L = lim_params(c);
+      LimParams L = lim_params_for(c, batch);
       CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 0, L, out, nullptr, c->stream));
       c->launches++;
     }
@@ -336,10 +399,11 @@ void split_coef(double v, float& hi, float& lo) {
 }
 
 // Enqueue one step on the float-pair state (d_xh, d_xl).
-int enqueue_step32(rkdg_ctx* c, double dt) {
+int enqueue_step32(rkdg_ctx* c, double dt, bool batch = false) {
   const int s = c->s;
   const bool lim = c->limiter_active();
   const long long n = c->ndofs * c->neq;
+  if (batch) dt = 1.0;
   for (int i = 0; i < s; ++i) {
     const float* in;
     if (i == 0) {
@@ -353,19 +417,25 @@ int enqueue_step32(rkdg_ctx* c, double dt) {
     } else {
       in = c->d_y32[i % 2];
     }
-    CUDA_TRY(c, cudaMemsetAsync(c->d_mcs + i, 0, sizeof(unsigned long long), c->stream));
+    CUDA_TRY(c, zero_slot(c, i, batch));
     EpiParams<float> ep;
     std::memset(&ep, 0, sizeof ep);
     ep.mode = 1;
     ep.basehi = c->d_xh;
     ep.baselo = c->d_xl;
+    if (batch) {
+      ep.prob = c->d_prob;
+      ep.pdt = c->d_pdtr;
+    }
     if (i < s - 1) {
       const int row = (i + 1) * i / 2;
       for (int j = 0; j < i; ++j) {
         ep.kprev[j] = c->d_k32[j];
+        ep.cprev[j] = c->a[row + j] * dt;
         split_coef(c->a[row + j] * dt, ep.cprev_hi[j], ep.cprev_lo[j]);
       }
       ep.nprev = i;
+      ep.ccur = c->a[row + i] * dt;
       split_coef(c->a[row + i] * dt, ep.ccur_hi, ep.ccur_lo);
       ep.kout = c->d_k32[i];
       ep.out32 = c->d_y32[(i + 1) % 2];
@@ -373,9 +443,11 @@ int enqueue_step32(rkdg_ctx* c, double dt) {
     } else {
       for (int j = 0; j < s - 1; ++j) {
         ep.kprev[j] = c->d_k32[j];
+        ep.cprev[j] = c->b[j] * dt;
         split_coef(c->b[j] * dt, ep.cprev_hi[j], ep.cprev_lo[j]);
       }
       ep.nprev = s - 1;
+      ep.ccur = c->b[s - 1] * dt;
       split_coef(c->b[s - 1] * dt, ep.ccur_hi, ep.ccur_lo);
       ep.out32 = c->d_xh;
       ep.outlo = c->d_xl;
@@ -383,10 +455,11 @@ int enqueue_step32(rkdg_ctx* c, double dt) {
     }
     ep.means = lim ? c->d_means : nullptr;
     RhsParams P = rhs_params(c, 1, 0, i);
-    CUDA_TRY(c, rkdg::launch_rhs(c->geom, c->p, 1, P, in, &ep, c->stream));
+    if (batch) set_batch(c, P, i);
+    CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,1, P, in, &ep, c->stream));
     c->launches++;
     if (lim) {
-      LimParams L = lim_params(c);
+      LimParams L = lim_params_for(c, batch);
       if (i < s - 1)
         CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 1, L, c->d_y32[(i + 1) % 2], nullptr, c->stream));
       else
@@ -565,6 +638,15 @@ int rkdg_set_precision(rkdg_ctx* c, int precision) {
   return RKDG_OK;
 }
 
+int rkdg_set_tuning(rkdg_ctx* c, int key, int value) {
+  if (!c) return RKDG_ERR_INVALID;
+  if (key == RKDG_TUNE_HEX_KERNEL && value >= 0 && value <= 2) {
+    c->hex_variant = value;
+    return RKDG_OK;
+  }
+  return fail(c, RKDG_ERR_INVALID, "unknown tuning key or value");
+}
+
 int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
   if (!c || !m) return RKDG_ERR_INVALID;
   cudaSetDevice(c->device);
@@ -597,6 +679,7 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
   // ---- element geometry (affine elements) ----
   c->h_egeo.assign((size_t)(dim * dim + 1) * ne, 0.0);
   c->h_wdet.assign(ne, 0.0);
+  c->h_ehmin.assign(ne, 0.0);
   c->h_nodes.assign((size_t)dim * c->ndofs, 0.0);
   const double refvol = geom == 2 ? 0.5 : 1.0;
   double hmin = 1e300;
@@ -652,7 +735,8 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
       for (int i = 0; i < 2; ++i)
         for (int j = 0; j < 2; ++j) Jp[i * 2 + j] = J[i * 2] * A[j] + J[i * 2 + 1] * A[2 + j];
     }
-    hmin = std::min(hmin, min_singular(dim, Jp));
+    c->h_ehmin[e] = min_singular(dim, Jp);
+    hmin = std::min(hmin, c->h_ehmin[e]);
     std::memcpy(&Jall[(size_t)e * 9], J, sizeof J);
   }
   c->hmin = hmin;
@@ -868,7 +952,7 @@ int rkdg_rhs(rkdg_ctx* c, const double* x, double* y, double* mcs_out) {
     ep.mode = 0;
     ep.out64 = y;
     RhsParams P = rhs_params(c, 0, 0, 0);
-    CUDA_TRY(c, rkdg::launch_rhs(c->geom, c->p, 0, P, x, &ep, c->stream));
+    CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,0, P, x, &ep, c->stream));
     c->launches++;
   } else {
     CUDA_TRY(c, rkdg::launch_to_float(n, x, c->d_y32[0], c->stream));
@@ -877,7 +961,7 @@ int rkdg_rhs(rkdg_ctx* c, const double* x, double* y, double* mcs_out) {
     ep.mode = 0;
     ep.out64 = y;
     RhsParams P = rhs_params(c, 1, 0, 0);
-    CUDA_TRY(c, rkdg::launch_rhs(c->geom, c->p, 1, P, c->d_y32[0], &ep, c->stream));
+    CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,1, P, c->d_y32[0], &ep, c->stream));
     c->launches += 2;
   }
   return read_mcs(c, 0, mcs_out);
@@ -890,7 +974,7 @@ int rkdg_face_speed(rkdg_ctx* c, const double* x, double* mcs_out) {
   EpiParams<double> ep;
   std::memset(&ep, 0, sizeof ep);
   RhsParams P = rhs_params(c, 0, 1, 0);
-  CUDA_TRY(c, rkdg::launch_rhs(c->geom, c->p, 0, P, x, &ep, c->stream));
+  CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,0, P, x, &ep, c->stream));
   c->launches++;
   return read_mcs(c, 0, mcs_out);
 }
@@ -970,7 +1054,7 @@ int rkdg_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0, int d
       if (st) return st;
       dt = cfl * c->hmin / mcs / denom;
       // The reference loops forever on a non-finite or vanishing dt; stop instead.
-      if (!std::isfinite(dt) || !(dt > 1e-14 * std::max(t_end, 1.0)))
+      if (!std::isfinite(dt) || !(dt > 0.0) || (t_end < 1e20 && dt < 1e-14 * t_end))
         return fail(c, RKDG_ERR_UNPHYSICAL, "non-finite or vanishing CFL time step", ti);
     }
     t += dt;
@@ -1019,6 +1103,179 @@ int rkdg_riemann_batch(rkdg_ctx* c, int n, const double* u1, const double* u2, c
                                          speed, c->gamma, c->cov, c->rs, c->avg, c->stream));
   c->launches++;
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return RKDG_OK;
+}
+
+int rkdg_batch_setup(rkdg_ctx* c, int nprob, const int* elem_offsets, const double* gamma,
+                     const double* covolume) {
+  NEED_MESH(c);
+  if (nprob <= 0 || !elem_offsets || !gamma || !covolume)
+    return fail(c, RKDG_ERR_INVALID, "invalid batch description");
+  if (c->geom == RKDG_GEOM_CUBE)
+    return fail(c, RKDG_ERR_UNSUPPORTED, "batched problems are supported on triangles and quads");
+  if (elem_offsets[0] != 0 || elem_offsets[nprob] != c->ne)
+    return fail(c, RKDG_ERR_INVALID, "element offsets must cover the mesh");
+  std::vector<int> prob(c->ne);
+  std::vector<double> phmin(nprob, 1e300);
+  for (int p = 0; p < nprob; ++p) {
+    if (elem_offsets[p + 1] <= elem_offsets[p] || !(gamma[p] > 1.0) || covolume[p] < 0.0)
+      return fail(c, RKDG_ERR_INVALID, "invalid problem", p);
+    for (int e = elem_offsets[p]; e < elem_offsets[p + 1]; ++e) {
+      prob[e] = p;
+      phmin[p] = std::min(phmin[p], c->h_ehmin[e]);
+    }
+  }
+  // a problem must not share a face with another one
+  for (int lf = 0; lf < c->nfpe; ++lf)
+    for (int e = 0; e < c->ne; ++e) {
+      const int nb = c->h_fnbr[(size_t)lf * c->ne + e];
+      if (nb >= 0 && prob[nb] != prob[e])
+        return fail(c, RKDG_ERR_INVALID, "problems are connected through a face", e);
+    }
+  c->nprob = nprob;
+  c->h_poff.assign(elem_offsets, elem_offsets + nprob + 1);
+  CUDA_TRY(c, dalloc(c->d_prob, (size_t)c->ne));
+  CUDA_TRY(c, dalloc(c->d_pgamma, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_pcov, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_phmin, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_pdt, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_pdtr, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_pt, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_psum, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_pactive, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_psteps, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_nactive, (size_t)1));
+  CUDA_TRY(c, dalloc(c->d_pmcs, (size_t)4 * nprob));
+  CUDA_TRY(c, cudaMemcpy(c->d_prob, prob.data(), prob.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->d_pgamma, gamma, nprob * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->d_pcov, covolume, nprob * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->d_phmin, phmin.data(), nprob * sizeof(double), cudaMemcpyHostToDevice));
+  return RKDG_OK;
+}
+
+int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0, int dt_mode,
+                   int max_steps, int use_graph, int* steps_out, double* t_out, double* sum_dt_out) {
+  NEED_MESH(c);
+  if (c->nprob <= 0) return fail(c, RKDG_ERR_INVALID, "rkdg_batch_setup was not called");
+  if (!x || dt_mode < 0 || dt_mode > 2 || !(t_end > 0.0) || (dt_mode == 2 && !(dt0 > 0.0)))
+    return fail(c, RKDG_ERR_INVALID, "invalid batch run arguments");
+  if (max_steps <= 0 && !(t_end < 1e20)) return fail(c, RKDG_ERR_INVALID, "unbounded batch run");
+  int st = ensure_scratch(c);
+  if (st) return st;
+  const int np = c->nprob;
+  const bool fp32 = c->precision != RKDG_FP64;
+  const long long n = c->ndofs * c->neq;
+  rkdg::BatchState bs;
+  std::memset(&bs, 0, sizeof bs);
+  bs.t_end = t_end;
+  bs.cfl = cfl;
+  bs.denom = 2.0 * c->p + 1.0;
+  bs.nprob = np;
+  bs.dt_mode = dt_mode;
+  bs.max_steps = max_steps;
+  bs.hmin = c->d_phmin;
+  bs.dt = c->d_pdt;
+  bs.dtr = c->d_pdtr;
+  bs.t = c->d_pt;
+  bs.sum_dt = c->d_psum;
+  bs.active = c->d_pactive;
+  bs.steps = c->d_psteps;
+  bs.nactive = c->d_nactive;
+  bs.mcs_last = c->d_pmcs + (size_t)(c->s - 1) * np;
+  // initial dt: face-only max speed per problem (main.cpp:467-484)
+  {
+    std::vector<int> ones(np, 1);
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_pactive, ones.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, zero_slot(c, c->s - 1, true));
+    EpiParams<double> ep;
+    std::memset(&ep, 0, sizeof ep);
+    RhsParams P = rhs_params(c, 0, 1, 0);
+    set_batch(c, P, c->s - 1);
+    CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,0, P, x, &ep, c->stream));
+    CUDA_TRY(c, rkdg::launch_batch_init(bs, dt0, c->stream));
+    c->launches += 2;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  }
+  if (fp32) {
+    CUDA_TRY(c, rkdg::launch_split(n, x, c->d_xh, c->d_xl, c->stream));
+    c->launches++;
+  }
+  const long long l0 = c->launches;
+  long long per_step = 0;
+  if (use_graph) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    CUDA_TRY(c, cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    CUDA_TRY(c, cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    CUDA_TRY(c, cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CUDA_TRY(c, cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal));
+    st = fp32 ? enqueue_step32(c, 0.0, true) : enqueue_step64(c, x, 0.0, true);
+    cudaError_t ce = st ? cudaSuccess : rkdg::launch_batch_control(bs, h, 1, c->stream);
+    cudaGraph_t captured = nullptr;
+    cudaError_t ce2 = cudaStreamEndCapture(c->stream, &captured);
+    per_step = c->launches - l0 + 1;
+    if (st || ce != cudaSuccess || ce2 != cudaSuccess) {
+      cudaGraphDestroy(g);
+      if (st) return st;
+      return fail(c, RKDG_ERR_CUDA, std::string("graph capture failed: ") +
+                                        cudaGetErrorString(ce != cudaSuccess ? ce : ce2));
+    }
+    cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+    if (ie != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return fail(c, RKDG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+    }
+    cudaError_t le = cudaGraphLaunch(ge, c->stream);
+    cudaError_t se = cudaStreamSynchronize(c->stream);
+    cudaGraphExecDestroy(ge);
+    cudaGraphDestroy(g);
+    if (le != cudaSuccess || se != cudaSuccess)
+      return fail(c, RKDG_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(le != cudaSuccess ? le : se));
+  } else {
+    int nact = np;
+    long long steps = 0;
+    while (nact > 0) {
+      st = fp32 ? enqueue_step32(c, 0.0, true) : enqueue_step64(c, x, 0.0, true);
+      if (st) return st;
+      CUDA_TRY(c, rkdg::launch_batch_control(bs, cudaGraphConditionalHandle(), 0, c->stream));
+      c->launches++;
+      if (per_step == 0) per_step = c->launches - l0;
+      CUDA_TRY(c, cudaMemcpyAsync(c->h_err, c->d_nactive, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      nact = c->h_err[0];
+      if (++steps > 100000000LL) return fail(c, RKDG_ERR_INVALID, "batch run did not terminate");
+    }
+  }
+  if (fp32) {
+    CUDA_TRY(c, rkdg::launch_join(n, c->d_xh, c->d_xl, x, c->stream));
+    c->launches++;
+  }
+  std::vector<int> steps(np);
+  std::vector<double> tt(np), sd(np);
+  CUDA_TRY(c, cudaMemcpyAsync(steps.data(), c->d_psteps, np * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(tt.data(), c->d_pt, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(sd.data(), c->d_psum, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  st = read_mcs(c, 0, nullptr);
+  if (st) return st;
+  if (use_graph) {
+    int mx = 0;
+    for (int v : steps) mx = std::max(mx, v);
+    c->launches = l0 + per_step * mx;
+  }
+  for (int p = 0; p < np; ++p) {
+    if (steps_out) steps_out[p] = steps[p];
+    if (t_out) t_out[p] = tt[p];
+    if (sum_dt_out) sum_dt_out[p] = sd[p];
+  }
   return RKDG_OK;
 }
 

@@ -11,6 +11,11 @@ bool generic_supported(int geom, int p);
 // prec: 0 = FP64, 1 = FP32.  ep points to EpiParams<double> or EpiParams<float>.
 cudaError_t launch_rhs(int geom, int p, int prec, const RhsParams& prm, const void* u,
                        const void* ep, cudaStream_t st);
+// Same with a hexahedral kernel variant (0 default, 1 warp per element, 2 team).
+cudaError_t launch_rhs_v(int variant, int geom, int p, int prec, const RhsParams& prm,
+                         const void* u, const void* ep, cudaStream_t st);
+cudaError_t launch_hex_variant(int variant, int p, int prec, const RhsParams& prm, const void* u,
+                               const void* ep, cudaStream_t st);
 // mode: 0 = double in place, 1 = float in place, 2 = float pair (u = hi, ulo = lo)
 cudaError_t launch_limit(int geom, int p, int mode, const LimParams& prm, void* u, float* ulo,
                          cudaStream_t st);
@@ -31,6 +36,10 @@ cudaError_t launch_copy_f(long long n, const float* x, float* y, cudaStream_t st
 cudaError_t launch_totals(int nd, int neq, int ne, long long ndofs, const RefTables* tab,
                           const double* wdet, const double* u, double* partial, int nblocks,
                           cudaStream_t st);
+
+cudaError_t launch_batch_init(const BatchState& bs, double dt0, cudaStream_t st);
+cudaError_t launch_batch_control(const BatchState& bs, cudaGraphConditionalHandle h,
+                                 int use_handle, cudaStream_t st);
 
 // Template launch helpers shared by the per-geometry translation units.
 template <int G, int P>

@@ -31,6 +31,12 @@ cudaError_t launch_rhs(int geom, int p, int prec, const RhsParams& prm, const vo
 #undef CALL_RHS
 }
 
+cudaError_t launch_rhs_v(int variant, int geom, int p, int prec, const RhsParams& prm,
+                         const void* u, const void* ep, cudaStream_t st) {
+  if (geom == 5 && variant != 0) return launch_hex_variant(variant, p, prec, prm, u, ep, st);
+  return launch_rhs(geom, p, prec, prm, u, ep, st);
+}
+
 cudaError_t launch_limit(int geom, int p, int mode, const LimParams& prm, void* u, float* ulo,
                          cudaStream_t st) {
 #define CALL_LIM(G, P) launch_limit_t<G, P>(mode, prm, u, ulo, st)
@@ -161,6 +167,72 @@ __global__ void k_totals(int nd, int neq, int ne, long long ndofs, const RefTabl
     if (threadIdx.x == 0) partial[k * gridDim.x + blockIdx.x] = red[0];
     __syncthreads();
   }
+}
+
+// ---- batched problems: device-side time control ------------------------------
+__device__ __forceinline__ double bits_to_double(unsigned long long b) {
+  return __longlong_as_double((long long)b);
+}
+
+// Initial dt per problem from its face-only max speed (main.cpp:467-484) or
+// the given constant, and the first step's dt_real.
+__global__ void k_batch_init(BatchState bs, double dt0) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < bs.nprob; p += gridDim.x * blockDim.x) {
+    double dt = dt0;
+    if (bs.dt_mode != 2) dt = bs.cfl * bs.hmin[p] / bits_to_double(bs.mcs_last[p]) / bs.denom;
+    bs.dt[p] = dt;
+    bs.t[p] = 0.0;
+    bs.sum_dt[p] = 0.0;
+    bs.steps[p] = 0;
+    const bool ok = isfinite(dt) && dt > 0.0;
+    bs.active[p] = ok ? 1 : 0;
+    bs.dtr[p] = fmin(dt, bs.t_end);
+  }
+}
+
+// After a step: per-problem bookkeeping of main.cpp:512-553,701-733 (dt from
+// the last stage's max speed, t += new dt, done test), the count of problems
+// still running, and the while-condition of the graph that drives the loop.
+__global__ void k_batch_control(BatchState bs, cudaGraphConditionalHandle handle, int use_handle) {
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  int local = 0;
+  for (int p = threadIdx.x; p < bs.nprob; p += blockDim.x) {
+    if (!bs.active[p]) continue;
+    bs.steps[p] += 1;
+    bs.sum_dt[p] += bs.dtr[p];
+    double dt = bs.dt[p];
+    if (bs.dt_mode == 0) dt = bs.cfl * bs.hmin[p] / bits_to_double(bs.mcs_last[p]) / bs.denom;
+    const double t = bs.t[p] + dt;
+    bs.dt[p] = dt;
+    bs.t[p] = t;
+    bool done = t >= bs.t_end - 1e-8 * dt;
+    if (bs.max_steps > 0 && bs.steps[p] >= bs.max_steps) done = true;
+    if (!isfinite(dt) || !(dt > 0.0)) done = true;
+    if (done) {
+      bs.active[p] = 0;
+    } else {
+      bs.dtr[p] = fmin(dt, bs.t_end - t);
+      ++local;
+    }
+  }
+  if (local) atomicAdd(&cnt, local);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bs.nactive[0] = cnt;
+    if (use_handle) cudaGraphSetConditional(handle, cnt > 0 ? 1u : 0u);
+  }
+}
+
+cudaError_t launch_batch_init(const BatchState& bs, double dt0, cudaStream_t st) {
+  k_batch_init<<<(bs.nprob + 127) / 128, 128, 0, st>>>(bs, dt0);
+  return cudaGetLastError();
+}
+cudaError_t launch_batch_control(const BatchState& bs, cudaGraphConditionalHandle h, int use_handle,
+                                 cudaStream_t st) {
+  k_batch_control<<<1, 1024, 0, st>>>(bs, h, use_handle);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_totals(int nd, int neq, int ne, long long ndofs, const RefTables* tab,

@@ -402,6 +402,13 @@ bool build_ref_tables(int geom, int p, RefTables& T, std::vector<FacePoint>* fpt
         for (int q = 0; q < f.n; ++q) {
           double xi[3];
           face_to_elem(geom, lf, &f.x[q * 2], xi);
+          int ia = -1, ib = -1;
+          for (int a = 0; a < s1.n; ++a) {
+            if (std::fabs(s1.x[a] - xi[t0]) < 1e-12) ia = a;
+            if (std::fabs(s1.x[a] - xi[t1]) < 1e-12) ib = a;
+          }
+          if (ia < 0 || ib < 0) return false;
+          T.fab[lf][q] = ia + s1.n * ib;
           for (int i0 = 0; i0 < B.n1; ++i0)
             for (int i1 = 0; i1 < B.n1; ++i1)
               T.B2[lf][q][i0 * B.n1 + i1] = lag(B.x1, i0, xi[t0]) * lag(B.x1, i1, xi[t1]);

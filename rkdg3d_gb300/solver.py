@@ -39,6 +39,7 @@ IND_NOWHERE, IND_EVERYWHERE, IND_BJ = 0, 1, 2
 FUN_BJ, FUN_VENKATAKRISHNAN, FUN_MICHALAK = 0, 1, 2
 QUIRK_MULTIPLIER_ONCE = 1
 FP64, FP32_BULK = 0, 1
+TUNE_HEX_KERNEL = 1
 
 # Butcher tableaux in MFEM lower-triangular packing.
 # True SSP-RK3 (Shu-Osher third order) in Butcher form.
@@ -175,6 +176,9 @@ class Context:
         self._chk(self._L.rkdg_set_precision(self.h, precision))
         self.precision = precision
 
+    def set_tuning(self, key: int, value: int):
+        self._chk(self._L.rkdg_set_tuning(self.h, key, value))
+
     def set_stream(self, stream_ptr: int | None):
         self._chk(self._L.rkdg_set_stream(self.h, stream_ptr))
 
@@ -242,6 +246,26 @@ class Context:
 
     def synchronize(self):
         self._chk(self._L.rkdg_synchronize(self.h))
+
+    # -- batched independent problems -----------------------------------------
+    def batch_setup(self, elem_offsets, gammas, covolumes):
+        off = np.ascontiguousarray(elem_offsets, dtype=np.int32)
+        g = np.ascontiguousarray(gammas, dtype=np.float64)
+        b = np.ascontiguousarray(covolumes, dtype=np.float64)
+        self.nprob = len(g)
+        self._chk(self._L.rkdg_batch_setup(self.h, self.nprob, off.ctypes.data_as(_capi._ip),
+                                           g.ctypes.data_as(_capi._dp), b.ctypes.data_as(_capi._dp)))
+
+    def batch_run(self, x, t_end: float, cfl: float = 0.3, dt0: float = 0.0, dt_mode: int = 0,
+                  max_steps: int = 0, use_graph: bool = True) -> dict:
+        np_ = self.nprob
+        steps = np.zeros(np_, np.int32)
+        t = np.zeros(np_)
+        sdt = np.zeros(np_)
+        self._chk(self._L.rkdg_batch_run(self.h, _ptr(x), t_end, cfl, dt0, dt_mode, max_steps,
+                                         int(use_graph), steps.ctypes.data_as(_capi._ip),
+                                         t.ctypes.data_as(_capi._dp), sdt.ctypes.data_as(_capi._dp)))
+        return {"steps": steps, "t": t, "sum_dt": sdt}
 
 
 # ---- reference-named mirrors -------------------------------------------------

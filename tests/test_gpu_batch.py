@@ -1,0 +1,72 @@
+"""Batched uneven solves (many independent Riemann problems in one context,
+one CUDA-graph launch) against per-problem oracle runs."""
+import numpy as np
+import pytest
+import torch
+
+from oracle.refcpu import Oracle
+from rkdg3d_gb300 import cases
+from rkdg3d_gb300.solver import FP32_BULK, FP64, Context
+from tests.helpers import rel_l1
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(nprob=8, nmin=20, nmax=60, t_end=0.05, seed=4):
+    return cases.batched_riemann(nprob=nprob, nmin=nmin, nmax=nmax, seed=seed, t_end=t_end)
+
+
+def _ctx(bc, prec=FP64):
+    ctx = Context(bc.mesh, bc.order, device=0, precision=prec)
+    cases.configure_batch(bc, ctx)
+    return ctx
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_batch_matches_per_problem_oracle(cuda, use_graph):
+    bc = _batch()
+    ctx = _ctx(bc)
+    x0 = bc.project(ctx.node_coords())
+    xd = torch.tensor(x0, dtype=torch.float64, device="cuda")
+    info = ctx.batch_run(xd, bc.t_end, bc.cfl, use_graph=use_graph)
+    x = xd.cpu().numpy().reshape(4, -1)
+    nd = 4
+    for p, c in enumerate(bc.cases):
+        orc = Oracle(c.mesh, c.order)
+        cases.configure_oracle(c, orc)
+        xp0 = cases.project(c, orc.node_coords())
+        xr, ir = orc.run(xp0, c.t_end, c.cfl)
+        rng = np.random.default_rng(p)
+        xs, _ = orc.run(xp0 * (1 + 1e-15 * rng.uniform(-1, 1, xp0.size)), c.t_end, c.cfl)
+        assert info["steps"][p] == ir["steps"], p
+        assert info["t"][p] == pytest.approx(ir["t"], rel=1e-9)
+        e0, e1 = bc.offsets[p], bc.offsets[p + 1]
+        rho = x[0, e0 * nd:e1 * nd]
+        d_gpu = rel_l1(rho, xr[:orc.ndofs])
+        d_self = rel_l1(xs[:orc.ndofs], xr[:orc.ndofs])
+        # limited runs amplify round-off (see test_full_run_sod)
+        assert d_gpu < 1e-3 and d_gpu < max(10 * d_self, 1e-10), (p, d_gpu, d_self)
+
+
+def test_batch_graph_equals_host_loop(cuda):
+    bc = _batch(nprob=6, seed=7)
+    ctx = _ctx(bc)
+    x0 = bc.project(ctx.node_coords())
+    a = torch.tensor(x0, dtype=torch.float64, device="cuda")
+    b = a.clone()
+    ia = ctx.batch_run(a, bc.t_end, bc.cfl, use_graph=True)
+    ib = ctx.batch_run(b, bc.t_end, bc.cfl, use_graph=False)
+    assert np.array_equal(ia["steps"], ib["steps"])
+    assert torch.equal(a, b)
+
+
+def test_batch_mixed_close_to_fp64(cuda):
+    bc = _batch(nprob=6, seed=9)
+    c64, c32 = _ctx(bc, FP64), _ctx(bc, FP32_BULK)
+    x0 = bc.project(c64.node_coords())
+    a = torch.tensor(x0, dtype=torch.float64, device="cuda")
+    b = a.clone()
+    c64.batch_run(a, bc.t_end, bc.cfl)
+    c32.batch_run(b, bc.t_end, bc.cfl)
+    n = a.numel() // 4
+    assert rel_l1(b.cpu().numpy()[:n], a.cpu().numpy()[:n]) < 1e-4

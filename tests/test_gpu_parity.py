@@ -106,6 +106,28 @@ def test_rhs_walls(cuda, geom, order, n, bc, rs, avg):
     assert abs(m - m_ref) <= 1e-13 * abs(m_ref)
 
 
+@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("walled", [False, True])
+def test_rhs_hex_kernel_variants(cuda, variant, order, walled):
+    """Both hexahedral kernels (warp per element, five-lane team) in FP64."""
+    from rkdg3d_gb300.solver import TUNE_HEX_KERNEL
+    case = (walled_case(M.GEOM_CUBE, 3, order, RS_HLLC, AVG_EINFELDT, bc=BC_SLIP) if walled
+            else periodic_case(M.GEOM_CUBE, 3, order, RS_LLF))
+    ctx, orc = pair(case)
+    ctx.set_tuning(TUNE_HEX_KERNEL, variant)
+    x = random_state(ctx.node_coords(), seed=21)
+    y_ref, m_ref = orc.rhs(x)
+    y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    m = ctx.rhs(dev(x), y)
+    assert rel_l1(y.cpu().numpy(), y_ref) < RHS_TOL
+    assert abs(m - m_ref) <= 1e-13 * m_ref
+    xs_ref, _ = orc.step(x, 1e-3)
+    xd = dev(x)
+    ctx.step(xd, 1e-3)
+    assert rel_l1(xd.cpu().numpy(), xs_ref) < RHS_TOL
+
+
 def test_node_coords_match_oracle(cuda):
     for geom, order in [(M.GEOM_SQUARE, 2), (M.GEOM_TRIANGLE, 2), (M.GEOM_CUBE, 2)]:
         case = walled_case(geom, 3, order, RS_RUSANOV)
