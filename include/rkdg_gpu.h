@@ -91,6 +91,14 @@ int rkdg_set_physics(rkdg_ctx* ctx, int rsolver, int averaging, double gamma,
  * builds every device face / element / stencil table.  Idempotent; call it
  * after every AMR adapt (main.cpp:610-611). */
 int rkdg_upload_mesh(rkdg_ctx* ctx, const rkdg_mesh_desc* mesh);
+/* Deviations from the shipped reference, off by default.
+ * RKDG_QUIRK_HLLC_NEGATIVE_SPEED_OK: the reference treats any negative face
+ * wave speed as a non-physical state and exits (face_integrator.cpp:214-218),
+ * which also fires on HLLC's signed max(SL, SR) (rs_hllc.cpp:98) in
+ * supersonic flow against the face normal; with this flag only the -1 of a
+ * non-physical state is an error. */
+enum { RKDG_QUIRK_HLLC_NEGATIVE_SPEED_OK = 1 };
+int rkdg_set_solver_quirks(rkdg_ctx* ctx, int flags);
 /* Replaces CaseManager::addBoundaryIntegrators (case_manager.cpp:614-820)
  * for one boundary attribute.  state: conservative variables or NULL. */
 int rkdg_set_bc(rkdg_ctx* ctx, int attr, int type, const double* state);
@@ -172,6 +180,23 @@ int rkdg_batch_setup(rkdg_ctx* ctx, int nprob, const int* elem_offsets,
 int rkdg_batch_run(rkdg_ctx* ctx, double* x_dev, double t_end, double cfl, double dt0,
                    int dt_mode, int max_steps, int use_graph, int* steps_out,
                    double* t_out, double* sum_dt_out);
+/* ---- discrete adjoint (FP64 path) ------------------------------------------
+ * Vector-Jacobian products of the hot path (no counterpart in the reference,
+ * which has no adjoint).  Supported: triangles P1, quads Q1/Q2, hexes Q1.
+ * xbar = (d FE_Evolution::Mult / dx)^T kbar: */
+int rkdg_rhs_vjp(rkdg_ctx* ctx, const double* x_dev, const double* kbar_dev, double* xbar_dev);
+/* zbar = (d Limiter::update / dz)^T ybar (active branch of min/max and of the
+ * indicator thresholds; Venkatakrishnan is differentiated exactly): */
+int rkdg_limit_vjp(rkdg_ctx* ctx, const double* z_dev, const double* ybar_dev, double* zbar_dev);
+/* Reverse of one ExplicitRKLimitedSolver::Step at x_n with step dt: xbar holds
+ * the adjoint of x_{n+1} on entry and the adjoint of x_n on return. */
+int rkdg_step_vjp(rkdg_ctx* ctx, const double* x_dev, double dt, double* xbar_dev);
+/* Gradient through nsteps fixed-dt steps from x0: xbar holds dJ/dx(T) on entry
+ * and dJ/dx0 on return; states are checkpointed every `checkpoint_every`
+ * steps and recomputed between checkpoints.  xT_dev (may be NULL) receives
+ * x(T). */
+int rkdg_adjoint_run(rkdg_ctx* ctx, const double* x0_dev, int nsteps, double dt,
+                     int checkpoint_every, double* xbar_dev, double* xT_dev);
 /* Number of kernels this context launched since creation (instrumentation). */
 long long rkdg_kernel_launches(rkdg_ctx* ctx);
 

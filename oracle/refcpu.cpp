@@ -643,6 +643,7 @@ struct ref_ctx {
   std::vector<std::vector<int>> el_el;  // ElementToElementTable
   std::map<int, BC> bcs;
   int lim = 0, ind = 0, fun = 2, last_hope = 1, quirks = 0;
+  int solver_quirks = 0;  // bit 0: a negative HLLC speed is not an error
   int s = 3;
   std::vector<double> a, b, cc;
   Rule frule, lrule;             // face rule (RHS), order-2 face rule (limiter)
@@ -884,7 +885,7 @@ bool face_item(const ref_ctx* c, const double* x, int face, const BC* bc, double
     for (int i = 0; i < dim; ++i) nor[i] *= inv;
     if (bc) compute_right_state(c, *bc, u1, u2, nor);
     const double mcs = rs_eval(c->P, c->rs, c->avg, u1, u2, nor, fluxN);
-    if (mcs < 0) {
+    if (mcs < 0 && (!(c->solver_quirks & 1) || mcs == -1.0)) {
       bad = face;
       return false;
     }
@@ -1174,6 +1175,11 @@ int ref_set_limiter(ref_ctx* c, int limiter, int indicator, int function, int la
   c->fun = function;
   c->last_hope = last_hope;
   c->quirks = quirks;
+  return REF_OK;
+}
+
+int ref_set_solver_quirks(ref_ctx* c, int flags) {
+  c->solver_quirks = flags;
   return REF_OK;
 }
 

@@ -66,6 +66,9 @@ int ref_set_limiter(ref_ctx* c, int limiter, int indicator, int function,
                     int last_hope, int quirks);
 int ref_set_tableau(ref_ctx* c, int s, const double* a, const double* b,
                     const double* cc);
+/* bit 0: a negative HLLC wave speed (signed max(SL,SR)) is not treated as a
+ * non-physical state (the reference exits on it). */
+int ref_set_solver_quirks(ref_ctx* c, int flags);
 void ref_set_threads(int n);
 
 long long ref_ndofs(ref_ctx* c);   /* scalar nodes (NDofs) */

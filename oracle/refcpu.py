@@ -43,6 +43,7 @@ def lib():
         L.ref_set_limiter.argtypes = [C.c_void_p] + [C.c_int] * 5
         L.ref_set_tableau.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
         L.ref_set_threads.argtypes = [C.c_int]
+        L.ref_set_solver_quirks.argtypes = [C.c_void_p, C.c_int]
         L.ref_ndofs.restype = C.c_longlong
         L.ref_ndofs.argtypes = [C.c_void_p]
         L.ref_nd.argtypes = [C.c_void_p]
@@ -123,6 +124,9 @@ class Oracle:
 
     def set_limiter(self, limiter=0, indicator=0, function=2, last_hope=1, quirks=0):
         self._chk(lib().ref_set_limiter(self.h, limiter, indicator, function, last_hope, quirks))
+
+    def set_solver_quirks(self, flags):
+        self._chk(lib().ref_set_solver_quirks(self.h, int(flags)))
 
     def set_tableau(self, s, a, b, c):
         a = np.ascontiguousarray(a if len(a) else [0.0], dtype=np.float64)

@@ -31,6 +31,7 @@ _SIGS = [
     ("rkdg_set_tableau", C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
     ("rkdg_set_precision", C.c_int, [_vp, C.c_int]),
     ("rkdg_set_tuning", C.c_int, [_vp, C.c_int, C.c_int]),
+    ("rkdg_set_solver_quirks", C.c_int, [_vp, C.c_int]),
     ("rkdg_sizes", C.c_int, [_vp, C.POINTER(C.c_longlong), _ip, _ip]),
     ("rkdg_node_coords_host", C.c_int, [_vp, _dp]),
     ("rkdg_hmin", C.c_int, [_vp, _dp]),
@@ -46,6 +47,10 @@ _SIGS = [
     ("rkdg_batch_setup", C.c_int, [_vp, C.c_int, _ip, _dp, _dp]),
     ("rkdg_batch_run", C.c_int, [_vp, _vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                                  C.c_int, _ip, _dp, _dp]),
+    ("rkdg_rhs_vjp", C.c_int, [_vp, _vp, _vp, _vp]),
+    ("rkdg_limit_vjp", C.c_int, [_vp, _vp, _vp, _vp]),
+    ("rkdg_step_vjp", C.c_int, [_vp, _vp, C.c_double, _vp]),
+    ("rkdg_adjoint_run", C.c_int, [_vp, _vp, C.c_int, C.c_double, C.c_int, _vp, _vp]),
     ("rkdg_kernel_launches", C.c_longlong, [_vp]),
 ]
 

@@ -37,6 +37,7 @@ class Case:
     dt0: float = 0.0
     max_steps: int = 0
     ic: object = None         # callable(coords[dim, NDofs]) -> primitive (rho, u, v, [w], p)
+    solver_quirks: int = 0    # RKDG_QUIRK_* of rkdg_set_solver_quirks
 
     @property
     def dim(self) -> int:
@@ -221,7 +222,7 @@ def batched_riemann(nprob=256, nmin=100, nmax=2000, seed=0, order=1, t_end=0.15,
                        bcs=[(1, BC_SLIP, None), (3, BC_SLIP, None), (2, BC_OPEN, None),
                             (4, BC_OPEN, None)],
                        limiter=(LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 0), tableau=tableau,
-                       t_end=t_end, cfl=cfl, ic=ic))
+                       t_end=t_end, cfl=cfl, ic=ic, solver_quirks=1))
     offs = np.concatenate([[0], np.cumsum([c.mesh.num_elements for c in cs])]).astype(np.int32)
     return BatchCase(cs, union_mesh([c.mesh for c in cs]), offs, gam, cov, order, t_end, cfl)
 
@@ -237,6 +238,7 @@ def configure_oracle(case: Case, oracle) -> None:
         oracle.set_bc(attr, t, st)
     oracle.set_limiter(*case.limiter)
     oracle.set_tableau(*case.tableau)
+    oracle.set_solver_quirks(case.solver_quirks)
 
 
 def configure_context(case: Case, ctx) -> None:
@@ -244,6 +246,7 @@ def configure_context(case: Case, ctx) -> None:
     rs = RiemannSolver(case.averaging)
     rs.code = case.rsolver
     ctx.set_physics(rs, Physics(case.gamma, case.covolume, 1.0))
+    ctx.set_solver_quirks(case.solver_quirks)
     for attr, t, st in case.bcs:
         ctx.set_bc(attr, t, st)
     ctx.set_limiter(*case.limiter)

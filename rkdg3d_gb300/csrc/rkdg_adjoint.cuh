@@ -1,0 +1,340 @@
+// Discrete adjoint (vector-Jacobian products) of the FP64 right-hand side and
+// limiter, one thread per element, dense reference operators.
+//
+// Right-hand side y = M^-1 z(u): given k_bar, r = M^-1 k_bar (M symmetric),
+// then u_bar = (dz/du)^T r with
+//   volume  z_j += sum_m sum_r D[r][j][m] G_r(u_m),  G_r = sum_d adj(J)[r][d] F_d
+//           -> u_bar_m += (dF_d/du)^T (sum_r adj[r][d] sum_j D[r][j][m] r_j)
+//   faces   z_e1 -= w|J| Fhat B1,  z_e2 += w|J| Fhat B2
+//           -> Fhat_bar = w|J| (-B1 r_e1 + B2 r_e2),
+//              u_bar_own += B_own (dFhat/du_own)^T Fhat_bar
+// Jacobians of the Euler flux and of the numerical flux (with the ghost state
+// of boundary faces) come from the same templates instantiated with Dual<5>,
+// so every branch is differentiated on its active side.  Each element
+// differentiates only with respect to its own trace, so no atomics are needed.
+//
+// Limiter (Multi, BJ-family indicator): the limited values are
+// v_i = mean + m^nd (u_i - mean) (the nd-fold application of
+// limiter_multiplier.cpp:24-38), m = density indicator.  The indicator is
+// recomputed with Dual numbers over the element's density DOFs and the
+// density means of its stencil; the derivative with respect to a
+// neighbour's mean is stored per face and gathered by the neighbour.
+#pragma once
+
+#include "rkdg_common.h"
+#include "rkdg_dual.cuh"
+#include "rkdg_generic.cuh"
+#include "rkdg_physics.cuh"
+
+namespace rkdg {
+
+// r = M^-1 k_bar per element (reference inverse mass / det J).
+template <int G, int P>
+__global__ void k_minv_apply(int ne, long long ndofs, const RefTables* tab, const double* egeo,
+                             const double* __restrict__ kb, double* __restrict__ r) {
+  using E = El<G, P>;
+  constexpr int ND = E::ND, NEQ = E::NEQ, DIM = E::DIM;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const double idet = egeo[(long long)(DIM * DIM) * ne + e];
+  for (int k = 0; k < NEQ; ++k) {
+    double in[ND];
+#pragma unroll
+    for (int j = 0; j < ND; ++j) in[j] = kb[k * ndofs + (long long)e * ND + j];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      double v = 0.0;
+#pragma unroll
+      for (int j = 0; j < ND; ++j) v += tab->Minv[j][i] * in[j];
+      r[k * ndofs + (long long)e * ND + i] = v * idet;
+    }
+  }
+}
+
+template <int G, int P>
+__global__ void __launch_bounds__(64)
+    k_rhs_vjp(const RhsParams prm, const double* __restrict__ u, const double* __restrict__ r,
+              double* __restrict__ ubar) {
+  using E = El<G, P>;
+  constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NFPE = E::NFPE, NQF = E::NQF;
+  using D = Dual<NEQ>;
+  const RefTables* T = prm.tab;
+  const int ne = prm.ne;
+  const long long NDa = prm.ndofs;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const D gamma = D(prm.gamma), cov = D(prm.covolume);
+  double acc[NEQ][ND];
+  for (int k = 0; k < NEQ; ++k)
+    for (int s = 0; s < ND; ++s) acc[k][s] = 0.0;
+  // faces
+  const double* fg = (const double*)prm.fgeo;
+  for (int lf = 0; lf < NFPE; ++lf) {
+    const int nb = prm.fnbr[lf * ne + e];
+    if (nb == -1) continue;
+    const int code = prm.fcode[lf * ne + e];
+    D n[DIM];
+    for (int c = 0; c < DIM; ++c) n[c] = D(fg[(long long)(lf * (DIM + 1) + c) * ne + e]);
+    const double jac = fg[(long long)(lf * (DIM + 1) + DIM) * ne + e];
+    const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
+    int e1 = e, lf1 = lf, e2 = nb, lf2 = lfo;
+    if (nb >= 0 && side) {
+      e1 = nb;
+      lf1 = lfo;
+      e2 = e;
+      lf2 = lf;
+    }
+    for (int q = 0; q < NQF; ++q) {
+      const int q2 = T->perm[pid][q];
+      const double* B1 = T->B[lf1][q];
+      const double* B2 = nb >= 0 ? T->B[lf2][q2] : nullptr;
+      D s1[NEQ], s2[NEQ];
+      double fbar[NEQ];
+      for (int k = 0; k < NEQ; ++k) {
+        double v1 = 0.0, r1 = 0.0;
+        for (int s = 0; s < ND; ++s) {
+          v1 += u[k * NDa + (long long)e1 * ND + s] * B1[s];
+          r1 += r[k * NDa + (long long)e1 * ND + s] * B1[s];
+        }
+        double v2 = 0.0, r2 = 0.0;
+        if (nb >= 0)
+          for (int s = 0; s < ND; ++s) {
+            v2 += u[k * NDa + (long long)e2 * ND + s] * B2[s];
+            r2 += r[k * NDa + (long long)e2 * ND + s] * B2[s];
+          }
+        const bool own1 = (nb < 0) || side == 0;
+        s1[k] = own1 ? D::var(v1, k) : D(v1);
+        s2[k] = own1 ? D(v2) : D::var(v2, k);
+        fbar[k] = T->wf[q] * jac * (-r1 + (nb >= 0 ? r2 : 0.0));
+      }
+      if (nb < 0) {
+        const BCSlot& bc = prm.bc[-2 - nb];
+        right_state<DIM>(bc.type, bc.state, s1, s2, n);
+      }
+      D F[NEQ];
+      riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg);
+      const double* Bo = T->B[lf][side ? q2 : q];
+      for (int kk = 0; kk < NEQ; ++kk) {
+        double g = 0.0;
+        for (int k = 0; k < NEQ; ++k) g += fbar[k] * F[k].d[kk];
+        for (int s = 0; s < ND; ++s) acc[kk][s] += Bo[s] * g;
+      }
+    }
+  }
+  // volume
+  double adj[DIM][DIM];
+  for (int rr = 0; rr < DIM; ++rr)
+    for (int d = 0; d < DIM; ++d) adj[rr][d] = ((const double*)prm.egeo)[(long long)(rr * DIM + d) * ne + e];
+  for (int m = 0; m < ND; ++m) {
+    D st[NEQ];
+    for (int k = 0; k < NEQ; ++k) st[k] = D::var(u[k * NDa + (long long)e * ND + m], k);
+    D F[NEQ][DIM];
+    flux_and_speed<DIM>(st, F, gamma, cov);
+    for (int k = 0; k < NEQ; ++k) {
+      double gbar[DIM];
+      for (int rr = 0; rr < DIM; ++rr) {
+        double s = 0.0;
+        for (int j = 0; j < ND; ++j) s += T->D[rr][j][m] * r[k * NDa + (long long)e * ND + j];
+        gbar[rr] = s;
+      }
+      for (int d = 0; d < DIM; ++d) {
+        double fb = 0.0;
+        for (int rr = 0; rr < DIM; ++rr) fb += adj[rr][d] * gbar[rr];
+        for (int kk = 0; kk < NEQ; ++kk) acc[kk][m] += fb * F[k][d].d[kk];
+      }
+    }
+  }
+  for (int k = 0; k < NEQ; ++k)
+    for (int s = 0; s < ND; ++s) ubar[k * NDa + (long long)e * ND + s] = acc[k][s];
+}
+
+// Limiter VJP, own part; cross[lf][e] receives the derivative with respect to
+// the density mean of the neighbour through face lf.
+template <int G, int P>
+__global__ void __launch_bounds__(64)
+    k_limit_vjp(const LimParams prm, const double* __restrict__ z, const double* __restrict__ ybar,
+                double* __restrict__ zbar, double* __restrict__ cross) {
+  using E = El<G, P>;
+  constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NFPE = E::NFPE, NQL = E::NQL, NV = E::NV;
+  constexpr int NVAR = ND + 1 + NFPE;
+  using D = Dual<NVAR>;
+  const RefTables* T = prm.tab;
+  const int ne = prm.ne;
+  const long long NDa = prm.ndofs;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  double el[NEQ][ND], yb[NEQ][ND], um[NEQ];
+  for (int k = 0; k < NEQ; ++k) {
+    um[k] = prm.means[(long long)k * ne + e];
+    for (int j = 0; j < ND; ++j) {
+      el[k][j] = z[k * NDa + (long long)e * ND + j];
+      yb[k][j] = ybar[k * NDa + (long long)e * ND + j];
+    }
+  }
+  for (int lf = 0; lf < NFPE; ++lf) cross[(long long)lf * ne + e] = 0.0;
+  double zb[NEQ][ND];
+  for (int k = 0; k < NEQ; ++k)
+    for (int j = 0; j < ND; ++j) zb[k][j] = 0.0;
+  // density indicator with derivatives
+  D m;
+  double elind_last = 1.0;
+  if (prm.indicator == 0) {
+    m = D(1.0);
+  } else if (prm.indicator == 1) {
+    m = D(0.0);
+    elind_last = 0.0;
+  } else {
+    D rho[ND];
+    for (int j = 0; j < ND; ++j) rho[j] = D::var(el[0][j], j);
+    const D mself = D::var(um[0], ND);
+    D mI = mself < D(1e9) ? mself : D(1e9);
+    D MI = mself > D(-1e9) ? mself : D(-1e9);
+    for (int lf = 0; lf < NFPE; ++lf) {
+      const int nb = prm.fnbr[lf * ne + e];
+      if (nb < 0) continue;
+      const D v = D::var(prm.means[nb], ND + 1 + lf);
+      mI = v < mI ? v : mI;
+      MI = v > MI ? v : MI;
+    }
+    D yMin = D(1e9);
+    for (int lf = 0; lf < NFPE; ++lf) {
+      if (prm.fnbr[lf * ne + e] < 0) continue;
+      for (int q = 0; q < NQL; ++q) {
+        D v = D(0.0);
+        for (int j = 0; j < ND; ++j) v += rho[j] * T->Bl[lf][q][j];
+        const D diff = v - mself;
+        D y;
+        if (diff > D(1e-3))
+          y = (MI - mself) / diff;
+        else if (diff < D(-1e-3))
+          y = (mI - mself) / diff;
+        else
+          y = D(1.0);
+        if (prm.function == 0) {
+          yMin = y < yMin ? y : yMin;
+          yMin = yMin > D(1.0) ? D(1.0) : yMin;
+        } else if (prm.function == 1) {
+          const D yc = (y * y + 2.0 * y) / (y * y + y + 2.0);
+          yMin = yc < yMin ? yc : yMin;
+        } else {
+          const double ys = 1.5;
+          const D yr = y / ys;
+          const D yc = y < D(1.0) ? y + (3.0 - 2.0 * ys) * yr * yr + (ys - 2.0) * yr * yr * yr : D(1.0);
+          yMin = yc < yMin ? yc : yMin;
+        }
+      }
+    }
+    m = yMin;
+    // FinDiff looks at the last equation's indicator; recompute it plainly
+    if (prm.limiter == 0) {
+      const int kl = NEQ - 1;
+      double mIl = um[kl], MIl = um[kl], yl = 1e9;
+      for (int lf = 0; lf < NFPE; ++lf) {
+        const int nb = prm.fnbr[lf * ne + e];
+        if (nb < 0) continue;
+        const double v = prm.means[(long long)kl * ne + nb];
+        mIl = v < mIl ? v : mIl;
+        MIl = v > MIl ? v : MIl;
+      }
+      for (int lf = 0; lf < NFPE; ++lf) {
+        if (prm.fnbr[lf * ne + e] < 0) continue;
+        for (int q = 0; q < NQL; ++q) {
+          double v = 0.0;
+          for (int j = 0; j < ND; ++j) v += el[kl][j] * T->Bl[lf][q][j];
+          const double diff = v - um[kl];
+          double y = diff > 1e-3 ? (MIl - um[kl]) / diff : (diff < -1e-3 ? (mIl - um[kl]) / diff : 1.0);
+          double yc;
+          if (prm.function == 0) {
+            yc = y < 1.0 ? y : 1.0;
+          } else if (prm.function == 1) {
+            yc = (y * y + 2.0 * y) / (y * y + y + 2.0);
+          } else {
+            const double yr = y / 1.5;
+            yc = y < 1.0 ? y + 0.0 * yr * yr - 0.5 * yr * yr * yr : 1.0;
+          }
+          yl = yc < yl ? yc : yl;
+        }
+      }
+      elind_last = yl;
+    }
+  }
+  const double* w = T->wmean;
+  if (prm.limiter == 1) {
+    const int reps = (prm.quirks & 1) ? 1 : ND;
+    const double mv = m.v;
+    double pm1 = 1.0;  // m^(reps-1)
+    for (int i = 1; i < reps; ++i) pm1 *= mv;
+    const double mnd = pm1 * mv;
+    const double dmnd = reps * pm1;
+    // forward values to test the last-hope reset
+    bool reset = false;
+    if (prm.last_hope) {
+      for (int v = 0; v < NV && !reset; ++v) {
+        double fv[NEQ];
+        for (int k = 0; k < NEQ; ++k) {
+          double s = 0.0;
+          for (int j = 0; j < ND; ++j) s += (um[k] + mnd * (el[k][j] - um[k])) * T->Bv[v][j];
+          fv[k] = s;
+        }
+        if (!state_is_physical<DIM>(fv, prm.gamma, prm.covolume)) reset = true;
+      }
+    }
+    if (reset) {
+      for (int k = 0; k < NEQ; ++k) {
+        double sy = 0.0;
+        for (int i = 0; i < ND; ++i) sy += yb[k][i];
+        for (int j = 0; j < ND; ++j) zb[k][j] += w[j] * sy;
+      }
+    } else {
+      double mbar = 0.0;
+      for (int k = 0; k < NEQ; ++k) {
+        double sy = 0.0;
+        for (int i = 0; i < ND; ++i) {
+          sy += yb[k][i];
+          mbar += yb[k][i] * dmnd * (el[k][i] - um[k]);
+        }
+        for (int j = 0; j < ND; ++j) zb[k][j] += w[j] * (1.0 - mnd) * sy + mnd * yb[k][j];
+      }
+      if (prm.indicator == 2) {
+        for (int j = 0; j < ND; ++j) zb[0][j] += mbar * (m.d[j] + m.d[ND] * w[j]);
+        for (int lf = 0; lf < NFPE; ++lf) cross[(long long)lf * ne + e] = mbar * m.d[ND + 1 + lf];
+      }
+    }
+  } else {
+    if (elind_last < 0.999) {
+      for (int k = 0; k < NEQ; ++k) {
+        double sy = 0.0;
+        for (int i = 0; i < ND; ++i) sy += yb[k][i];
+        for (int j = 0; j < ND; ++j) zb[k][j] += w[j] * sy;
+      }
+    } else {
+      for (int k = 0; k < NEQ; ++k)
+        for (int j = 0; j < ND; ++j) zb[k][j] += yb[k][j];
+    }
+  }
+  for (int k = 0; k < NEQ; ++k)
+    for (int j = 0; j < ND; ++j) zbar[k * NDa + (long long)e * ND + j] = zb[k][j];
+}
+
+// Gather the neighbours' derivatives with respect to this element's density
+// mean (mean = sum_j wmean_j rho_j).
+template <int G, int P>
+__global__ void k_limit_vjp_gather(const RhsParams prm, const double* __restrict__ cross,
+                                   double* __restrict__ zbar) {
+  using E = El<G, P>;
+  constexpr int ND = E::ND, NFPE = E::NFPE;
+  const int ne = prm.ne;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ne) return;
+  double s = 0.0;
+  for (int lf = 0; lf < NFPE; ++lf) {
+    const int e = prm.fnbr[lf * ne + c];
+    if (e < 0) continue;
+    const int lfo = prm.fcode[lf * ne + c] & 7;
+    s += cross[(long long)lfo * ne + e];
+  }
+  if (s != 0.0)
+    for (int j = 0; j < ND; ++j) zbar[(long long)c * ND + j] += prm.tab->wmean[j] * s;
+}
+
+}  // namespace rkdg

@@ -86,6 +86,7 @@ struct RhsParams {
   double gamma, covolume;
   int rs, avg;
   int faces_only;       // 1: face terms only (A.Mult for the initial dt)
+  int quirks;           // bit 0: negative HLLC speed is not an error
   BCSlot bc[RKDG_MAX_BC];
   unsigned long long* mcs;  // atomicMax target, bits of a non-negative double
   int* err;                 // [0] status (first writer wins), [1] element

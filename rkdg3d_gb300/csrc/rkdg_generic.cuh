@@ -65,6 +65,20 @@ __device__ __forceinline__ void flag_error(int* err, int code, int where) {
   if (atomicCAS(&err[0], 0, code) == 0) err[1] = where;
 }
 
+// The reference aborts when a face wave speed is negative
+// (face_integrator.cpp:214-218).  That is how its solvers report a
+// non-physical state (-1), but HLLC's signed max(SL, SR) (rs_hllc.cpp:98) is
+// also negative in supersonic flow against the normal.  With quirk bit 0 only
+// the -1 of a non-physical state is an error; the speed enters the max as 0.
+template <typename R>
+__device__ __forceinline__ R checked_speed(const RhsParams& prm, R sp, int e) {
+  if (sp < R(0)) {
+    if (!(prm.quirks & 1) || sp == R(-1)) flag_error(prm.err, 2, e);
+    return R(0);
+  }
+  return sp;
+}
+
 // Per-problem max wave speed for batched problems: elements of one problem
 // are contiguous, so a warp holds a few contiguous runs; a segmented shuffle
 // reduction leaves each run's max in its first lane, which commits it.
@@ -259,11 +273,7 @@ __global__ void __launch_bounds__(128)
           right_state<DIM>(bc.type, bc.state, s1, s2, n);
         }
         R F[NEQ];
-        R sp = riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg);
-        if (sp < R(0)) {
-          flag_error(prm.err, 2, e);
-          sp = R(0);
-        }
+        const R sp = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e);
         lmax = fmax(lmax, sp);
         const R* Bo = sB[lf][side ? q2 : q];
         const R wq = sW[q];
@@ -295,11 +305,11 @@ __global__ void __launch_bounds__(128)
         for (int k = 0; k < NEQ; ++k)
 #pragma unroll
           for (int r = 0; r < DIM; ++r) {
-            R G = R(0);
+            R gc = R(0);
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) G += adj[r][d] * F[k][d];
+            for (int d = 0; d < DIM; ++d) gc += adj[r][d] * F[k][d];
 #pragma unroll
-            for (int j = 0; j < ND; ++j) acc[k][j] += sD[r][j][m] * G;
+            for (int j = 0; j < ND; ++j) acc[k][j] += sD[r][j][m] * gc;
           }
       }
 #pragma unroll

@@ -272,11 +272,7 @@ __global__ void __launch_bounds__(256)
           right_state<3>(bc.type, bc.state, s1, s2, n);
         }
         R F[NEQ];
-        R sp = riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg);
-        if (sp < R(0)) {
-          flag_error(prm.err, 2, e);
-          sp = R(0);
-        }
+        const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e);
         lmax = fmax(lmax, sp);
         const R sg = side ? R(1) : R(-1);
         const R wq = tWf[q];

@@ -153,17 +153,48 @@ __device__ __forceinline__ void team_lift(const R* f, const R* l1d, const R* len
     }
 }
 
-// One face of one element, for the team's variable k.
-template <int P, int LF, typename R>
-__device__ __forceinline__ void team_face(const RhsParams& prm, const R* __restrict__ ug, int e, int k,
-                                          int tl, R (&u)[(P + 1) * (P + 1) * (P + 1)],
+template <int P, typename R>
+__device__ __forceinline__ void team_contract_any(int lf, const R (&u)[(P + 1) * (P + 1) * (P + 1)],
+                                                  const R* lend, R (&v)[(P + 1) * (P + 1)]) {
+  switch (lf) {
+    case 0: team_contract<P, 0>(u, lend, v); break;
+    case 1: team_contract<P, 1>(u, lend, v); break;
+    case 2: team_contract<P, 2>(u, lend, v); break;
+    case 3: team_contract<P, 3>(u, lend, v); break;
+    case 4: team_contract<P, 4>(u, lend, v); break;
+    default: team_contract<P, 5>(u, lend, v); break;
+  }
+}
+
+template <int P, typename R>
+__device__ __forceinline__ void team_lift_any(int lf, const R* f, const R* l1d, const R* lend,
+                                              R (&acc)[(P + 1) * (P + 1) * (P + 1)]) {
+  switch (lf) {
+    case 0: team_lift<P, 0>(f, l1d, lend, acc); break;
+    case 1: team_lift<P, 1>(f, l1d, lend, acc); break;
+    case 2: team_lift<P, 2>(f, l1d, lend, acc); break;
+    case 3: team_lift<P, 3>(f, l1d, lend, acc); break;
+    case 4: team_lift<P, 4>(f, l1d, lend, acc); break;
+    default: team_lift<P, 5>(f, l1d, lend, acc); break;
+  }
+}
+
+// One face (runtime index lf) of one element, for the team's variable k.
+// The register arrays need compile-time indices only in the own-side
+// contraction and the lift (small switches); the neighbour contraction reads
+// global memory through a node table, and the numerical flux has a single
+// call site.
+template <int P, typename R>
+__device__ __forceinline__ void team_face(const int LF, const RhsParams& prm, const R* __restrict__ ug,
+                                          int e, int k, int tl, R (&u)[(P + 1) * (P + 1) * (P + 1)],
                                           R (&acc)[(P + 1) * (P + 1) * (P + 1)], R* xch,
                                           const R* l1d, const R* lend, const R* wf,
                                           const unsigned char (*perm)[(P + 2) * (P + 2)],
-                                          const int (*fab)[RKDG_MAX_NQF], R gamma, R cov,
-                                          R& lmax, unsigned mask) {
+                                          const int (*fab)[RKDG_MAX_NQF],
+                                          const unsigned char (*nodet)[(P + 1) * (P + 1) * (P + 1)],
+                                          R gamma, R cov, R& lmax, unsigned mask) {
   using S = TeamSize<P>;
-  constexpr int N1 = S::N1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ;
+  constexpr int N1 = S::N1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, NF2 = S::NF2;
   const int ne = prm.ne;
   const long long NDa = prm.ndofs;
   const int nb = prm.fnbr[LF * ne + e];
@@ -173,14 +204,23 @@ __device__ __forceinline__ void team_face(const RhsParams& prm, const R* __restr
   R* Fh = Tn + NEQ * NQF;      // [NEQ][NQF] lifted flux values (own tensor order)
   {
     R v[N1 * N1];
-    team_contract<P, LF>(u, lend, v);
+    team_contract_any<P>(LF, u, lend, v);
     team_interp<P>(v, l1d, To + k * NQF);
   }
   const int code = prm.fcode[LF * ne + e];
   const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
   if (nb >= 0) {
+    const R* ugn = ug + k * NDa + (long long)nb * ND;
+    const int sdn = hex_face_side(lfo);
+    const unsigned char* nt = nodet[lfo];  // [(i0*N1+i1)*N1 + jn]
     R v[N1 * N1];
-    team_contract_g_any<P>(lfo, ug + k * NDa + (long long)nb * ND, lend, v);
+#pragma unroll
+    for (int r = 0; r < NF2; ++r) {
+      R s = R(0);
+#pragma unroll
+      for (int jn = 0; jn < N1; ++jn) s += lend[sdn * N1 + jn] * __ldg(ugn + nt[r * N1 + jn]);
+      v[r] = s;
+    }
     team_interp<P>(v, l1d, Tn + k * NQF);
   }
   __syncwarp(mask);
@@ -190,7 +230,7 @@ __device__ __forceinline__ void team_face(const RhsParams& prm, const R* __restr
   for (int c = 0; c < 3; ++c) n[c] = fg[(long long)(LF * 4 + c) * ne + e];
   const R jac = fg[(long long)(LF * 4 + 3) * ne + e];
   const R sg = side ? R(1) : R(-1);
-#pragma unroll
+#pragma unroll 1
   for (int rr = 0; rr < (NQF + NEQ - 1) / NEQ; ++rr) {
     const int q = tl + NEQ * rr;
     if (q < NQF) {
@@ -215,11 +255,7 @@ __device__ __forceinline__ void team_face(const RhsParams& prm, const R* __restr
         right_state<3>(bc.type, bc.state, s1, s2, n);
       }
       R F[NEQ];
-      R sp = riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg);
-      if (sp < R(0)) {
-        flag_error(prm.err, 2, e);
-        sp = R(0);
-      }
+      const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e);
       lmax = fmax(lmax, sp);
       const R wq = wf[q];
 #pragma unroll
@@ -227,7 +263,7 @@ __device__ __forceinline__ void team_face(const RhsParams& prm, const R* __restr
     }
   }
   __syncwarp(mask);
-  if (!prm.faces_only) team_lift<P, LF>(Fh + k * NQF, l1d, lend, acc);
+  if (!prm.faces_only) team_lift_any<P>(LF, Fh + k * NQF, l1d, lend, acc);
   __syncwarp(mask);
 }
 
@@ -239,6 +275,7 @@ __global__ void __launch_bounds__(128)
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ unsigned char sPerm[RKDG_MAX_PERM][NQF];
   __shared__ int sFab[6][RKDG_MAX_NQF];
+  __shared__ unsigned char sNodeT[6][ND];  // node of (face, i0*N1+i1, jn)
   R* sm = reinterpret_cast<R*>(smraw);
   R* tL1 = sm;                  // [NQ1][N1]
   R* tLend = tL1 + NQ1 * N1;    // [2][N1]
@@ -260,6 +297,10 @@ __global__ void __launch_bounds__(128)
   for (int t = tid; t < NQF; t += blockDim.x) tWf[t] = (R)T->wf[t];
   for (int t = tid; t < T->nperm * NQF; t += blockDim.x) sPerm[t / NQF][t % NQF] = (unsigned char)T->perm[t / NQF][t % NQF];
   for (int t = tid; t < 6 * NQF; t += blockDim.x) sFab[t / NQF][t % NQF] = T->fab[t / NQF][t % NQF];
+  for (int t = tid; t < 6 * ND; t += blockDim.x) {
+    const int lf = t / ND, r = (t % ND) / N1, jn = t % N1;
+    sNodeT[lf][t % ND] = (unsigned char)hnode<N1>(hex_face_axis(lf), jn, r / N1, r % N1);
+  }
 
   const int ne = prm.ne;
   const long long NDa = prm.ndofs;
@@ -289,12 +330,10 @@ __global__ void __launch_bounds__(128)
       uv[i] = sU[(el * NEQ + k) * ND + i];
       acc[i] = R(0);
     }
-    team_face<P, 0>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
-    team_face<P, 1>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
-    team_face<P, 2>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
-    team_face<P, 3>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
-    team_face<P, 4>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
-    team_face<P, 5>(prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, gamma, cov, lmax, mask);
+#pragma unroll 1
+    for (int lf = 0; lf < 6; ++lf)
+      team_face<P, R>(lf, prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, sNodeT,
+                      gamma, cov, lmax, mask);
     if (!prm.faces_only) {
       // nodal fluxes: lane tl handles nodes tl, tl+5, ...; contravariant
       // components of all variables go to the exchange buffer [3][NEQ][ND]

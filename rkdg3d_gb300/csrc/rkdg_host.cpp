@@ -45,6 +45,7 @@ struct rkdg_ctx {
   std::vector<double> a{1.0, 0.25, 0.25}, b{1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0}, c{1.0, 0.5};
   int precision = RKDG_FP64;
   int hex_variant = 0;  // RKDG_TUNE_HEX_KERNEL
+  int solver_quirks = 0;
   // mesh (host copies)
   bool has_mesh = false;
   int dim = 0, geom = 0, p = 0, ne = 0, nd = 0, neq = 0, nfpe = 0, nvpe = 0;
@@ -91,6 +92,9 @@ struct rkdg_ctx {
   int* d_psteps = nullptr;
   int* d_nactive = nullptr;
   unsigned long long* d_pmcs = nullptr;  // [4][nprob]
+  // discrete adjoint scratch (FP64)
+  double* d_adj = nullptr;
+  size_t adj_n = 0;
 
   bool limiter_active() const { return !(lim == RKDG_LIM_FINDIFF && ind == RKDG_IND_NOWHERE); }
 };
@@ -155,6 +159,8 @@ void free_mesh(rkdg_ctx* c) {
   dfree(c->d_psteps);
   dfree(c->d_nactive);
   dfree(c->d_pmcs);
+  dfree(c->d_adj);
+  c->adj_n = 0;
   c->nprob = 0;
   c->has_mesh = false;
 }
@@ -236,6 +242,7 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   P.rs = c->rs;
   P.avg = c->avg;
   P.faces_only = faces_only;
+  P.quirks = c->solver_quirks;
   int k = 0;
   for (auto& kv : c->bcs) P.bc[k++] = kv.second;
   P.mcs = c->d_mcs + slot;
@@ -635,6 +642,13 @@ int rkdg_set_precision(rkdg_ctx* c, int precision) {
     cudaSetDevice(c->device);
     return ensure_scratch(c);
   }
+  return RKDG_OK;
+}
+
+int rkdg_set_solver_quirks(rkdg_ctx* c, int flags) {
+  if (!c) return RKDG_ERR_INVALID;
+  if (flags & ~1) return fail(c, RKDG_ERR_INVALID, "unknown solver quirk flag");
+  c->solver_quirks = flags;
   return RKDG_OK;
 }
 
@@ -1277,6 +1291,223 @@ int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0,
     if (sum_dt_out) sum_dt_out[p] = sd[p];
   }
   return RKDG_OK;
+}
+
+}  // extern "C"
+
+// ---- discrete adjoint --------------------------------------------------------
+namespace {
+
+struct Adj {
+  double *r, *ub, *zb, *acc, *w, *cross;
+  double *kb[4], *z[4], *y[4], *k[4];
+};
+
+int adj_bufs(rkdg_ctx* c, Adj& A) {
+  const size_t n = (size_t)c->ndofs * c->neq;
+  const size_t nvec = 5 + 16;
+  const size_t need = nvec * n + (size_t)c->nfpe * c->ne;
+  if (c->adj_n < need) {
+    CUDA_TRY(c, dalloc(c->d_adj, need));
+    c->adj_n = need;
+  }
+  double* p = c->d_adj;
+  A.r = p; p += n;
+  A.ub = p; p += n;
+  A.zb = p; p += n;
+  A.acc = p; p += n;
+  A.w = p; p += n;
+  for (int i = 0; i < 4; ++i) { A.kb[i] = p; p += n; }
+  for (int i = 0; i < 4; ++i) { A.z[i] = p; p += n; }
+  for (int i = 0; i < 4; ++i) { A.y[i] = p; p += n; }
+  for (int i = 0; i < 4; ++i) { A.k[i] = p; p += n; }
+  A.cross = p;
+  return RKDG_OK;
+}
+
+int plain_rhs(rkdg_ctx* c, const double* in, double* out) {
+  EpiParams<double> ep;
+  std::memset(&ep, 0, sizeof ep);
+  ep.mode = 0;
+  ep.out64 = out;
+  RhsParams P = rhs_params(c, 0, 0, 7);
+  CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p, 0, P, in, &ep, c->stream));
+  c->launches++;
+  return RKDG_OK;
+}
+
+int limit_in_place(rkdg_ctx* c, double* x) {
+  if (!c->limiter_active()) return RKDG_OK;
+  CUDA_TRY(c, rkdg::launch_means(c->geom, c->p, 0, c->ne, c->ndofs, c->d_tab, x, nullptr, c->d_means, c->stream));
+  LimParams L = lim_params(c);
+  CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 0, L, x, nullptr, c->stream));
+  c->launches += 2;
+  return RKDG_OK;
+}
+
+// out = (df/dy)^T kbar
+int rhs_t(rkdg_ctx* c, Adj& A, const double* y, const double* kbar, double* out) {
+  CUDA_TRY(c, rkdg::launch_minv_apply(c->geom, c->p, c->ne, c->ndofs, c->d_tab, c->d_egeo64, kbar, A.r, c->stream));
+  RhsParams P = rhs_params(c, 0, 0, 7);
+  CUDA_TRY(c, rkdg::launch_rhs_vjp(c->geom, c->p, P, y, A.r, out, c->stream));
+  c->launches += 2;
+  return RKDG_OK;
+}
+
+// out = (dL/dz)^T ybar
+int lim_t(rkdg_ctx* c, Adj& A, const double* z, const double* ybar, double* out) {
+  const long long n = c->ndofs * c->neq;
+  if (!c->limiter_active()) {
+    CUDA_TRY(c, cudaMemcpyAsync(out, ybar, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    return RKDG_OK;
+  }
+  CUDA_TRY(c, rkdg::launch_means(c->geom, c->p, 0, c->ne, c->ndofs, c->d_tab, z, nullptr, c->d_means, c->stream));
+  LimParams L = lim_params(c);
+  CUDA_TRY(c, rkdg::launch_limit_vjp(c->geom, c->p, L, z, ybar, out, A.cross, c->stream));
+  RhsParams P = rhs_params(c, 0, 0, 7);
+  CUDA_TRY(c, rkdg::launch_limit_vjp_gather(c->geom, c->p, P, A.cross, out, c->stream));
+  c->launches += 3;
+  return RKDG_OK;
+}
+
+// Reverse of ExplicitRKLimitedSolver::Step at state x with step dt: xbar holds
+// the adjoint of x_{n+1} on entry and of x_n on return.
+int step_t(rkdg_ctx* c, Adj& A, const double* x, double dt, double* xbar) {
+  const int s = c->s;
+  const long long n = c->ndofs * c->neq;
+  const size_t bytes = n * sizeof(double);
+  int st;
+  // forward recompute of the stage values
+  if ((st = plain_rhs(c, x, A.k[0]))) return st;
+  for (int i = 1; i < s; ++i) {
+    const int row = i * (i - 1) / 2;
+    CUDA_TRY(c, cudaMemcpyAsync(A.z[i], x, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    for (int j = 0; j < i; ++j) CUDA_TRY(c, rkdg::launch_axpy(n, c->a[row + j] * dt, A.k[j], A.z[i], c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(A.y[i], A.z[i], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if ((st = limit_in_place(c, A.y[i]))) return st;
+    if ((st = plain_rhs(c, A.y[i], A.k[i]))) return st;
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(A.w, x, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  for (int j = 0; j < s; ++j) CUDA_TRY(c, rkdg::launch_axpy(n, c->b[j] * dt, A.k[j], A.w, c->stream));
+  // reverse sweep
+  if ((st = lim_t(c, A, A.w, xbar, A.acc))) return st;
+  for (int j = 0; j < s; ++j) CUDA_TRY(c, rkdg::launch_scale_copy(n, c->b[j] * dt, A.acc, A.kb[j], c->stream));
+  for (int i = s - 1; i >= 1; --i) {
+    const int row = i * (i - 1) / 2;
+    if ((st = rhs_t(c, A, A.y[i], A.kb[i], A.ub))) return st;
+    if ((st = lim_t(c, A, A.z[i], A.ub, A.zb))) return st;
+    CUDA_TRY(c, rkdg::launch_axpy(n, 1.0, A.zb, A.acc, c->stream));
+    for (int j = 0; j < i; ++j) CUDA_TRY(c, rkdg::launch_axpy(n, c->a[row + j] * dt, A.zb, A.kb[j], c->stream));
+  }
+  if ((st = rhs_t(c, A, x, A.kb[0], A.ub))) return st;
+  CUDA_TRY(c, rkdg::launch_axpy(n, 1.0, A.ub, A.acc, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(xbar, A.acc, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  return RKDG_OK;
+}
+
+int adjoint_ready(rkdg_ctx* c) {
+  if (c->precision != RKDG_FP64)
+    return fail(c, RKDG_ERR_UNSUPPORTED, "the discrete adjoint runs on the FP64 path");
+  if (!rkdg::adjoint_supported(c->geom, c->p))
+    return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint kernels for this element type / order");
+  if (c->nprob > 0) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for batched problems");
+  return RKDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rkdg_rhs_vjp(rkdg_ctx* c, const double* x, const double* kbar, double* xbar) {
+  NEED_MESH(c);
+  int st = adjoint_ready(c);
+  if (st) return st;
+  if (!x || !kbar || !xbar) return fail(c, RKDG_ERR_INVALID, "null pointer");
+  Adj A;
+  if ((st = adj_bufs(c, A))) return st;
+  if ((st = rhs_t(c, A, x, kbar, xbar))) return st;
+  return read_mcs(c, 7, nullptr);
+}
+
+int rkdg_limit_vjp(rkdg_ctx* c, const double* z, const double* ybar, double* zbar) {
+  NEED_MESH(c);
+  int st = adjoint_ready(c);
+  if (st) return st;
+  if (!z || !ybar || !zbar) return fail(c, RKDG_ERR_INVALID, "null pointer");
+  Adj A;
+  if ((st = adj_bufs(c, A))) return st;
+  if ((st = lim_t(c, A, z, ybar, zbar))) return st;
+  return read_mcs(c, 7, nullptr);
+}
+
+int rkdg_step_vjp(rkdg_ctx* c, const double* x, double dt, double* xbar) {
+  NEED_MESH(c);
+  int st = adjoint_ready(c);
+  if (st) return st;
+  if (!x || !xbar) return fail(c, RKDG_ERR_INVALID, "null pointer");
+  Adj A;
+  if ((st = adj_bufs(c, A))) return st;
+  if ((st = step_t(c, A, x, dt, xbar))) return st;
+  return read_mcs(c, 7, nullptr);
+}
+
+int rkdg_adjoint_run(rkdg_ctx* c, const double* x0, int nsteps, double dt, int every,
+                     double* xbar, double* xT) {
+  NEED_MESH(c);
+  int st = adjoint_ready(c);
+  if (st) return st;
+  if (!x0 || !xbar || nsteps <= 0 || !(dt > 0.0) || every <= 0)
+    return fail(c, RKDG_ERR_INVALID, "invalid adjoint run arguments");
+  if ((st = ensure_scratch(c))) return st;
+  Adj A;
+  if ((st = adj_bufs(c, A))) return st;
+  const long long n = c->ndofs * c->neq;
+  const size_t bytes = n * sizeof(double);
+  const int ncp = (nsteps + every - 1) / every;
+  double* store = nullptr;  // ncp checkpoints + `every` segment states
+  if (cudaMalloc((void**)&store, (size_t)(ncp + every) * bytes) != cudaSuccess)
+    return fail(c, RKDG_ERR_ALLOC, "adjoint checkpoint storage");
+  auto cp = [&](int i) { return store + (size_t)i * n; };
+  auto seg = [&](int i) { return store + (size_t)(ncp + i) * n; };
+  int rc = RKDG_OK;
+  do {
+    // forward sweep storing a checkpoint every `every` steps
+    double* x = seg(0);
+    if (cudaMemcpyAsync(x, x0, bytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) {
+      rc = fail(c, RKDG_ERR_CUDA, "copy");
+      break;
+    }
+    for (int s = 0; s < nsteps && !rc; ++s) {
+      if (s % every == 0 &&
+          cudaMemcpyAsync(cp(s / every), x, bytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+        rc = fail(c, RKDG_ERR_CUDA, "copy");
+      if (!rc) rc = enqueue_step64(c, x, dt);
+    }
+    if (rc) break;
+    if (xT && cudaMemcpyAsync(xT, x, bytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) {
+      rc = fail(c, RKDG_ERR_CUDA, "copy");
+      break;
+    }
+    if ((rc = read_mcs(c, c->s - 1, nullptr))) break;
+    // reverse sweep, segment by segment, recomputing the segment's states
+    for (int g = ncp - 1; g >= 0 && !rc; --g) {
+      const int s0 = g * every, len = std::min(every, nsteps - s0);
+      if (cudaMemcpyAsync(seg(0), cp(g), bytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) {
+        rc = fail(c, RKDG_ERR_CUDA, "copy");
+        break;
+      }
+      for (int j = 1; j < len && !rc; ++j) {
+        if (cudaMemcpyAsync(seg(j), seg(j - 1), bytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+          rc = fail(c, RKDG_ERR_CUDA, "copy");
+        if (!rc) rc = enqueue_step64(c, seg(j), dt);
+      }
+      for (int j = len - 1; j >= 0 && !rc; --j) rc = step_t(c, A, seg(j), dt, xbar);
+      if (!rc) rc = read_mcs(c, 7, nullptr);
+    }
+  } while (false);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(store);
+  return rc;
 }
 
 long long rkdg_kernel_launches(rkdg_ctx* c) { return c ? c->launches : -1; }

@@ -41,6 +41,19 @@ cudaError_t launch_batch_init(const BatchState& bs, double dt0, cudaStream_t st)
 cudaError_t launch_batch_control(const BatchState& bs, cudaGraphConditionalHandle h,
                                  int use_handle, cudaStream_t st);
 
+// discrete adjoint (FP64)
+bool adjoint_supported(int geom, int p);
+cudaError_t launch_minv_apply(int geom, int p, int ne, long long ndofs, const RefTables* tab,
+                              const double* egeo, const double* kb, double* r, cudaStream_t st);
+cudaError_t launch_rhs_vjp(int geom, int p, const RhsParams& prm, const double* u, const double* r,
+                           double* ub, cudaStream_t st);
+cudaError_t launch_limit_vjp(int geom, int p, const LimParams& prm, const double* z,
+                             const double* yb, double* zb, double* cross, cudaStream_t st);
+cudaError_t launch_limit_vjp_gather(int geom, int p, const RhsParams& prm, const double* cross,
+                                    double* zb, cudaStream_t st);
+cudaError_t launch_axpy(long long n, double a, const double* x, double* y, cudaStream_t st);
+cudaError_t launch_scale_copy(long long n, double a, const double* x, double* y, cudaStream_t st);
+
 // Template launch helpers shared by the per-geometry translation units.
 template <int G, int P>
 cudaError_t launch_rhs_t(int prec, const RhsParams& prm, const void* u, const void* ep,

@@ -176,6 +176,9 @@ class Context:
         self._chk(self._L.rkdg_set_precision(self.h, precision))
         self.precision = precision
 
+    def set_solver_quirks(self, flags: int):
+        self._chk(self._L.rkdg_set_solver_quirks(self.h, flags))
+
     def set_tuning(self, key: int, value: int):
         self._chk(self._L.rkdg_set_tuning(self.h, key, value))
 
@@ -246,6 +249,20 @@ class Context:
 
     def synchronize(self):
         self._chk(self._L.rkdg_synchronize(self.h))
+
+    # -- discrete adjoint (FP64) ----------------------------------------------
+    def rhs_vjp(self, x, kbar, xbar):
+        self._chk(self._L.rkdg_rhs_vjp(self.h, _ptr(x), _ptr(kbar), _ptr(xbar)))
+
+    def limit_vjp(self, z, ybar, zbar):
+        self._chk(self._L.rkdg_limit_vjp(self.h, _ptr(z), _ptr(ybar), _ptr(zbar)))
+
+    def step_vjp(self, x, dt: float, xbar):
+        self._chk(self._L.rkdg_step_vjp(self.h, _ptr(x), dt, _ptr(xbar)))
+
+    def adjoint_run(self, x0, nsteps: int, dt: float, checkpoint_every: int, xbar, xT=None):
+        self._chk(self._L.rkdg_adjoint_run(self.h, _ptr(x0), nsteps, dt, checkpoint_every,
+                                           _ptr(xbar), _ptr(xT) if xT is not None else None))
 
     # -- batched independent problems -----------------------------------------
     def batch_setup(self, elem_offsets, gammas, covolumes):

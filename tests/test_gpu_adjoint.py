@@ -1,0 +1,147 @@
+"""Discrete adjoint (VJP) kernels against central finite differences of the
+plain FP64 GPU path (itself parity-checked against the oracle).
+
+Directional check: <v, J^T w> versus (<w, F(x + eps v)> - <w, F(x - eps v)>) / (2 eps)
+with relative tolerance 1e-5 (the benchmark spec's bar for the gradient)."""
+import numpy as np
+import pytest
+import torch
+
+from rkdg3d_gb300 import cases
+from rkdg3d_gb300 import mesh as M
+from rkdg3d_gb300.solver import (AVG_TRRS, BC_SLIP, FUN_MICHALAK, FUN_VENKATAKRISHNAN, FP64,
+                                 IND_BJ, LIM_FINDIFF, LIM_MULTI, RS_HLL, RS_HLLC, RS_RUSANOV,
+                                 TABLEAU_SSPRK3, Context)
+from tests.helpers import periodic_case, random_state, walled_case
+
+pytestmark = pytest.mark.gpu
+
+
+def ctx_for(case):
+    ctx = Context(case.mesh, case.order, device=0, precision=FP64)
+    cases.configure_context(case, ctx)
+    return ctx
+
+
+def dev(a):
+    return torch.tensor(a, dtype=torch.float64, device="cuda")
+
+
+def smooth_state(X, dim, amp=0.05):
+    rho = 1 + amp * np.sin(2 * np.pi * X[0]) * np.cos(2 * np.pi * X[1])
+    vel = [0.1 * np.cos(2 * np.pi * X[d]) for d in range(dim)]
+    p = 1 + 0.5 * amp * np.sin(2 * np.pi * X[1])
+    return cases.conservative([rho, *vel, p], 1.4, 0.0)
+
+
+def fd_check(apply, vjp, x, seed, eps=1e-6, tol=1e-5):
+    rng = np.random.default_rng(seed)
+    w = rng.normal(size=x.size)
+    v = rng.normal(size=x.size) * np.abs(x).mean()
+    g = vjp(w)
+    lhs = float(np.dot(v, g))
+    fp = float(np.dot(w, apply(x + eps * v)))
+    fm = float(np.dot(w, apply(x - eps * v)))
+    rhs = (fp - fm) / (2 * eps)
+    assert abs(lhs - rhs) <= tol * max(abs(rhs), 1e-12), (lhs, rhs)
+
+
+@pytest.mark.parametrize("geom,order,rs,walled", [(M.GEOM_CUBE, 1, RS_HLLC, False),
+                                                  (M.GEOM_SQUARE, 1, RS_HLL, True),
+                                                  (M.GEOM_SQUARE, 2, RS_RUSANOV, False),
+                                                  (M.GEOM_TRIANGLE, 1, RS_HLLC, True)])
+def test_rhs_vjp_fd(cuda, geom, order, rs, walled):
+    case = walled_case(geom, 3, order, rs, bc=BC_SLIP) if walled else periodic_case(geom, 3, order, rs)
+    ctx = ctx_for(case)
+    x = random_state(ctx.node_coords(), seed=3, amp=0.1, vel=0.2)
+
+    def apply(xx):
+        y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.rhs(dev(xx), y)
+        return y.cpu().numpy()
+
+    def vjp(w):
+        out = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.rhs_vjp(dev(x), dev(w), out)
+        return out.cpu().numpy()
+
+    fd_check(apply, vjp, x, seed=1)
+
+
+@pytest.mark.parametrize("fun", [FUN_VENKATAKRISHNAN, FUN_MICHALAK])
+@pytest.mark.parametrize("geom", [M.GEOM_SQUARE, M.GEOM_CUBE])
+def test_limit_vjp_fd(cuda, fun, geom):
+    case = periodic_case(geom, 4, 1, RS_HLLC)
+    case.limiter = (LIM_MULTI, IND_BJ, fun, 1, 0)
+    ctx = ctx_for(case)
+    x = random_state(ctx.node_coords(), seed=5, amp=0.1, vel=0.2)
+
+    def apply(xx):
+        y = dev(xx)
+        ctx.limit(y)
+        return y.cpu().numpy()
+
+    def vjp(w):
+        out = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.limit_vjp(dev(x), dev(w), out)
+        return out.cpu().numpy()
+
+    fd_check(apply, vjp, x, seed=2, eps=1e-7)
+
+
+def test_step_vjp_fd(cuda):
+    case = periodic_case(M.GEOM_CUBE, 3, 1, RS_HLLC)
+    case.limiter = (LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN, 1, 0)
+    case.tableau = TABLEAU_SSPRK3
+    ctx = ctx_for(case)
+    x = smooth_state(ctx.node_coords(), 3)
+    dt = 2e-3
+
+    def apply(xx):
+        y = dev(xx)
+        ctx.step(y, dt)
+        return y.cpu().numpy()
+
+    def vjp(w):
+        xb = dev(w)
+        ctx.step_vjp(dev(x), dt, xb)
+        return xb.cpu().numpy()
+
+    fd_check(apply, vjp, x, seed=4, eps=1e-7)
+
+
+def test_adjoint_run_gradient(cuda):
+    """C5 set-up at small size: periodic hex Q1, HLLC, Venkatakrishnan,
+    SSP-RK3 fixed dt, 12 steps with a checkpoint every 5 steps; J = 1/2 ||rho(T) - rho_t||^2."""
+    case = periodic_case(M.GEOM_CUBE, 4, 1, RS_HLLC)
+    case.limiter = (LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN, 1, 0)
+    case.tableau = TABLEAU_SSPRK3
+    ctx = ctx_for(case)
+    X = ctx.node_coords()
+    x0 = smooth_state(X, 3)
+    xt = smooth_state(X + 0.05, 3)
+    nd = ctx.ndofs
+    dt, nsteps = 2e-3, 12
+
+    def J(xx):
+        y = dev(xx)
+        ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps)
+        r = y.cpu().numpy()[:nd] - xt[:nd]
+        return 0.5 * float(np.dot(r, r))
+
+    xT = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    y = dev(x0)
+    ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps)
+    xbar = np.zeros(ctx.n)
+    xbar[:nd] = y.cpu().numpy()[:nd] - xt[:nd]
+    xb = dev(xbar)
+    ctx.adjoint_run(dev(x0), nsteps, dt, 5, xb, xT)
+    assert torch.allclose(xT, y, rtol=0, atol=1e-12)
+    g = xb.cpu().numpy()
+    rng = np.random.default_rng(11)
+    for _ in range(4):
+        v = rng.normal(size=ctx.n) * 1e-2
+        eps = 1e-5
+        fd = (J(x0 + eps * v) - J(x0 - eps * v)) / (2 * eps)
+        ad = float(np.dot(g, v))
+        assert abs(ad - fd) <= 1e-5 * abs(fd), (ad, fd)
