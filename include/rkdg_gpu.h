@@ -176,7 +176,10 @@ int rkdg_batch_setup(rkdg_ctx* ctx, int nprob, const int* elem_offsets,
  * use_graph != 0 the whole multi-step solve is one CUDA-graph launch: the RK
  * step is captured once as the body of a device-controlled while node and the
  * loop ends on the device when the last problem finishes.  Host outputs
- * (arrays of nprob, may be NULL): steps, booked t, integrated time. */
+ * (arrays of nprob, may be NULL): steps, booked t, integrated time.  A
+ * problem that meets a non-physical state stops there (where the reference
+ * would exit) while the others continue; its steps entry is then negative
+ * (-steps taken). */
 int rkdg_batch_run(rkdg_ctx* ctx, double* x_dev, double t_end, double cfl, double dt0,
                    int dt_mode, int max_steps, int use_graph, int* steps_out,
                    double* t_out, double* sum_dt_out);

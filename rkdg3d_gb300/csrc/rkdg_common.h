@@ -98,6 +98,7 @@ struct RhsParams {
   const double* pcov;
   const int* pactive;
   unsigned long long* pmcs;
+  int* pfail;           // per-problem failure flag (non-physical state)
 };
 
 // Stage epilogue.
@@ -161,6 +162,7 @@ struct BatchState {
   int* steps;           // [nprob]
   int* nactive;         // [1]
   const unsigned long long* mcs_last;  // [nprob] max speed of the last stage
+  int* fail;            // [nprob] set by the kernels on a non-physical state
 };
 
 }  // namespace rkdg

@@ -70,10 +70,17 @@ __device__ __forceinline__ void flag_error(int* err, int code, int where) {
 // non-physical state (-1), but HLLC's signed max(SL, SR) (rs_hllc.cpp:98) is
 // also negative in supersonic flow against the normal.  With quirk bit 0 only
 // the -1 of a non-physical state is an error; the speed enters the max as 0.
+// In a batch of independent problems (pb >= 0) a non-physical state stops
+// only its own problem: the problem is marked failed and the others go on.
 template <typename R>
-__device__ __forceinline__ R checked_speed(const RhsParams& prm, R sp, int e) {
+__device__ __forceinline__ R checked_speed(const RhsParams& prm, R sp, int e, int pb = -1) {
   if (sp < R(0)) {
-    if (!(prm.quirks & 1) || sp == R(-1)) flag_error(prm.err, 2, e);
+    if (!(prm.quirks & 1) || sp == R(-1)) {
+      if (pb >= 0 && prm.pfail)
+        prm.pfail[pb] = 1;
+      else
+        flag_error(prm.err, 2, e);
+    }
     return R(0);
   }
   return sp;
@@ -273,7 +280,7 @@ __global__ void __launch_bounds__(128)
           right_state<DIM>(bc.type, bc.state, s1, s2, n);
         }
         R F[NEQ];
-        const R sp = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e);
+        const R sp = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e, pb);
         lmax = fmax(lmax, sp);
         const R* Bo = sB[lf][side ? q2 : q];
         const R wq = sW[q];

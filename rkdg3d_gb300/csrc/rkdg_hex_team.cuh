@@ -192,33 +192,45 @@ __device__ __forceinline__ void team_face(const int LF, const RhsParams& prm, co
                                           const unsigned char (*perm)[(P + 2) * (P + 2)],
                                           const int (*fab)[RKDG_MAX_NQF],
                                           const unsigned char (*nodet)[(P + 1) * (P + 1) * (P + 1)],
-                                          R gamma, R cov, R& lmax, unsigned mask) {
+                                          const int* fnb, const int* fcd, const R* sU, int e0,
+                                          int nel, R gamma, R cov, R& lmax, unsigned mask) {
   using S = TeamSize<P>;
   constexpr int N1 = S::N1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, NF2 = S::NF2;
   const int ne = prm.ne;
   const long long NDa = prm.ndofs;
-  const int nb = prm.fnbr[LF * ne + e];
+  const int nb = fnb[LF], code = fcd[LF];  // preloaded face table entries
   if (nb == -1) return;
   R* To = xch;                 // [NEQ][NQF] own traces (tensor order)
   R* Tn = To + NEQ * NQF;      // [NEQ][NQF] neighbour traces (its tensor order)
   R* Fh = Tn + NEQ * NQF;      // [NEQ][NQF] lifted flux values (own tensor order)
+  const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
+  // issue the neighbour's loads first; the own-side work hides their latency
+  R nbv[ND];
+  if (nb >= 0) {
+    const unsigned char* nt = nodet[lfo];  // [(i0*N1+i1)*N1 + jn]
+    if (nb >= e0 && nb < e0 + nel) {  // neighbour staged in this tile
+      const R* sn = sU + ((nb - e0) * NEQ + k) * ND;
+#pragma unroll
+      for (int i = 0; i < ND; ++i) nbv[i] = sn[nt[i]];
+    } else {
+      const R* ugn = ug + k * NDa + (long long)nb * ND;
+#pragma unroll
+      for (int i = 0; i < ND; ++i) nbv[i] = __ldg(ugn + nt[i]);
+    }
+  }
   {
     R v[N1 * N1];
     team_contract_any<P>(LF, u, lend, v);
     team_interp<P>(v, l1d, To + k * NQF);
   }
-  const int code = prm.fcode[LF * ne + e];
-  const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
   if (nb >= 0) {
-    const R* ugn = ug + k * NDa + (long long)nb * ND;
     const int sdn = hex_face_side(lfo);
-    const unsigned char* nt = nodet[lfo];  // [(i0*N1+i1)*N1 + jn]
     R v[N1 * N1];
 #pragma unroll
     for (int r = 0; r < NF2; ++r) {
       R s = R(0);
 #pragma unroll
-      for (int jn = 0; jn < N1; ++jn) s += lend[sdn * N1 + jn] * __ldg(ugn + nt[r * N1 + jn]);
+      for (int jn = 0; jn < N1; ++jn) s += lend[sdn * N1 + jn] * nbv[r * N1 + jn];
       v[r] = s;
     }
     team_interp<P>(v, l1d, Tn + k * NQF);
@@ -306,6 +318,12 @@ __global__ void __launch_bounds__(128)
   const long long NDa = prm.ndofs;
   const int e0 = blockIdx.x * EPB;
   const int nel = min(EPB, ne - e0);
+  __shared__ int sFnb[EPB][6], sFcd[EPB][6];
+  for (int t = tid; t < nel * 6; t += blockDim.x) {
+    const int lf = t / nel, el = t % nel;
+    sFnb[el][lf] = prm.fnbr[lf * ne + e0 + el];
+    sFcd[el][lf] = prm.fcode[lf * ne + e0 + el];
+  }
   for (int k = 0; k < NEQ; ++k)
     for (int t = tid; t < nel * ND; t += blockDim.x)
       sU[((t / ND) * NEQ + k) * ND + (t % ND)] = u[k * NDa + (long long)e0 * ND + t];
@@ -320,11 +338,11 @@ __global__ void __launch_bounds__(128)
   const unsigned mask = act ? (0x1Fu << (team * NEQ)) : 0u;
   const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
   R lmax = R(0);
+  const int e = e0 + el;
+  const int k = tl;
+  R* xch = sX + el * S::XCH;
+  R uv[ND], acc[ND];
   if (act) {
-    const int e = e0 + el;
-    const int k = tl;
-    R* xch = sX + el * S::XCH;
-    R uv[ND], acc[ND];
 #pragma unroll
     for (int i = 0; i < ND; ++i) {
       uv[i] = sU[(el * NEQ + k) * ND + i];
@@ -333,7 +351,12 @@ __global__ void __launch_bounds__(128)
 #pragma unroll 1
     for (int lf = 0; lf < 6; ++lf)
       team_face<P, R>(lf, prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, sNodeT,
-                      gamma, cov, lmax, mask);
+                      sFnb[el], sFcd[el], sU, e0, nel, gamma, cov, lmax, mask);
+  }
+  // neighbours inside the tile were read from the staged DOFs, which the
+  // volume phase below overwrites with the result
+  __syncthreads();
+  if (act) {
     if (!prm.faces_only) {
       // nodal fluxes: lane tl handles nodes tl, tl+5, ...; contravariant
       // components of all variables go to the exchange buffer [3][NEQ][ND]
@@ -446,16 +469,82 @@ __global__ void __launch_bounds__(128)
     // coalesced Runge-Kutta epilogue over the CTA's elements; the combined
     // state (hi, lo) is kept in shared memory when the limiter needs means
     const bool need_means = ep.mode == 1 && ep.means;
-    for (int k = 0; k < NEQ; ++k)
-      for (int t = tid; t < nel * ND; t += blockDim.x) {
-        const int s = ((t / ND) * NEQ + k) * ND + (t % ND);
-        R hi, lo;
-        epi_value2<R>(ep, k * NDa + (long long)e0 * ND + t, sU[s], hi, lo);
-        if (need_means) {
-          sU[s] = hi;
-          sX[s] = lo;
+    if (ep.mode == 1 && !need_means) {
+      // chunked: all loads of a chunk are issued before its stores (the final
+      // stage updates the state in place, which would otherwise serialise
+      // the memory latency value by value)
+      constexpr int CH = 8;
+      const int total = NEQ * nel * ND;
+      for (int c0 = tid; c0 < total; c0 += CH * blockDim.x) {
+        long long idx[CH];
+        R y[CH], bh[CH], bl[CH], kp[3][CH];
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          const int g = c0 + c * blockDim.x;
+          const int gg = g < total ? g : c0;
+          const int k = gg / (nel * ND), t = gg % (nel * ND);
+          idx[c] = k * NDa + (long long)e0 * ND + t;
+          y[c] = sU[((t / ND) * NEQ + k) * ND + (t % ND)];
+          if constexpr (std::is_same<R, double>::value) {
+            bh[c] = ep.base ? ep.base[idx[c]] : R(0);
+            bl[c] = R(0);
+          } else {
+            bh[c] = ep.basehi[idx[c]];
+            bl[c] = ep.baselo[idx[c]];
+          }
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            if (j < ep.nprev) kp[j][c] = ep.kprev[j][idx[c]];
+        }
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          if (c0 + c * blockDim.x >= total) break;
+          if constexpr (std::is_same<R, double>::value) {
+            double v = bh[c];
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              if (j < ep.nprev) v += ep.cprev[j] * kp[j][c];
+            v += ep.ccur * y[c];
+            if (ep.kout) ep.kout[idx[c]] = y[c];
+            if (ep.out64) ep.out64[idx[c]] = v;
+            if (ep.out32) ep.out32[idx[c]] = (float)v;
+          } else if (!ep.final_stage) {
+            float inc = bl[c];
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              if (j < ep.nprev) inc = fmaf(ep.cprev_hi[j], kp[j][c], inc);
+            inc = fmaf(ep.ccur_hi, y[c], inc);
+            if (ep.kout) ep.kout[idx[c]] = y[c];
+            ep.out32[idx[c]] = bh[c] + inc;
+          } else {
+            float sh = 0.0f, sl = 0.0f, ph, pl;
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              if (j < ep.nprev) {
+                ds_mul_f(ep.cprev_hi[j], ep.cprev_lo[j], kp[j][c], ph, pl);
+                ds_add(sh, sl, ph, pl);
+              }
+            ds_mul_f(ep.ccur_hi, ep.ccur_lo, y[c], ph, pl);
+            ds_add(sh, sl, ph, pl);
+            float h = bh[c], l = bl[c];
+            ds_add(h, l, sh, sl);
+            ep.out32[idx[c]] = h;
+            ep.outlo[idx[c]] = l;
+          }
         }
       }
+    } else {
+      for (int k = 0; k < NEQ; ++k)
+        for (int t = tid; t < nel * ND; t += blockDim.x) {
+          const int s = ((t / ND) * NEQ + k) * ND + (t % ND);
+          R hi, lo;
+          epi_value2<R>(ep, k * NDa + (long long)e0 * ND + t, sU[s], hi, lo);
+          if (need_means) {
+            sU[s] = hi;
+            sX[s] = lo;
+          }
+        }
+    }
     if (need_means) {
       __syncthreads();
       // cell means of the combined state, one (element, variable) per thread

@@ -91,6 +91,7 @@ struct rkdg_ctx {
   int* d_pactive = nullptr;
   int* d_psteps = nullptr;
   int* d_nactive = nullptr;
+  int* d_pfail = nullptr;
   unsigned long long* d_pmcs = nullptr;  // [4][nprob]
   // discrete adjoint scratch (FP64)
   double* d_adj = nullptr;
@@ -158,6 +159,7 @@ void free_mesh(rkdg_ctx* c) {
   dfree(c->d_pactive);
   dfree(c->d_psteps);
   dfree(c->d_nactive);
+  dfree(c->d_pfail);
   dfree(c->d_pmcs);
   dfree(c->d_adj);
   c->adj_n = 0;
@@ -256,6 +258,7 @@ void set_batch(rkdg_ctx* c, RhsParams& P, int slot) {
   P.pcov = c->d_pcov;
   P.pactive = c->d_pactive;
   P.pmcs = c->d_pmcs + (size_t)slot * c->nprob;
+  P.pfail = c->d_pfail;
 }
 
 LimParams lim_params(rkdg_ctx* c) {
@@ -1159,6 +1162,7 @@ int rkdg_batch_setup(rkdg_ctx* c, int nprob, const int* elem_offsets, const doub
   CUDA_TRY(c, dalloc(c->d_pactive, (size_t)nprob));
   CUDA_TRY(c, dalloc(c->d_psteps, (size_t)nprob));
   CUDA_TRY(c, dalloc(c->d_nactive, (size_t)1));
+  CUDA_TRY(c, dalloc(c->d_pfail, (size_t)nprob));
   CUDA_TRY(c, dalloc(c->d_pmcs, (size_t)4 * nprob));
   CUDA_TRY(c, cudaMemcpy(c->d_prob, prob.data(), prob.size() * sizeof(int), cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy(c->d_pgamma, gamma, nprob * sizeof(double), cudaMemcpyHostToDevice));
@@ -1196,6 +1200,8 @@ int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0,
   bs.steps = c->d_psteps;
   bs.nactive = c->d_nactive;
   bs.mcs_last = c->d_pmcs + (size_t)(c->s - 1) * np;
+  bs.fail = c->d_pfail;
+  CUDA_TRY(c, cudaMemsetAsync(c->d_pfail, 0, np * sizeof(int), c->stream));
   // initial dt: face-only max speed per problem (main.cpp:467-484)
   {
     std::vector<int> ones(np, 1);
@@ -1273,9 +1279,10 @@ int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0,
     CUDA_TRY(c, rkdg::launch_join(n, c->d_xh, c->d_xl, x, c->stream));
     c->launches++;
   }
-  std::vector<int> steps(np);
+  std::vector<int> steps(np), failed(np);
   std::vector<double> tt(np), sd(np);
   CUDA_TRY(c, cudaMemcpyAsync(steps.data(), c->d_psteps, np * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(failed.data(), c->d_pfail, np * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(tt.data(), c->d_pt, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(sd.data(), c->d_psum, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   st = read_mcs(c, 0, nullptr);
@@ -1286,7 +1293,7 @@ int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0,
     c->launches = l0 + per_step * mx;
   }
   for (int p = 0; p < np; ++p) {
-    if (steps_out) steps_out[p] = steps[p];
+    if (steps_out) steps_out[p] = failed[p] ? -steps[p] : steps[p];
     if (t_out) t_out[p] = tt[p];
     if (sum_dt_out) sum_dt_out[p] = sd[p];
   }

@@ -201,6 +201,10 @@ __global__ void k_batch_control(BatchState bs, cudaGraphConditionalHandle handle
   for (int p = threadIdx.x; p < bs.nprob; p += blockDim.x) {
     if (!bs.active[p]) continue;
     bs.steps[p] += 1;
+    if (bs.fail[p]) {  // the reference would exit here; this problem stops
+      bs.active[p] = 0;
+      continue;
+    }
     bs.sum_dt[p] += bs.dtr[p];
     double dt = bs.dt[p];
     if (bs.dt_mode == 0) dt = bs.cfl * bs.hmin[p] / bits_to_double(bs.mcs_last[p]) / bs.denom;

@@ -1,10 +1,14 @@
 // Device-side Euler physics and approximate Riemann solvers (sm_103a).
 //
 // Pointwise restatement of src/physics/physics.cpp and src/riemannsolvers/
-// for compile-time dimension DIM and arithmetic type R (double for the plain
-// FP64 path, float for the FP32-bulk path).  In the FP32 path the pressure is
-// recovered in FP64 whenever internal energy loses more than three digits to
-// cancellation (near vacuum / strong shocks).
+// for compile-time dimension DIM and arithmetic type R: double for the plain
+// FP64 path, float for the FP32-bulk path, Dual<N> (rkdg_dual.cuh) for the
+// discrete adjoint.  In the FP32 path the pressure is recovered in FP64
+// whenever internal energy loses more than three digits to cancellation (near
+// vacuum / strong shocks), and divisions / square roots use the hardware
+// reciprocal and reciprocal-square-root approximations (about 2 ulp) instead
+// of the multi-instruction IEEE sequences; double and Dual keep IEEE
+// division and square root.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -14,8 +18,20 @@
 namespace rkdg {
 
 template <typename R>
-__device__ __forceinline__ R rsqrt_(R x) {
+__device__ __forceinline__ R fdv(R a, R b) {
+  return a / b;
+}
+template <>
+__device__ __forceinline__ float fdv<float>(float a, float b) {
+  return __fdividef(a, b);
+}
+template <typename R>
+__device__ __forceinline__ R fsq(R x) {
   return sqrt(x);
+}
+template <>
+__device__ __forceinline__ float fsq<float>(float x) {
+  return x > 0.0f ? x * rsqrtf(x) : 0.0f;
 }
 
 // ComputePressure (physics.cpp:101-112), covolume EoS.
@@ -25,7 +41,7 @@ __device__ __forceinline__ R pressure(const R* s, R gamma, R b) {
   R v2 = R(0);
 #pragma unroll
   for (int d = 0; d < DIM; d++) v2 += s[1 + d] * s[1 + d];
-  v2 /= den;
+  v2 = fdv(v2, den);
   const R ie = s[1 + DIM] - R(0.5) * v2;
   if constexpr (std::is_same<R, float>::value) {
     if (fabsf(ie) < 1e-3f * fabsf(s[1 + DIM])) {
@@ -37,14 +53,14 @@ __device__ __forceinline__ R pressure(const R* s, R gamma, R b) {
                      (1.0 - (double)den * (double)b));
     }
   }
-  return (gamma - R(1)) * ie / (R(1) - den * b);
+  return fdv((gamma - R(1)) * ie, R(1) - den * b);
 }
 
 // ComputeSoundSpeed (physics.cpp:134-140)
 template <int DIM, typename R>
 __device__ __forceinline__ R sound_speed_p(const R* s, R p, R gamma, R b) {
   const R den = s[0];
-  return sqrt(gamma * p / den / (R(1) - den * b));
+  return fsq(fdv(fdv(gamma * p, den), R(1) - den * b));
 }
 
 // StateIsPhysical (physics.cpp:6-50): covolume-aware pressure.
@@ -69,7 +85,7 @@ __device__ __forceinline__ bool state_is_physical_say(const R* s, R gamma) {
   R v2 = R(0);
 #pragma unroll
   for (int i = 0; i < DIM; i++) v2 += s[1 + i] * s[1 + i];
-  v2 /= den;
+  v2 = fdv(v2, den);
   const R p = (gamma - R(1)) * (e - R(0.5) * v2);
   if (p <= R(0) || p != p) return false;
   return true;
@@ -82,10 +98,10 @@ __device__ __forceinline__ R max_char_speed(const R* s, R gamma, R b) {
   R v2 = R(0);
 #pragma unroll
   for (int d = 0; d < DIM; d++) v2 += s[1 + d] * s[1 + d];
-  v2 /= den;
+  v2 = fdv(v2, den);
   const R p = pressure<DIM>(s, gamma, b);
   const R c = sound_speed_p<DIM>(s, p, gamma, b);
-  return sqrt(v2 / den) + c;
+  return fsq(fdv(v2, den)) + c;
 }
 
 // ComputeFlux (physics.cpp:143-168): F[k][d]; also returns |u|+c at the node
@@ -93,7 +109,7 @@ __device__ __forceinline__ R max_char_speed(const R* s, R gamma, R b) {
 template <int DIM, typename R>
 __device__ __forceinline__ R flux_and_speed(const R* s, R F[DIM + 2][DIM], R gamma, R b) {
   const R den = s[0];
-  const R inv = R(1) / den;
+  const R inv = fdv(R(1), den);
   R v2 = R(0);
 #pragma unroll
   for (int d = 0; d < DIM; d++) v2 += s[1 + d] * s[1 + d];
@@ -108,8 +124,8 @@ __device__ __forceinline__ R flux_and_speed(const R* s, R F[DIM + 2][DIM], R gam
   const R H = (s[1 + DIM] + pres) * inv;
 #pragma unroll
   for (int d = 0; d < DIM; d++) F[1 + DIM][d] = s[1 + d] * H;
-  const R c = sqrt(gamma * pres * inv / (R(1) - den * b));
-  return sqrt(v2 * inv * inv) + c;
+  const R c = fsq(fdv(gamma * pres * inv, R(1) - den * b));
+  return fsq(v2 * inv * inv) + c;
 }
 
 // ComputeFluxDotN (physics.cpp:171-195)
@@ -121,8 +137,8 @@ __device__ __forceinline__ void flux_dot_n(const R* s, const R* n, R* fn, R p) {
   for (int d = 0; d < DIM; d++) dvn += s[1 + d] * n[d];
   fn[0] = dvn;
 #pragma unroll
-  for (int d = 0; d < DIM; d++) fn[1 + d] = dvn * s[1 + d] / den + p * n[d];
-  const R H = (s[1 + DIM] + p) / den;
+  for (int d = 0; d < DIM; d++) fn[1 + d] = fdv(dvn * s[1 + d], den) + p * n[d];
+  const R H = fdv(s[1 + DIM] + p, den);
   fn[1 + DIM] = dvn * H;
 }
 
@@ -130,10 +146,10 @@ __device__ __forceinline__ void flux_dot_n(const R* s, const R* n, R* fn, R p) {
 template <int DIM, typename R>
 __device__ __forceinline__ void flux_F(const R* s, R* f, R p) {
   f[0] = s[1];
-  f[1] = s[1] * s[1] / s[0] + p;
+  f[1] = fdv(s[1] * s[1], s[0]) + p;
 #pragma unroll
-  for (int d = 1; d < DIM; d++) f[d + 1] = s[1] * s[d + 1] / s[0];
-  const R H = (s[1 + DIM] + p) / s[0];
+  for (int d = 1; d < DIM; d++) f[d + 1] = fdv(s[1] * s[d + 1], s[0]);
+  const R H = fdv(s[1 + DIM] + p, s[0]);
   f[1 + DIM] = s[1] * H;
 }
 
@@ -149,10 +165,10 @@ __device__ __forceinline__ void rotate(R* s, const R* n) {
     m[1] = my;
   } else {
     const R sp = n[2];
-    const R cp = sqrt(R(1) - sp * sp);
+    const R cp = fsq(R(1) - sp * sp);
     const bool ok = fabs(cp) > R(1e-6);
-    const R st = ok ? n[1] / cp : R(1);
-    const R ct = ok ? n[0] / cp : R(0);
+    const R st = ok ? fdv(n[1], cp) : R(1);
+    const R ct = ok ? fdv(n[0], cp) : R(0);
     const R mx = cp * ct * m[0] + cp * st * m[1] + sp * m[2];
     const R my = -st * m[0] + ct * m[1];
     const R mz = -sp * ct * m[0] - sp * st * m[1] + cp * m[2];
@@ -171,10 +187,10 @@ __device__ __forceinline__ void inverse_rotate(R* s, const R* n) {
     m[1] = my;
   } else {
     const R sp = n[2];
-    const R cp = sqrt(R(1) - sp * sp);
+    const R cp = fsq(R(1) - sp * sp);
     const bool ok = fabs(cp) > R(1e-6);
-    const R st = ok ? n[1] / cp : R(1);
-    const R ct = ok ? n[0] / cp : R(0);
+    const R st = ok ? fdv(n[1], cp) : R(1);
+    const R ct = ok ? fdv(n[0], cp) : R(0);
     const R mx = cp * ct * m[0] - st * m[1] - sp * ct * m[2];
     const R my = cp * st * m[0] + ct * m[1] - sp * st * m[2];
     const R mz = sp * m[0] + cp * m[2];
@@ -199,24 +215,24 @@ __device__ __forceinline__ void wave_speeds(const R* s1, const R* s2, R p1, R p2
   const R cR = sound_speed_p<DIM>(s2, p2, gamma, b);
   if (avg == 1) {
     const R ruL = s1[1], ruR = s2[1];
-    const R uL = ruL / s1[0], uR = ruR / s2[0];
-    const R sL = sqrt(s1[0]), sR = sqrt(s2[0]);
+    const R uL = fdv(ruL, s1[0]), uR = fdv(ruR, s2[0]);
+    const R sL = fsq(s1[0]), sR = fsq(s2[0]);
     const R sum = sL + sR;
-    const R eta2 = R(0.5) * sL * sR / ((sL + sR) * (sL + sR));
-    const R uav = (ruL / sL + ruR / sR) / sum;
-    const R cav = sqrt((sL * cL * cL + sR * cR * cR) / sum + eta2 * (uR - uL) * (uR - uL));
+    const R eta2 = fdv(R(0.5) * sL * sR, (sL + sR) * (sL + sR));
+    const R uav = fdv(fdv(ruL, sL) + fdv(ruR, sR), sum);
+    const R cav = fsq(fdv(sL * cL * cL + sR * cR * cR, sum) + eta2 * (uR - uL) * (uR - uL));
     SL = uav - cav;
     SR = uav + cav;
     return;
   }
-  const R uL = s1[1] / s1[0], uR = s2[1] / s2[0];
-  const R z = R(0.5) * (gamma - R(1)) / gamma;
-  const R pStar = powr(
-      (cL + cR - R(0.5) * (gamma - R(1)) * (uR - uL)) / (cL / powr(p1, z) + cR / powr(p2, z)),
-      R(1) / z);
-  const R qL = pStar > p1 ? sqrt(R(1) + R(0.5) * (gamma + R(1)) * (pStar / p1 - R(1)) / gamma)
+  const R uL = fdv(s1[1], s1[0]), uR = fdv(s2[1], s2[0]);
+  const R z = fdv(R(0.5) * (gamma - R(1)), gamma);
+  const R pStar = powr(fdv(cL + cR - R(0.5) * (gamma - R(1)) * (uR - uL),
+                           fdv(cL, powr(p1, z)) + fdv(cR, powr(p2, z))),
+                       fdv(R(1), z));
+  const R qL = pStar > p1 ? fsq(R(1) + fdv(R(0.5) * (gamma + R(1)) * (fdv(pStar, p1) - R(1)), gamma))
                           : R(1);
-  const R qR = pStar > p2 ? sqrt(R(1) + R(0.5) * (gamma + R(1)) * (pStar / p2 - R(1)) / gamma)
+  const R qR = pStar > p2 ? fsq(R(1) + fdv(R(0.5) * (gamma + R(1)) * (fdv(pStar, p2) - R(1)), gamma))
                           : R(1);
   SL = uL - qL * cL;
   SR = uR + qR * cR;
@@ -241,8 +257,8 @@ __device__ __forceinline__ R riemann(R* s1, R* s2, const R* n, R* flux, R gamma,
       v1 += s1[1 + d] * s1[1 + d];
       v2 += s2[1 + d] * s2[1 + d];
     }
-    const R e1 = sqrt(v1 / s1[0] / s1[0]) + sound_speed_p<DIM>(s1, p1, gamma, b);
-    const R e2 = sqrt(v2 / s2[0] / s2[0]) + sound_speed_p<DIM>(s2, p2, gamma, b);
+    const R e1 = fsq(fdv(fdv(v1, s1[0]), s1[0])) + sound_speed_p<DIM>(s1, p1, gamma, b);
+    const R e2 = fsq(fdv(fdv(v2, s2[0]), s2[0])) + sound_speed_p<DIM>(s2, p2, gamma, b);
     const R maxE = e1 > e2 ? e1 : e2;
     R f1[NEQ], f2[NEQ];
     flux_dot_n<DIM>(s1, n, f1, p1);
@@ -250,10 +266,10 @@ __device__ __forceinline__ R riemann(R* s1, R* s2, const R* n, R* flux, R gamma,
     R nm = R(0);
 #pragma unroll
     for (int i = 0; i < DIM; i++) nm += n[i] * n[i];
-    nm = sqrt(nm);
+    nm = fsq(nm);
 #pragma unroll
     for (int i = 0; i < NEQ; i++)
-      flux[i] = R(0.5) * (f1[i] + f2[i]) / nm - R(0.5) * maxE * (s2[i] - s1[i]);
+      flux[i] = fdv(R(0.5) * (f1[i] + f2[i]), nm) - R(0.5) * maxE * (s2[i] - s1[i]);
     return maxE;
   }
   rotate<DIM>(s1, n);
@@ -280,9 +296,14 @@ __device__ __forceinline__ R riemann(R* s1, R* s2, const R* n, R* flux, R gamma,
 #pragma unroll
       for (int i = 0; i < NEQ; ++i) flux[i] = f2[i];
     } else {
+      const R inv = fdv(R(1), SR - SL);
 #pragma unroll
-      for (int i = 0; i < NEQ; ++i)
-        flux[i] = (SR * f1[i] - SL * f2[i] + SL * SR * (s2[i] - s1[i])) / (SR - SL);
+      for (int i = 0; i < NEQ; ++i) {
+        if constexpr (std::is_same<R, float>::value)
+          flux[i] = (SR * f1[i] - SL * f2[i] + SL * SR * (s2[i] - s1[i])) * inv;
+        else
+          flux[i] = (SR * f1[i] - SL * f2[i] + SL * SR * (s2[i] - s1[i])) / (SR - SL);
+      }
     }
     ret = maxE;
   } else {
@@ -294,9 +315,9 @@ __device__ __forceinline__ R riemann(R* s1, R* s2, const R* n, R* flux, R gamma,
 #pragma unroll
       for (int i = 0; i < NEQ; ++i) flux[i] = f2[i];
     } else {
-      const R cL = SL - s1[1] / s1[0];
-      const R cR = SR - s2[1] / s2[0];
-      const R sStar = (p2 - p1 + s1[1] * cL - s2[1] * cR) / (s1[0] * cL - s2[0] * cR);
+      const R cL = SL - fdv(s1[1], s1[0]);
+      const R cR = SR - fdv(s2[1], s2[0]);
+      const R sStar = fdv(p2 - p1 + s1[1] * cL - s2[1] * cR, s1[0] * cL - s2[0] * cR);
       const bool left = sStar > R(0);
       const R* st = left ? s1 : s2;
       const R* fK = left ? f1 : f2;
@@ -304,8 +325,8 @@ __device__ __forceinline__ R riemann(R* s1, R* s2, const R* n, R* flux, R gamma,
       const R SK = left ? SL : SR;
       const R cK = left ? cL : cR;
       const R rhoL = st[0];
-      const R extra = SK * (pK + rhoL * cK * (sStar - st[1] / st[0]));
-      const R inv = R(1) / (SK - sStar);
+      const R extra = SK * (pK + rhoL * cK * (sStar - fdv(st[1], st[0])));
+      const R inv = fdv(R(1), SK - sStar);
 #pragma unroll
       for (int i = 0; i < NEQ; ++i) {
         const R Di = (i == 1) ? R(1) : ((i == DIM + 1) ? sStar : R(0));
