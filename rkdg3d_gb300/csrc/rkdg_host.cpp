@@ -1519,4 +1519,27 @@ int rkdg_adjoint_run(rkdg_ctx* c, const double* x0, int nsteps, double dt, int e
 
 long long rkdg_kernel_launches(rkdg_ctx* c) { return c ? c->launches : -1; }
 
+// rkdg_limit with the cell means in the library's fixed device array: the
+// means kernel writes all neq * NE entries before the limiter kernel reads
+// them on the same stream, so nothing needs clearing first.
+int rkdg_limit_static(rkdg_ctx* c, double* x) {
+  NEED_MESH(c);
+  if (!x) return fail(c, RKDG_ERR_INVALID, "null state pointer");
+  const unsigned long long need = (unsigned long long)c->neq * (unsigned long long)c->ne;
+  if (need > RKDG_LIMIT_STATIC_MAX_VALUES)
+    return fail(c, RKDG_ERR_INVALID,
+                "mesh too large for the fixed limiter scratch: neq * NE = " + std::to_string(need) +
+                    " > " + std::to_string(RKDG_LIMIT_STATIC_MAX_VALUES));
+  if (!c->limiter_active()) return RKDG_OK;
+  double* means = nullptr;
+  CUDA_TRY(c, rkdg::static_means_scratch(c->device, &means));
+  CUDA_TRY(c, rkdg::launch_means(c->geom, c->p, 0, c->ne, c->ndofs, c->d_tab, x, nullptr, means, c->stream));
+  LimParams L = lim_params(c);
+  L.means = means;
+  CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 0, L, x, nullptr, c->stream));
+  c->launches += 2;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return RKDG_OK;
+}
+
 }  // extern "C"

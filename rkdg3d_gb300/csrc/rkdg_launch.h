@@ -53,6 +53,8 @@ cudaError_t launch_limit_vjp_gather(int geom, int p, const RhsParams& prm, const
                                     double* zb, cudaStream_t st);
 cudaError_t launch_axpy(long long n, double a, const double* x, double* y, cudaStream_t st);
 cudaError_t launch_scale_copy(long long n, double a, const double* x, double* y, cudaStream_t st);
+// Fixed means scratch of rkdg_limit_static on `device` (must be current).
+cudaError_t static_means_scratch(int device, double** out);
 
 // Template launch helpers shared by the per-geometry translation units.
 template <int G, int P>

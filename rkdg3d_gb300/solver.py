@@ -217,6 +217,12 @@ class Context:
     def limit(self, x):
         self._chk(self._L.rkdg_limit(self.h, _ptr(x)))
 
+    def limit_static(self, x):
+        """Same as limit(), with the cell means in the library's fixed device
+        array instead of context memory (no allocation; one call at a time
+        per device)."""
+        self._chk(self._L.rkdg_limit_static(self.h, _ptr(x)))
+
     def cell_means(self, x, means):
         self._chk(self._L.rkdg_cell_means(self.h, _ptr(x), _ptr(means)))
 
