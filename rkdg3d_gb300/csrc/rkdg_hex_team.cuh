@@ -32,14 +32,20 @@ struct TeamSize {
   static constexpr int N1 = P + 1, NQ1 = P + 2, ND = N1 * N1 * N1, NQF = NQ1 * NQ1, NEQ = 5,
                        NF2 = N1 * N1;
   static constexpr int TPW = 6, WARPS = 4, EPB = TPW * WARPS, THREADS = 32 * WARPS;
-  // per team exchange: max(traces + fluxes, volume fluxes)
+  // per team exchange: max(traces + fluxes, volume fluxes), padded to whole
+  // 32-word rows; team t of a warp starts xoff(t) words into its row so that
+  // the team-parallel stores (30 lanes) and the warp-parallel flux reads (two
+  // teams of 16 points) fall in distinct banks
   static constexpr int XF = 3 * NEQ * NQF, XV = 3 * NEQ * ND;
   static constexpr int XCH = XF > XV ? XF : XV;
+  static constexpr int XSTR = (XCH + 31) & ~31;
+  static constexpr int WSTR = TPW * XSTR + 32;
   static constexpr int TAB = NQ1 * N1 + 2 * N1 + 2 * N1 * N1 + N1 + NQF;
   static constexpr int TAB_AL = (TAB + 3) & ~3;
+  __host__ __device__ static constexpr int xoff(int t) { return 16 * (t & 1) + 5 * (t >> 1); }
   template <typename R>
   static constexpr size_t smem_bytes() {
-    return sizeof(R) * (size_t)(TAB_AL + EPB * NEQ * ND + EPB * XCH);
+    return sizeof(R) * (size_t)(TAB_AL + EPB * NEQ * ND + WARPS * WSTR);
   }
 };
 
@@ -101,8 +107,8 @@ __device__ __forceinline__ void team_contract_g_any(int lf, const R* __restrict_
 }
 
 // v (N1 x N1 on the face's tangential axes) -> values at the NQ1 x NQ1 face
-// points in tensor order a + NQ1*b, written to dst.
-template <int P, typename R>
+// points in tensor order a + NQ1*b, written to dst[(a + NQ1*b) * ST].
+template <int P, int ST, typename R>
 __device__ __forceinline__ void team_interp(const R (&v)[(P + 1) * (P + 1)], const R* l1d, R* dst) {
   constexpr int N1 = P + 1, NQ1 = P + 2;
   R w[NQ1][N1];
@@ -122,12 +128,12 @@ __device__ __forceinline__ void team_interp(const R (&v)[(P + 1) * (P + 1)], con
       R s = R(0);
 #pragma unroll
       for (int i1 = 0; i1 < N1; ++i1) s += l1d[b * N1 + i1] * w[a][i1];
-      dst[a + NQ1 * b] = s;
+      dst[(a + NQ1 * b) * ST] = s;
     }
 }
 
-// Lift face values f (tensor order) of face LF into the accumulators.
-template <int P, int LF, typename R>
+// Lift face values f[(a + NQ1*b) * ST] of face LF into the accumulators.
+template <int P, int LF, int ST, typename R>
 __device__ __forceinline__ void team_lift(const R* f, const R* l1d, const R* lend,
                                           R (&acc)[(P + 1) * (P + 1) * (P + 1)]) {
   constexpr int N1 = P + 1, NQ1 = P + 2, NAX = hex_face_axis(LF), SD = hex_face_side(LF);
@@ -138,7 +144,7 @@ __device__ __forceinline__ void team_lift(const R* f, const R* l1d, const R* len
     for (int b = 0; b < NQ1; ++b) {
       R s = R(0);
 #pragma unroll
-      for (int a = 0; a < NQ1; ++a) s += l1d[a * N1 + i0] * f[a + NQ1 * b];
+      for (int a = 0; a < NQ1; ++a) s += l1d[a * N1 + i0] * f[(a + NQ1 * b) * ST];
       w[i0][b] = s;
     }
 #pragma unroll
@@ -166,44 +172,36 @@ __device__ __forceinline__ void team_contract_any(int lf, const R (&u)[(P + 1) *
   }
 }
 
-template <int P, typename R>
+template <int P, int ST, typename R>
 __device__ __forceinline__ void team_lift_any(int lf, const R* f, const R* l1d, const R* lend,
                                               R (&acc)[(P + 1) * (P + 1) * (P + 1)]) {
   switch (lf) {
-    case 0: team_lift<P, 0>(f, l1d, lend, acc); break;
-    case 1: team_lift<P, 1>(f, l1d, lend, acc); break;
-    case 2: team_lift<P, 2>(f, l1d, lend, acc); break;
-    case 3: team_lift<P, 3>(f, l1d, lend, acc); break;
-    case 4: team_lift<P, 4>(f, l1d, lend, acc); break;
-    default: team_lift<P, 5>(f, l1d, lend, acc); break;
+    case 0: team_lift<P, 0, ST>(f, l1d, lend, acc); break;
+    case 1: team_lift<P, 1, ST>(f, l1d, lend, acc); break;
+    case 2: team_lift<P, 2, ST>(f, l1d, lend, acc); break;
+    case 3: team_lift<P, 3, ST>(f, l1d, lend, acc); break;
+    case 4: team_lift<P, 4, ST>(f, l1d, lend, acc); break;
+    default: team_lift<P, 5, ST>(f, l1d, lend, acc); break;
   }
 }
 
-// One face (runtime index lf) of one element, for the team's variable k.
-// The register arrays need compile-time indices only in the own-side
-// contraction and the lift (small switches); the neighbour contraction reads
-// global memory through a node table, and the numerical flux has a single
-// call site.
+// Phase 1 of one face (runtime index LF) for the team's variable k: the own
+// trace and, across an interior face, the neighbour's trace at the face
+// points, stored point-major (To[q*NEQ + k], Tn[q*NEQ + k]).  The register
+// arrays need compile-time indices only in the own-side contraction (a small
+// switch); the neighbour's values come from the staged tile when it is there,
+// else from global memory, through a node table.
 template <int P, typename R>
-__device__ __forceinline__ void team_face(const int LF, const RhsParams& prm, const R* __restrict__ ug,
-                                          int e, int k, int tl, R (&u)[(P + 1) * (P + 1) * (P + 1)],
-                                          R (&acc)[(P + 1) * (P + 1) * (P + 1)], R* xch,
-                                          const R* l1d, const R* lend, const R* wf,
-                                          const unsigned char (*perm)[(P + 2) * (P + 2)],
-                                          const int (*fab)[RKDG_MAX_NQF],
-                                          const unsigned char (*nodet)[(P + 1) * (P + 1) * (P + 1)],
-                                          const int* fnb, const int* fcd, const R* sU, int e0,
-                                          int nel, R gamma, R cov, R& lmax, unsigned mask) {
+__device__ __forceinline__ void team_traces(const int LF, const R* __restrict__ ug, long long NDa,
+                                            int k, const R (&u)[(P + 1) * (P + 1) * (P + 1)], R* xch,
+                                            const R* l1d, const R* lend,
+                                            const unsigned char (*nodet)[(P + 1) * (P + 1) * (P + 1)],
+                                            int nb, int code, const R* sU, int e0, int nel) {
   using S = TeamSize<P>;
   constexpr int N1 = S::N1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, NF2 = S::NF2;
-  const int ne = prm.ne;
-  const long long NDa = prm.ndofs;
-  const int nb = fnb[LF], code = fcd[LF];  // preloaded face table entries
-  if (nb == -1) return;
-  R* To = xch;                 // [NEQ][NQF] own traces (tensor order)
-  R* Tn = To + NEQ * NQF;      // [NEQ][NQF] neighbour traces (its tensor order)
-  R* Fh = Tn + NEQ * NQF;      // [NEQ][NQF] lifted flux values (own tensor order)
-  const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
+  R* To = xch;
+  R* Tn = To + NEQ * NQF;
+  const int lfo = code & 7;
   // issue the neighbour's loads first; the own-side work hides their latency
   R nbv[ND];
   if (nb >= 0) {
@@ -221,7 +219,7 @@ __device__ __forceinline__ void team_face(const int LF, const RhsParams& prm, co
   {
     R v[N1 * N1];
     team_contract_any<P>(LF, u, lend, v);
-    team_interp<P>(v, l1d, To + k * NQF);
+    team_interp<P, NEQ>(v, l1d, To + k);
   }
   if (nb >= 0) {
     const int sdn = hex_face_side(lfo);
@@ -233,50 +231,68 @@ __device__ __forceinline__ void team_face(const int LF, const RhsParams& prm, co
       for (int jn = 0; jn < N1; ++jn) s += lend[sdn * N1 + jn] * nbv[r * N1 + jn];
       v[r] = s;
     }
-    team_interp<P>(v, l1d, Tn + k * NQF);
+    team_interp<P, NEQ>(v, l1d, Tn + k);
   }
-  __syncwarp(mask);
-  const R* fg = (const R*)prm.fgeo;
-  R n[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) n[c] = fg[(long long)(LF * 4 + c) * ne + e];
-  const R jac = fg[(long long)(LF * 4 + 3) * ne + e];
-  const R sg = side ? R(1) : R(-1);
+}
+
+// Phase 2 of face LF: the numerical flux at the face points of all the warp's
+// elements, spread over the 32 lanes (point pt of the warp = team pt / NQF,
+// point pt % NQF); arguments in Elem1, Elem2 order with the Elem1-outward
+// normal (face_integrator.cpp:11-276), boundary faces through the boundary
+// condition's right state.  Writes sign * w_q * |J_f| * Fhat to the team's
+// Fh[q*NEQ + k] in its own tensor order.
+template <int P, typename R>
+__device__ __forceinline__ void warp_fluxes(const int LF, const RhsParams& prm, int lane, int wel0,
+                                            int nel, R* wx, const R* wf,
+                                            const unsigned char (*perm)[(P + 2) * (P + 2)],
+                                            const int (*fab)[RKDG_MAX_NQF], const int (*sfnb)[6],
+                                            const int (*sfcd)[6], const R (*sgeo)[6][4], int e0,
+                                            R gamma, R cov, R& lmax) {
+  using S = TeamSize<P>;
+  constexpr int NQF = S::NQF, NEQ = S::NEQ, TPW = S::TPW;
 #pragma unroll 1
-  for (int rr = 0; rr < (NQF + NEQ - 1) / NEQ; ++rr) {
-    const int q = tl + NEQ * rr;
-    if (q < NQF) {
+  for (int pt = lane; pt < TPW * NQF; pt += 32) {
+    const int t = pt / NQF, q = pt - t * NQF;
+    const int el = wel0 + t;
+    if (el >= nel) continue;
+    const int nb = sfnb[el][LF];
+    if (nb == -1) continue;
+    const int code = sfcd[el][LF];
+    R* To = wx + t * S::XSTR + S::xoff(t);
+    const R* Tn = To + NEQ * NQF;
+    R* Fh = To + 2 * NEQ * NQF;
+    const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
+    R n[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) n[c] = sgeo[el][LF][c];
+    const R jac = sgeo[el][LF][3];
+    R s1[NEQ], s2[NEQ];
+    int own = fab[LF][q];
+    if (nb >= 0) {
       const int q2 = perm[pid][q];
-      R s1[NEQ], s2[NEQ];
-      int own = fab[LF][q];
-      if (nb >= 0) {
-        const int a1 = side ? fab[lfo][q] : fab[LF][q];
-        const int a2 = side ? fab[LF][q2] : fab[lfo][q2];
-        const R* T1 = side ? Tn : To;
-        const R* T2 = side ? To : Tn;
+      const int a1 = side ? fab[lfo][q] : fab[LF][q];
+      const int a2 = side ? fab[LF][q2] : fab[lfo][q2];
+      const R* T1 = side ? Tn : To;
+      const R* T2 = side ? To : Tn;
 #pragma unroll
-        for (int kk = 0; kk < NEQ; ++kk) {
-          s1[kk] = T1[kk * NQF + a1];
-          s2[kk] = T2[kk * NQF + a2];
-        }
-        if (side) own = a2;
-      } else {
-#pragma unroll
-        for (int kk = 0; kk < NEQ; ++kk) s1[kk] = To[kk * NQF + own];
-        const BCSlot& bc = prm.bc[-2 - nb];
-        right_state<3>(bc.type, bc.state, s1, s2, n);
+      for (int kk = 0; kk < NEQ; ++kk) {
+        s1[kk] = T1[a1 * NEQ + kk];
+        s2[kk] = T2[a2 * NEQ + kk];
       }
-      R F[NEQ];
-      const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e);
-      lmax = fmax(lmax, sp);
-      const R wq = wf[q];
+      if (side) own = a2;
+    } else {
 #pragma unroll
-      for (int kk = 0; kk < NEQ; ++kk) Fh[kk * NQF + own] = sg * (F[kk] * wq) * jac;
+      for (int kk = 0; kk < NEQ; ++kk) s1[kk] = To[own * NEQ + kk];
+      const BCSlot& bc = prm.bc[-2 - nb];
+      right_state<3>(bc.type, bc.state, s1, s2, n);
     }
+    R F[NEQ];
+    const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e0 + el);
+    lmax = fmax(lmax, sp);
+    const R w = (side ? R(1) : R(-1)) * wf[q] * jac;
+#pragma unroll
+    for (int kk = 0; kk < NEQ; ++kk) Fh[own * NEQ + kk] = w * F[kk];
   }
-  __syncwarp(mask);
-  if (!prm.faces_only) team_lift_any<P>(LF, Fh + k * NQF, l1d, lend, acc);
-  __syncwarp(mask);
 }
 
 template <int P, typename R>
@@ -296,7 +312,7 @@ __global__ void __launch_bounds__(128)
   R* tW1 = tMinv + N1 * N1;     // [N1]
   R* tWf = tW1 + N1;            // [NQF]
   R* sU = sm + S::TAB_AL;       // [EPB][NEQ][ND]
-  R* sX = sU + EPB * NEQ * ND;  // [EPB][XCH]
+  R* sX = sU + EPB * NEQ * ND;  // [WARPS][WSTR] team exchange rows
   const RefTables* T = prm.tab;
   const int tid = threadIdx.x;
   for (int t = tid; t < NQ1 * N1; t += blockDim.x) tL1[t] = (R)T->l1d[t / N1][t % N1];
@@ -319,10 +335,18 @@ __global__ void __launch_bounds__(128)
   const int e0 = blockIdx.x * EPB;
   const int nel = min(EPB, ne - e0);
   __shared__ int sFnb[EPB][6], sFcd[EPB][6];
-  for (int t = tid; t < nel * 6; t += blockDim.x) {
-    const int lf = t / nel, el = t % nel;
-    sFnb[el][lf] = prm.fnbr[lf * ne + e0 + el];
-    sFcd[el][lf] = prm.fcode[lf * ne + e0 + el];
+  __shared__ R sGeo[EPB][6][4];  // unit normal and |J_f| per (element, face)
+  {
+    const R* fg = (const R*)prm.fgeo;
+    for (int t = tid; t < nel * 6; t += blockDim.x) {
+      const int lf = t / nel, el = t % nel;
+      sFnb[el][lf] = prm.fnbr[lf * ne + e0 + el];
+      sFcd[el][lf] = prm.fcode[lf * ne + e0 + el];
+    }
+    for (int t = tid; t < nel * 24; t += blockDim.x) {
+      const int c = t / nel, el = t % nel;  // c = lf * 4 + component
+      sGeo[el][c >> 2][c & 3] = fg[(long long)c * ne + e0 + el];
+    }
   }
   for (int k = 0; k < NEQ; ++k)
     for (int t = tid; t < nel * ND; t += blockDim.x)
@@ -340,7 +364,9 @@ __global__ void __launch_bounds__(128)
   R lmax = R(0);
   const int e = e0 + el;
   const int k = tl;
-  R* xch = sX + el * S::XCH;
+  const int wel0 = warp * S::TPW;
+  R* wx = sX + warp * S::WSTR;
+  R* xch = wx + (team < S::TPW ? team * S::XSTR + S::xoff(team) : 0);
   R uv[ND], acc[ND];
   if (act) {
 #pragma unroll
@@ -348,10 +374,20 @@ __global__ void __launch_bounds__(128)
       uv[i] = sU[(el * NEQ + k) * ND + i];
       acc[i] = R(0);
     }
+  }
+  // the warp steps through the six faces together: traces per team, the
+  // numerical fluxes over all 32 lanes, the lifting per team again
 #pragma unroll 1
-    for (int lf = 0; lf < 6; ++lf)
-      team_face<P, R>(lf, prm, u, e, k, tl, uv, acc, xch, tL1, tLend, tWf, sPerm, sFab, sNodeT,
-                      sFnb[el], sFcd[el], sU, e0, nel, gamma, cov, lmax, mask);
+  for (int lf = 0; lf < 6; ++lf) {
+    const int nb = act ? sFnb[el][lf] : -1;
+    if (nb != -1)
+      team_traces<P, R>(lf, u, NDa, k, uv, xch, tL1, tLend, sNodeT, nb, sFcd[el][lf], sU, e0, nel);
+    __syncwarp();
+    warp_fluxes<P, R>(lf, prm, lane, wel0, nel, wx, tWf, sPerm, sFab, sFnb, sFcd, sGeo, e0, gamma,
+                      cov, lmax);
+    __syncwarp();
+    if (nb != -1 && !prm.faces_only)
+      team_lift_any<P, NEQ>(lf, xch + 2 * NEQ * NQF + k, tL1, tLend, acc);
   }
   // neighbours inside the tile were read from the staged DOFs, which the
   // volume phase below overwrites with the result

@@ -104,10 +104,92 @@ __device__ __forceinline__ R max_char_speed(const R* s, R gamma, R b) {
   return fsq(fdv(v2, den)) + c;
 }
 
+// FP32 pointwise state quantities with one reciprocal of the density and one
+// of the covolume factor: r = 1/rho, q = 1/(1 - rho b), the pressure (FP64
+// where E - |m|^2/(2 rho) cancels, as pressure() does) and |u| + c.  Returns
+// false where StateIsPhysicalSay fails (rho < 0, E <= 0, perfect-gas p <= 0,
+// NaN).  Same quantities as the double path, rounded in a different order.
+template <int DIM>
+__device__ __forceinline__ bool state_f32(const float* s, float gamma, float b, float& r, float& q,
+                                          float& p, float& speed) {
+  const float den = s[0], E = s[1 + DIM];
+  if (!(den >= 0.0f) || !(E > 0.0f)) return false;
+  r = __fdividef(1.0f, den);
+  float m2 = 0.0f;
+#pragma unroll
+  for (int d = 0; d < DIM; d++) m2 = fmaf(s[1 + d], s[1 + d], m2);
+  const float v2 = m2 * r;  // |m|^2 / rho
+  const float ie = E - 0.5f * v2;
+  if (!((gamma - 1.0f) * ie > 0.0f)) return false;
+  q = __fdividef(1.0f, 1.0f - den * b);
+  if (fabsf(ie) < 1e-3f * fabsf(E)) {
+    double m2d = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) m2d += (double)s[1 + d] * (double)s[1 + d];
+    p = (float)(((double)gamma - 1.0) * ((double)E - 0.5 * m2d / (double)den) /
+                (1.0 - (double)den * (double)b));
+  } else {
+    p = (gamma - 1.0f) * ie * q;
+  }
+  speed = fsq(v2 * r) + fsq(gamma * p * r * q);
+  return true;
+}
+
+// FP32 Rusanov flux (rs_rusanov.cpp:6-40) on unrotated states, built on
+// state_f32.  Returns the wave speed, or -1 for a non-physical state.
+template <int DIM>
+__device__ __forceinline__ float rusanov_f32(const float* s1, const float* s2, const float* n,
+                                             float* flux, float gamma, float b) {
+  constexpr int NEQ = DIM + 2;
+  float r1, q1, p1, e1, r2, q2, p2, e2;
+  if (!state_f32<DIM>(s1, gamma, b, r1, q1, p1, e1)) return -1.0f;
+  if (!state_f32<DIM>(s2, gamma, b, r2, q2, p2, e2)) return -1.0f;
+  const float maxE = e1 > e2 ? e1 : e2;
+  float d1 = 0.0f, d2 = 0.0f, nn = 0.0f;
+#pragma unroll
+  for (int d = 0; d < DIM; d++) {
+    d1 = fmaf(s1[1 + d], n[d], d1);
+    d2 = fmaf(s2[1 + d], n[d], d2);
+    nn = fmaf(n[d], n[d], nn);
+  }
+  const float h = 0.5f * rsqrtf(nn), a = 0.5f * maxE;
+  const float u1 = d1 * r1, u2 = d2 * r2;
+  flux[0] = h * (d1 + d2) - a * (s2[0] - s1[0]);
+#pragma unroll
+  for (int d = 0; d < DIM; d++)
+    flux[1 + d] = h * (fmaf(u1, s1[1 + d], p1 * n[d]) + fmaf(u2, s2[1 + d], p2 * n[d])) -
+                  a * (s2[1 + d] - s1[1 + d]);
+  flux[NEQ - 1] = h * (u1 * (s1[NEQ - 1] + p1) + u2 * (s2[NEQ - 1] + p2)) -
+                  a * (s2[NEQ - 1] - s1[NEQ - 1]);
+  return maxE;
+}
+
 // ComputeFlux (physics.cpp:143-168): F[k][d]; also returns |u|+c at the node
 // (FE_Evolution::GetFlux, fe_evolution.cpp:219-245).
 template <int DIM, typename R>
 __device__ __forceinline__ R flux_and_speed(const R* s, R F[DIM + 2][DIM], R gamma, R b) {
+  if constexpr (std::is_same<R, float>::value) {
+    float r, q, p, speed;
+    if (!state_f32<DIM>(s, gamma, b, r, q, p, speed)) {
+      // non-physical node: same arithmetic as the double path
+      r = __fdividef(1.0f, s[0]);
+      p = pressure<DIM>(s, gamma, b);
+      float m2 = 0.0f;
+#pragma unroll
+      for (int d = 0; d < DIM; d++) m2 += s[1 + d] * s[1 + d];
+      speed = fsq(m2 * r * r) + fsq(fdv(gamma * p * r, 1.0f - s[0] * b));
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      const float ud = s[1 + d] * r;
+      F[0][d] = s[1 + d];
+#pragma unroll
+      for (int i = 0; i < DIM; i++) F[1 + i][d] = s[1 + i] * ud;
+      F[1 + d][d] += p;
+      F[1 + DIM][d] = (s[1 + DIM] + p) * ud;
+    }
+    return speed;
+  }
   const R den = s[0];
   const R inv = fdv(R(1), den);
   R v2 = R(0);
@@ -246,6 +328,9 @@ template <int DIM, typename R>
 __device__ __forceinline__ R riemann(R* s1, R* s2, const R* n, R* flux, R gamma, R b, int rs,
                                      int avg) {
   constexpr int NEQ = DIM + 2;
+  if constexpr (std::is_same<R, float>::value) {
+    if (rs == 0) return rusanov_f32<DIM>(s1, s2, n, flux, gamma, b);
+  }
   if (!state_is_physical_say<DIM>(s1, gamma)) return R(-1);
   if (!state_is_physical_say<DIM>(s2, gamma)) return R(-1);
   if (rs == 0) {

@@ -24,6 +24,12 @@ def _ctx(bc, prec=FP64):
 
 @pytest.mark.parametrize("use_graph", [True, False])
 def test_batch_matches_per_problem_oracle(cuda, use_graph):
+    """Each problem of the batch is bit-identical to the same problem run
+    alone in its own context, and close to its own oracle run.  Limited
+    Riemann problems cross the indicator's hard thresholds (the +-1e-3
+    switches of indicator_bj.cpp:49-51) at slightly different times under
+    different rounding, so GPU and oracle part by ~1e-10 over the run (dt by ~1e-8);
+    the oracle itself does not move under a 1e-15 input perturbation."""
     bc = _batch()
     ctx = _ctx(bc)
     x0 = bc.project(ctx.node_coords())
@@ -43,18 +49,18 @@ def test_batch_matches_per_problem_oracle(cuda, use_graph):
             assert info["steps"][p] < 0, p
             nfail += 1
             continue
-        rng = np.random.default_rng(p)
-        xs, _ = orc.run(xp0 * (1 + 1e-15 * rng.uniform(-1, 1, xp0.size)), c.t_end, c.cfl)
-        assert info["steps"][p] == ir["steps"], p
-        # t books the CFL dt of each step, which follows the (round-off
-        # amplifying) limited solution
-        assert info["t"][p] == pytest.approx(ir["t"], rel=1e-6)
         e0, e1 = bc.offsets[p], bc.offsets[p + 1]
-        rho = x[0, e0 * nd:e1 * nd]
-        d_gpu = rel_l1(rho, xr[:orc.ndofs])
-        d_self = rel_l1(xs[:orc.ndofs], xr[:orc.ndofs])
-        # limited runs amplify round-off (see test_full_run_sod)
-        assert d_gpu < 1e-3 and d_gpu < max(10 * d_self, 1e-10), (p, d_gpu, d_self)
+        xb = x[:, e0 * nd:e1 * nd]
+        single = Context(c.mesh, c.order, device=0, precision=FP64)
+        cases.configure_context(c, single)
+        xs = torch.tensor(cases.project(c, single.node_coords()), dtype=torch.float64, device="cuda")
+        isg = single.run(xs, c.t_end, c.cfl)
+        assert info["steps"][p] == isg["steps"] == ir["steps"], p
+        assert info["t"][p] == isg["t"], p
+        assert np.array_equal(xb, xs.cpu().numpy().reshape(4, -1)), p
+        assert info["t"][p] == pytest.approx(ir["t"], rel=1e-7)
+        d_gpu = rel_l1(xb[0], xr[:orc.ndofs])
+        assert d_gpu < 1e-8, (p, d_gpu)
     assert nfail < len(bc.cases)
 
 
