@@ -50,6 +50,13 @@ def workload_config(case, n_elem_side):
     }
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element per
+# stage launch of k_rhs_hex_team<2,float>: mean of the three stage launches of
+# one RK step captured with ncu on the 48^3 pulse (330.0 MB / 110,592
+# elements); traffic scales with the element count.
+TRAFFIC_BYTES_PER_ELEMENT_LAUNCH = 2984.0
+
+
 def algorithmic_bytes_per_step(N, ne, precision):
     """Bytes one SSP-RK3 step must move at stored widths:
     FP32-bulk: stage 0 reads x_hi, x_lo, writes k0, y1 (16N); stage 1 reads
@@ -203,6 +210,9 @@ def run_ours(args, rank, world, local):
         ctx = Context(case.mesh, case.order, device=local, precision=prec)
         cases.configure_context(case, ctx)
         ctx.set_stream(stream.cuda_stream)
+        if args.hex_kernel and prec == FP32_BULK:
+            from rkdg3d_gb300.solver import TUNE_HEX_KERNEL
+            ctx.set_tuning(TUNE_HEX_KERNEL, args.hex_kernel)
         return ctx
 
     ctx32 = make(FP32_BULK)
@@ -261,21 +271,31 @@ def run_ours(args, rank, world, local):
     }
     del ctx64
 
-    # end to end through the C ABI from pinned host memory
+    # end to end through the C ABI with host buffers: every step uploads the
+    # state from pinned host memory, runs one rkdg_step (ExplicitRKLimitedSolver
+    # ::Step) and reads the state back, as a drop-in Step() on host vectors does
     xh = torch.tensor(x0, dtype=torch.float64).pin_memory()
-    out = torch.empty_like(xh).pin_memory()
     xd = torch.empty(N, dtype=torch.float64, device=dev)
+    for _ in range(min(args.warmup, 3)):
+        xd.copy_(xh, non_blocking=True)
+        ctx32.step(xd, dt)
+        xh.copy_(xd, non_blocking=True)
+    xh.copy_(torch.from_numpy(x0))
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    xd.copy_(xh, non_blocking=True)
-    ctx32.run(xd, 1e30, dt0=dt, dt_mode=2, max_steps=args.steps)
-    out.copy_(xd, non_blocking=True)
+    for _ in range(args.steps):
+        xd.copy_(xh, non_blocking=True)
+        ctx32.step(xd, dt)
+        xh.copy_(xd, non_blocking=True)
     torch.cuda.synchronize(dev)
     sec_e2e = barrier_max(time.perf_counter() - t0, world)
     e2e = {"value": world * N * STAGES * args.steps / sec_e2e, "unit": UNIT,
-           "h2d_bytes_per_step": 8 * N / args.steps, "d2h_bytes_per_step": 8 * N / args.steps,
-           "note": "state uploaded once and downloaded once per job of `steps` RK steps; "
-                   "call = rkdg_run through the ctypes C ABI"}
+           "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
+           "note": "per step: pinned host -> device copy of the FP64 state, rkdg_step through "
+                   "the ctypes C ABI, device -> pinned host copy of the state"}
 
     peaks = {}
     try:
@@ -289,8 +309,11 @@ def run_ours(args, rank, world, local):
     ms_step = 1e3 * sec32 / args.steps
     achieved = bps / (ms_step / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": args.traffic_per_launch,
-            "peak_source": peak_src, "kernel": "k_rhs_hex_sf (stage kernel)",
+            "frac": achieved / peak,
+            "traffic": args.traffic_per_launch or TRAFFIC_BYTES_PER_ELEMENT_LAUNCH * ctx32.ne,
+            "traffic_source": "ncu dram bytes, 48^3 capture scaled by elements"
+                              if not args.traffic_per_launch else "command line",
+            "peak_source": peak_src, "kernel": "k_rhs_hex_team<2,float> (stage kernel, 3 launches per step)",
             "algorithmic_bytes_per_launch": bps / STAGES}
 
     cpu = None
@@ -329,12 +352,15 @@ def run_ours(args, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=64, help="elements per side")
-    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--fp64-steps", type=int, default=500,
+                    help="steps of the plain FP64 run (timed, and the accuracy reference)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--hex-kernel", type=int, default=0,
+                    help="RKDG_TUNE_HEX_KERNEL of the FP32-bulk context (0: library default)")
     ap.add_argument("--traffic-per-launch", type=float, default=None,
                     help="DRAM bytes per stage launch from an ncu capture (profiles/)")
     args = ap.parse_args()

@@ -111,11 +111,25 @@ int rkdg_set_limiter(rkdg_ctx* ctx, int limiter, int indicator, int function,
 int rkdg_set_tableau(rkdg_ctx* ctx, int s, const double* a, const double* b,
                      const double* c);
 int rkdg_set_precision(rkdg_ctx* ctx, int precision);
-/* Kernel tuning knobs (no counterpart in the reference; used by the
- * autotuner).  RKDG_TUNE_HEX_KERNEL: 0 default, 1 warp per element,
- * 2 five-lane team per element (hexahedra). */
-enum { RKDG_TUNE_HEX_KERNEL = 1 };
+/* Kernel tuning knobs (no counterpart in the reference; set by hand or by
+ * rkdg_autotune).  RKDG_TUNE_HEX_KERNEL: 0 default, 1 warp per element,
+ * 2 five-lane team per element, 3 five-lane team face pass (each face once,
+ * into per-element flux slots the context allocates) + element pass
+ * (hexahedra).  RKDG_TUNE_GENERIC_BLOCK /
+ * RKDG_TUNE_LIMITER_BLOCK: elements (threads) per CTA of the triangle/quad
+ * right-hand-side kernel and of the limiter, 0 (default 128) or a multiple of
+ * 32 up to 256. */
+enum { RKDG_TUNE_HEX_KERNEL = 1, RKDG_TUNE_GENERIC_BLOCK = 2, RKDG_TUNE_LIMITER_BLOCK = 3 };
 int rkdg_set_tuning(rkdg_ctx* ctx, int key, int value);
+/* Autotuner (no counterpart in the reference): times each candidate launch
+ * shape of the stage kernel, and of the limiter when one is set, on the state
+ * x_dev and keeps the fastest for this context (mesh, order and precision as
+ * set now).  Outputs (each may be NULL) receive the chosen
+ * RKDG_TUNE_HEX_KERNEL, RKDG_TUNE_GENERIC_BLOCK and RKDG_TUNE_LIMITER_BLOCK.
+ * Results do not depend on the choice beyond rounding of the hexahedral
+ * kernels' summation order. */
+int rkdg_autotune(rkdg_ctx* ctx, const double* x_dev, int* hex_kernel, int* generic_block,
+                  int* limiter_block);
 
 /* ---- queries ------------------------------------------------------------ */
 /* NDofs (scalar nodes), nodes per element, number of equations. */

@@ -53,6 +53,7 @@ _SIGS = [
     ("rkdg_adjoint_run", C.c_int, [_vp, _vp, C.c_int, C.c_double, C.c_int, _vp, _vp]),
     ("rkdg_kernel_launches", C.c_longlong, [_vp]),
     ("rkdg_limit_static", C.c_int, [_vp, _vp]),
+    ("rkdg_autotune", C.c_int, [_vp, _vp, _ip, _ip, _ip]),
 ]
 
 EXPORTED = [s[0] for s in _SIGS]

@@ -107,6 +107,38 @@ def pulse3d(n=64, order=2, steps=500, cfl=0.2) -> Case:
                 dt_mode=1, max_steps=steps, ic=ic)
 
 
+def gaussian_pulses(n=32, order=1, seed=0, steps=200, cfl=0.2, npulse=8) -> Case:
+    """3D periodic box [0,1]^3 on an n^3 hex mesh with
+    rho = 1 + sum_i a_i exp(-d_i^2 / w_i^2), p = rho^gamma, u = 0, where d_i is
+    the periodic (minimum-image) distance to centre c_i; a_i ~ U[0.005, 0.02],
+    w_i ~ U[0.03, 0.08], c_i ~ U[0,1]^3, drawn from
+    numpy.random.default_rng(seed) in the order a, w, c.  HLLC + TRRS,
+    Multi limiter with the Venkatakrishnan indicator function, SSP-RK3 with
+    dt fixed from CFL at t = 0, `steps` steps (the adjoint workload)."""
+    rng = np.random.default_rng(seed)
+    amp = rng.uniform(0.005, 0.02, npulse)
+    wid = rng.uniform(0.03, 0.08, npulse)
+    cen = rng.uniform(0.0, 1.0, (npulse, 3))
+    mesh = M.hex_grid(n, n, n)
+    gamma = 1.4
+
+    def ic(x):
+        rho = np.ones_like(x[0])
+        for a, w, c in zip(amp, wid, cen):
+            d2 = np.zeros_like(x[0])
+            for k in range(3):
+                dk = np.abs(x[k] - c[k])
+                dk = np.minimum(dk, 1.0 - dk)
+                d2 += dk * dk
+            rho += a * np.exp(-d2 / (w * w))
+        z = np.zeros_like(rho)
+        return rho, z, z, z, rho ** gamma
+
+    return Case(f"gaussian_pulses{seed}", mesh, order, RS_HLLC, AVG_TRRS, gamma=gamma,
+                limiter=(LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN, 1, 0), tableau=TABLEAU_SSPRK3,
+                t_end=1e30, cfl=cfl, dt_mode=1, max_steps=steps, ic=ic)
+
+
 def double_mach(nx=1024, ny=256, order=1, jitter=0.2, seed=0, t_end=0.2, cfl=0.25) -> Case:
     """Double Mach reflection on [0,4]x[0,1]: jittered triangulation of an
     nx x ny grid; Mach-10 shock at 60 degrees through (1/6, 0); pre-shock

@@ -10,6 +10,7 @@
 #define RKDG_MAX_NQL 4    // limiter face rule (order 2): 2 (segment) or 2x2
 #define RKDG_MAX_NV 8
 #define RKDG_MAX_PERM 64
+#define RKDG_HEX_MAX_PERM 8  // orientations of a square face
 #define RKDG_MAX_BC 32
 
 namespace rkdg {
@@ -99,6 +100,8 @@ struct RhsParams {
   const int* pactive;
   unsigned long long* pmcs;
   int* pfail;           // per-problem failure flag (non-physical state)
+  int block;            // threads per CTA of the generic kernels (0: default)
+  void* fslot;          // hexahedral face-pass flux slots [ne][6][neq][nqf] (or null)
 };
 
 // Stage epilogue.
@@ -147,6 +150,7 @@ struct LimParams {
   const double* pgamma;
   const double* pcov;
   const int* pactive;
+  int block;            // threads per CTA (0: default)
 };
 
 // Device-side time control of batched problems (one entry per problem).

@@ -25,21 +25,38 @@ static cudaError_t launch_hex_sf(const RhsParams& prm, const R* u, const EpiPara
   return cudaGetLastError();
 }
 
-template <int P, typename R>
-static cudaError_t launch_hex_team(const RhsParams& prm, const R* u, const EpiParams<R>& ep,
-                                   cudaStream_t st) {
+template <int P, typename R, int MODE>
+static cudaError_t launch_hex_team_mode(const RhsParams& prm, const R* u, const EpiParams<R>& ep,
+                                        cudaStream_t st) {
   using S = TeamSize<P>;
-  const size_t smem = S::template smem_bytes<R>();
+  const size_t smem = S::template smem_bytes<R, MODE>();
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_rhs_hex_team<P, R>,
+    cudaError_t e = cudaFuncSetAttribute(k_rhs_hex_team<P, R, MODE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured = true;
   }
   const int grid = (prm.ne + S::EPB - 1) / S::EPB;
-  k_rhs_hex_team<P, R><<<grid, S::THREADS, smem, st>>>(prm, u, ep);
+  k_rhs_hex_team<P, R, MODE><<<grid, S::THREADS, smem, st>>>(prm, u, ep);
   return cudaGetLastError();
+}
+
+template <int P, typename R>
+static cudaError_t launch_hex_team(const RhsParams& prm, const R* u, const EpiParams<R>& ep,
+                                   cudaStream_t st) {
+  return launch_hex_team_mode<P, R, 0>(prm, u, ep, st);
+}
+
+// Face pass then element pass (each face evaluated once); falls back to the
+// fused kernel without a slot buffer and for the face-only evaluation.
+template <int P, typename R>
+static cudaError_t launch_hex_split(const RhsParams& prm, const R* u, const EpiParams<R>& ep,
+                                    cudaStream_t st) {
+  if (!prm.fslot || prm.faces_only) return launch_hex_team_mode<P, R, 0>(prm, u, ep, st);
+  cudaError_t e = launch_hex_team_mode<P, R, 1>(prm, u, ep, st);
+  if (e != cudaSuccess) return e;
+  return launch_hex_team_mode<P, R, 2>(prm, u, ep, st);
 }
 
 template <>
@@ -64,10 +81,18 @@ template cudaError_t launch_means_t<5, 1>(int, int, long long, const RefTables*,
 template cudaError_t launch_means_t<5, 2>(int, int, long long, const RefTables*, const void*,
                                           const float*, double*, cudaStream_t);
 
-// Both hexahedral right-hand-side kernels, selectable for tests (0 = default
-// choice above, 1 = warp-per-element sum factorisation, 2 = team kernel).
+// The hexahedral right-hand-side kernels, selectable for tests and the
+// autotuner (0 = default choice above, 1 = warp-per-element sum
+// factorisation, 2 = team kernel, 3 = face pass + element pass).
 cudaError_t launch_hex_variant(int variant, int p, int prec, const RhsParams& prm, const void* u,
                                const void* ep, cudaStream_t st) {
+  if (variant == 3) {
+    if (p == 1)
+      return prec == 0 ? launch_hex_split<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)
+                       : launch_hex_split<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+    return prec == 0 ? launch_hex_split<2, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)
+                     : launch_hex_split<2, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+  }
   if (variant == 1) {
     if (p == 1)
       return prec == 0 ? launch_hex_sf<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)

@@ -17,6 +17,9 @@
 
 namespace rkdg {
 
+// Largest CTA the generic (thread-per-element) kernels are launched with.
+constexpr int kGenericMaxBlock = 256;
+
 // ---- double-single (float pair) helpers for the FP32-bulk path --------------
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
@@ -188,7 +191,7 @@ __device__ __forceinline__ void epilogue(const EpiParams<R>& ep, long long base_
 
 // ---- right-hand side --------------------------------------------------------
 template <int G, int P, typename R>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kGenericMaxBlock)
     k_rhs_generic(const RhsParams prm, const R* __restrict__ u, const EpiParams<R> ep) {
   using E = El<G, P>;
   constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NFPE = E::NFPE, NQF = E::NQF;
@@ -351,7 +354,7 @@ __global__ void __launch_bounds__(128)
 // done in place.  DS = true: the values are a float pair (u = hi, ulo = lo)
 // and the multiplier update runs in double-single arithmetic.
 template <int G, int P, typename R, bool DS>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kGenericMaxBlock)
     k_limit_generic(const LimParams prm, R* __restrict__ u, float* __restrict__ ulo) {
   using E = El<G, P>;
   constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NFPE = E::NFPE, NQL = E::NQL, NV = E::NV;

@@ -36,16 +36,30 @@ struct TeamSize {
   // 32-word rows; team t of a warp starts xoff(t) words into its row so that
   // the team-parallel stores (30 lanes) and the warp-parallel flux reads (two
   // teams of 16 points) fall in distinct banks
+  // MODE 0 (fused right-hand side) needs both; MODE 1 (face pass) the two
+  // traces only; MODE 2 (element pass) the volume fluxes only.
   static constexpr int XF = 3 * NEQ * NQF, XV = 3 * NEQ * ND;
-  static constexpr int XCH = XF > XV ? XF : XV;
-  static constexpr int XSTR = (XCH + 31) & ~31;
-  static constexpr int WSTR = TPW * XSTR + 32;
+  template <int MODE>
+  __host__ __device__ static constexpr int xch() {
+    return MODE == 1 ? 2 * NEQ * NQF : (MODE == 2 ? XV : (XF > XV ? XF : XV));
+  }
+  // row stride: a multiple of 32 words with room for the offsets (team t + 1
+  // may start up to 11 words earlier within its row than team t)
+  template <int MODE>
+  __host__ __device__ static constexpr int xstr() { return (xch<MODE>() + 11 + 31) & ~31; }
+  template <int MODE>
+  __host__ __device__ static constexpr int wstr() { return TPW * xstr<MODE>() + 32; }
   static constexpr int TAB = NQ1 * N1 + 2 * N1 + 2 * N1 * N1 + N1 + NQF;
   static constexpr int TAB_AL = (TAB + 3) & ~3;
   __host__ __device__ static constexpr int xoff(int t) { return 16 * (t & 1) + 5 * (t >> 1); }
-  template <typename R>
+  template <typename R, int MODE>
   static constexpr size_t smem_bytes() {
-    return sizeof(R) * (size_t)(TAB_AL + EPB * NEQ * ND + WARPS * WSTR);
+    return sizeof(R) * (size_t)(TAB_AL + EPB * NEQ * ND + WARPS * wstr<MODE>());
+  }
+  // resident CTAs per SM the register allocation is bounded for
+  template <typename R, int MODE>
+  __host__ __device__ static constexpr int min_ctas() {
+    return sizeof(R) == 4 ? (MODE == 1 ? 5 : 4) : 2;
   }
 };
 
@@ -159,6 +173,34 @@ __device__ __forceinline__ void team_lift(const R* f, const R* l1d, const R* len
     }
 }
 
+// Same contraction reading the element's staged values from shared memory.
+template <int P, int LF, typename R>
+__device__ __forceinline__ void team_contract_s(const R* su, const R* lend, R (&v)[(P + 1) * (P + 1)]) {
+  constexpr int N1 = P + 1, NAX = hex_face_axis(LF), SD = hex_face_side(LF);
+#pragma unroll
+  for (int i0 = 0; i0 < N1; ++i0)
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1) {
+      R s = R(0);
+#pragma unroll
+      for (int jn = 0; jn < N1; ++jn) s += lend[SD * N1 + jn] * su[hnode<N1>(NAX, jn, i0, i1)];
+      v[i0 * N1 + i1] = s;
+    }
+}
+
+template <int P, typename R>
+__device__ __forceinline__ void team_contract_s_any(int lf, const R* su, const R* lend,
+                                                    R (&v)[(P + 1) * (P + 1)]) {
+  switch (lf) {
+    case 0: team_contract_s<P, 0>(su, lend, v); break;
+    case 1: team_contract_s<P, 1>(su, lend, v); break;
+    case 2: team_contract_s<P, 2>(su, lend, v); break;
+    case 3: team_contract_s<P, 3>(su, lend, v); break;
+    case 4: team_contract_s<P, 4>(su, lend, v); break;
+    default: team_contract_s<P, 5>(su, lend, v); break;
+  }
+}
+
 template <int P, typename R>
 __device__ __forceinline__ void team_contract_any(int lf, const R (&u)[(P + 1) * (P + 1) * (P + 1)],
                                                   const R* lend, R (&v)[(P + 1) * (P + 1)]) {
@@ -187,13 +229,13 @@ __device__ __forceinline__ void team_lift_any(int lf, const R* f, const R* l1d, 
 
 // Phase 1 of one face (runtime index LF) for the team's variable k: the own
 // trace and, across an interior face, the neighbour's trace at the face
-// points, stored point-major (To[q*NEQ + k], Tn[q*NEQ + k]).  The register
-// arrays need compile-time indices only in the own-side contraction (a small
-// switch); the neighbour's values come from the staged tile when it is there,
-// else from global memory, through a node table.
+// points, stored point-major (To[q*NEQ + k], Tn[q*NEQ + k]).  The own values
+// are read from the staged tile su (compile-time offsets, a small switch over
+// the face); the neighbour's values come from the staged tile when it is
+// there, else from global memory, through a node table.
 template <int P, typename R>
 __device__ __forceinline__ void team_traces(const int LF, const R* __restrict__ ug, long long NDa,
-                                            int k, const R (&u)[(P + 1) * (P + 1) * (P + 1)], R* xch,
+                                            int k, const R* su, R* xch,
                                             const R* l1d, const R* lend,
                                             const unsigned char (*nodet)[(P + 1) * (P + 1) * (P + 1)],
                                             int nb, int code, const R* sU, int e0, int nel) {
@@ -218,7 +260,7 @@ __device__ __forceinline__ void team_traces(const int LF, const R* __restrict__ 
   }
   {
     R v[N1 * N1];
-    team_contract_any<P>(LF, u, lend, v);
+    team_contract_s_any<P>(LF, su, lend, v);
     team_interp<P, NEQ>(v, l1d, To + k);
   }
   if (nb >= 0) {
@@ -239,17 +281,20 @@ __device__ __forceinline__ void team_traces(const int LF, const R* __restrict__ 
 // elements, spread over the 32 lanes (point pt of the warp = team pt / NQF,
 // point pt % NQF); arguments in Elem1, Elem2 order with the Elem1-outward
 // normal (face_integrator.cpp:11-276), boundary faces through the boundary
-// condition's right state.  Writes sign * w_q * |J_f| * Fhat to the team's
-// Fh[q*NEQ + k] in its own tensor order.
-template <int P, typename R>
+// condition's right state.  MODE 0 writes sign * w_q * |J_f| * Fhat to the
+// team's Fh[q*NEQ + k] in its own tensor order.  MODE 1 (face pass) handles
+// only the faces the element owns (Elem1 of an interior face, or a boundary
+// face) and writes the value into the flux slots of both elements
+// (prm.fslot[element][local face][k][tensor point]) with each side's sign.
+template <int P, typename R, int MODE>
 __device__ __forceinline__ void warp_fluxes(const int LF, const RhsParams& prm, int lane, int wel0,
                                             int nel, R* wx, const R* wf,
                                             const unsigned char (*perm)[(P + 2) * (P + 2)],
-                                            const int (*fab)[RKDG_MAX_NQF], const int (*sfnb)[6],
-                                            const int (*sfcd)[6], const R (*sgeo)[6][4], int e0,
-                                            R gamma, R cov, R& lmax) {
+                                            const unsigned char (*fab)[(P + 2) * (P + 2)],
+                                            const int (*sfnb)[6], const unsigned char (*sfcd)[6],
+                                            int e0, R gamma, R cov, R& lmax) {
   using S = TeamSize<P>;
-  constexpr int NQF = S::NQF, NEQ = S::NEQ, TPW = S::TPW;
+  constexpr int NQF = S::NQF, NEQ = S::NEQ, TPW = S::TPW, XSTR = S::template xstr<MODE>();
 #pragma unroll 1
   for (int pt = lane; pt < TPW * NQF; pt += 32) {
     const int t = pt / NQF, q = pt - t * NQF;
@@ -258,16 +303,18 @@ __device__ __forceinline__ void warp_fluxes(const int LF, const RhsParams& prm, 
     const int nb = sfnb[el][LF];
     if (nb == -1) continue;
     const int code = sfcd[el][LF];
-    R* To = wx + t * S::XSTR + S::xoff(t);
+    const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
+    if (MODE == 1 && side) continue;  // the face's Elem1 evaluates it
+    R* To = wx + t * XSTR + S::xoff(t);
     const R* Tn = To + NEQ * NQF;
     R* Fh = To + 2 * NEQ * NQF;
-    const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
+    const R* fg = (const R*)prm.fgeo + (long long)(LF * 4) * prm.ne + e0 + el;
     R n[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) n[c] = sgeo[el][LF][c];
-    const R jac = sgeo[el][LF][3];
+    for (int c = 0; c < 3; ++c) n[c] = __ldg(fg + (long long)c * prm.ne);
+    const R jac = __ldg(fg + 3LL * prm.ne);
     R s1[NEQ], s2[NEQ];
-    int own = fab[LF][q];
+    int own = fab[LF][q], other = 0;
     if (nb >= 0) {
       const int q2 = perm[pid][q];
       const int a1 = side ? fab[lfo][q] : fab[LF][q];
@@ -280,6 +327,7 @@ __device__ __forceinline__ void warp_fluxes(const int LF, const RhsParams& prm, 
         s2[kk] = T2[a2 * NEQ + kk];
       }
       if (side) own = a2;
+      other = a2;
     } else {
 #pragma unroll
       for (int kk = 0; kk < NEQ; ++kk) s1[kk] = To[own * NEQ + kk];
@@ -289,20 +337,39 @@ __device__ __forceinline__ void warp_fluxes(const int LF, const RhsParams& prm, 
     R F[NEQ];
     const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e0 + el);
     lmax = fmax(lmax, sp);
-    const R w = (side ? R(1) : R(-1)) * wf[q] * jac;
+    if constexpr (MODE == 1) {
+      R* fs = (R*)prm.fslot;
+      const R w = wf[q] * jac;
+      R* so = fs + ((long long)(e0 + el) * 6 + LF) * (NEQ * NQF) + own;
 #pragma unroll
-    for (int kk = 0; kk < NEQ; ++kk) Fh[own * NEQ + kk] = w * F[kk];
+      for (int kk = 0; kk < NEQ; ++kk) so[kk * NQF] = -w * F[kk];
+      if (nb >= 0) {
+        R* sn = fs + ((long long)nb * 6 + lfo) * (NEQ * NQF) + other;
+#pragma unroll
+        for (int kk = 0; kk < NEQ; ++kk) sn[kk * NQF] = w * F[kk];
+      }
+    } else {
+      const R w = (side ? R(1) : R(-1)) * wf[q] * jac;
+#pragma unroll
+      for (int kk = 0; kk < NEQ; ++kk) Fh[own * NEQ + kk] = w * F[kk];
+    }
   }
 }
 
-template <int P, typename R>
-__global__ void __launch_bounds__(128)
+// MODE 0: the whole right-hand side of the CTA's elements (every face
+// evaluated by both its elements).  MODE 1 + MODE 2 (two launches): a face pass
+// that evaluates each face once into per-element flux slots, then an element
+// pass that lifts the six slots and adds the volume term, inverse mass and
+// Runge-Kutta epilogue.
+template <int P, typename R, int MODE>
+__global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>())
     k_rhs_hex_team(const RhsParams prm, const R* __restrict__ u, const EpiParams<R> ep) {
   using S = TeamSize<P>;
   constexpr int N1 = S::N1, NQ1 = S::NQ1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, EPB = S::EPB;
+  constexpr int XSTR = S::template xstr<MODE>(), WSTR = S::template wstr<MODE>();
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ unsigned char sPerm[RKDG_MAX_PERM][NQF];
-  __shared__ int sFab[6][RKDG_MAX_NQF];
+  __shared__ unsigned char sPerm[RKDG_HEX_MAX_PERM][NQF];
+  __shared__ unsigned char sFab[6][NQF];
   __shared__ unsigned char sNodeT[6][ND];  // node of (face, i0*N1+i1, jn)
   R* sm = reinterpret_cast<R*>(smraw);
   R* tL1 = sm;                  // [NQ1][N1]
@@ -323,8 +390,9 @@ __global__ void __launch_bounds__(128)
   }
   for (int t = tid; t < N1; t += blockDim.x) tW1[t] = (R)T->w1[t];
   for (int t = tid; t < NQF; t += blockDim.x) tWf[t] = (R)T->wf[t];
-  for (int t = tid; t < T->nperm * NQF; t += blockDim.x) sPerm[t / NQF][t % NQF] = (unsigned char)T->perm[t / NQF][t % NQF];
-  for (int t = tid; t < 6 * NQF; t += blockDim.x) sFab[t / NQF][t % NQF] = T->fab[t / NQF][t % NQF];
+  for (int t = tid; t < min(T->nperm, RKDG_HEX_MAX_PERM) * NQF; t += blockDim.x)
+    sPerm[t / NQF][t % NQF] = (unsigned char)T->perm[t / NQF][t % NQF];
+  for (int t = tid; t < 6 * NQF; t += blockDim.x) sFab[t / NQF][t % NQF] = (unsigned char)T->fab[t / NQF][t % NQF];
   for (int t = tid; t < 6 * ND; t += blockDim.x) {
     const int lf = t / ND, r = (t % ND) / N1, jn = t % N1;
     sNodeT[lf][t % ND] = (unsigned char)hnode<N1>(hex_face_axis(lf), jn, r / N1, r % N1);
@@ -334,19 +402,12 @@ __global__ void __launch_bounds__(128)
   const long long NDa = prm.ndofs;
   const int e0 = blockIdx.x * EPB;
   const int nel = min(EPB, ne - e0);
-  __shared__ int sFnb[EPB][6], sFcd[EPB][6];
-  __shared__ R sGeo[EPB][6][4];  // unit normal and |J_f| per (element, face)
-  {
-    const R* fg = (const R*)prm.fgeo;
-    for (int t = tid; t < nel * 6; t += blockDim.x) {
-      const int lf = t / nel, el = t % nel;
-      sFnb[el][lf] = prm.fnbr[lf * ne + e0 + el];
-      sFcd[el][lf] = prm.fcode[lf * ne + e0 + el];
-    }
-    for (int t = tid; t < nel * 24; t += blockDim.x) {
-      const int c = t / nel, el = t % nel;  // c = lf * 4 + component
-      sGeo[el][c >> 2][c & 3] = fg[(long long)c * ne + e0 + el];
-    }
+  __shared__ int sFnb[EPB][6];
+  __shared__ unsigned char sFcd[EPB][6];  // pid << 4 | side << 3 | other local face
+  for (int t = tid; t < nel * 6; t += blockDim.x) {
+    const int lf = t / nel, el = t % nel;
+    sFnb[el][lf] = prm.fnbr[lf * ne + e0 + el];
+    sFcd[el][lf] = (unsigned char)prm.fcode[lf * ne + e0 + el];
   }
   for (int k = 0; k < NEQ; ++k)
     for (int t = tid; t < nel * ND; t += blockDim.x)
@@ -365,29 +426,44 @@ __global__ void __launch_bounds__(128)
   const int e = e0 + el;
   const int k = tl;
   const int wel0 = warp * S::TPW;
-  R* wx = sX + warp * S::WSTR;
-  R* xch = wx + (team < S::TPW ? team * S::XSTR + S::xoff(team) : 0);
-  R uv[ND], acc[ND];
-  if (act) {
+  R* wx = sX + warp * WSTR;
+  R* xch = wx + (team < S::TPW ? team * XSTR + S::xoff(team) : 0);
+  const R* su = sU + (el * NEQ + k) * ND;  // this lane's staged values
+  R acc[ND];
 #pragma unroll
-    for (int i = 0; i < ND; ++i) {
-      uv[i] = sU[(el * NEQ + k) * ND + i];
-      acc[i] = R(0);
-    }
-  }
-  // the warp steps through the six faces together: traces per team, the
-  // numerical fluxes over all 32 lanes, the lifting per team again
+  for (int i = 0; i < ND; ++i) acc[i] = R(0);
+  if constexpr (MODE != 2) {
+    // the warp steps through the six faces together: traces per team, the
+    // numerical fluxes over all 32 lanes, the lifting per team again (MODE 0)
 #pragma unroll 1
-  for (int lf = 0; lf < 6; ++lf) {
-    const int nb = act ? sFnb[el][lf] : -1;
-    if (nb != -1)
-      team_traces<P, R>(lf, u, NDa, k, uv, xch, tL1, tLend, sNodeT, nb, sFcd[el][lf], sU, e0, nel);
-    __syncwarp();
-    warp_fluxes<P, R>(lf, prm, lane, wel0, nel, wx, tWf, sPerm, sFab, sFnb, sFcd, sGeo, e0, gamma,
-                      cov, lmax);
-    __syncwarp();
-    if (nb != -1 && !prm.faces_only)
-      team_lift_any<P, NEQ>(lf, xch + 2 * NEQ * NQF + k, tL1, tLend, acc);
+    for (int lf = 0; lf < 6; ++lf) {
+      const int nb = act ? sFnb[el][lf] : -1;
+      const bool mine = nb != -1 && (MODE == 0 || ((sFcd[el][lf] >> 3) & 1) == 0);
+      if (MODE == 1 && !__any_sync(0xffffffffu, mine)) continue;
+      if (mine)
+        team_traces<P, R>(lf, u, NDa, k, su, xch, tL1, tLend, sNodeT, nb, sFcd[el][lf], sU, e0, nel);
+      __syncwarp();
+      warp_fluxes<P, R, MODE>(lf, prm, lane, wel0, nel, wx, tWf, sPerm, sFab, sFnb, sFcd, e0, gamma,
+                              cov, lmax);
+      __syncwarp();
+      if (MODE == 0 && nb != -1 && !prm.faces_only)
+        team_lift_any<P, NEQ>(lf, xch + 2 * NEQ * NQF + k, tL1, tLend, acc);
+    }
+    if constexpr (MODE == 1) {
+      block_max_commit<R>(lmax, prm.mcs);
+      return;
+    }
+  } else if (act) {
+    // lift the six flux slots the face pass wrote for this element
+    const R* fs = (const R*)prm.fslot + (long long)e * 6 * (NEQ * NQF) + k * NQF;
+#pragma unroll 1
+    for (int lf = 0; lf < 6; ++lf) {
+      if (sFnb[el][lf] == -1) continue;
+      R fv[NQF];
+#pragma unroll
+      for (int q = 0; q < NQF; ++q) fv[q] = __ldg(fs + lf * (NEQ * NQF) + q);
+      team_lift_any<P, 1>(lf, fv, tL1, tLend, acc);
+    }
   }
   // neighbours inside the tile were read from the staged DOFs, which the
   // volume phase below overwrites with the result

@@ -45,6 +45,10 @@ struct rkdg_ctx {
   std::vector<double> a{1.0, 0.25, 0.25}, b{1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0}, c{1.0, 0.5};
   int precision = RKDG_FP64;
   int hex_variant = 0;  // RKDG_TUNE_HEX_KERNEL
+  int gen_block = 0;    // RKDG_TUNE_GENERIC_BLOCK
+  double* d_fslot = nullptr;  // face-pass flux slots (split hexahedral variant)
+  size_t fslot_n = 0;
+  int lim_block = 0;    // RKDG_TUNE_LIMITER_BLOCK
   int solver_quirks = 0;
   // mesh (host copies)
   bool has_mesh = false;
@@ -163,6 +167,8 @@ void free_mesh(rkdg_ctx* c) {
   dfree(c->d_pmcs);
   dfree(c->d_adj);
   c->adj_n = 0;
+  dfree(c->d_fslot);
+  c->fslot_n = 0;
   c->nprob = 0;
   c->has_mesh = false;
 }
@@ -249,7 +255,28 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   for (auto& kv : c->bcs) P.bc[k++] = kv.second;
   P.mcs = c->d_mcs + slot;
   P.err = c->d_err;
+  P.block = c->gen_block;
+  P.fslot = c->d_fslot;
   return P;
+}
+
+// Kernels one right-hand-side launch issues (the split hexahedral variant
+// runs a face pass and an element pass).
+int rhs_kernels(const rkdg_ctx* c, const RhsParams& P) {
+  return (c->geom == RKDG_GEOM_CUBE && c->hex_variant == 3 && P.fslot && !P.faces_only) ? 2 : 1;
+}
+
+// Flux slots of the split hexahedral variant: [ne][6][neq][nqf] values of
+// the widest precision.
+int ensure_fslot(rkdg_ctx* c) {
+  if (c->geom != RKDG_GEOM_CUBE) return RKDG_OK;
+  const size_t n = (size_t)c->ne * 6 * c->neq * c->tab.nqf;
+  if (c->d_fslot && c->fslot_n == n) return RKDG_OK;
+  dfree(c->d_fslot);
+  c->fslot_n = 0;
+  CUDA_TRY(c, dalloc(c->d_fslot, n));
+  c->fslot_n = n;
+  return RKDG_OK;
 }
 
 void set_batch(rkdg_ctx* c, RhsParams& P, int slot) {
@@ -276,6 +303,7 @@ LimParams lim_params(rkdg_ctx* c) {
   L.function = c->fun;
   L.last_hope = c->last_hope;
   L.quirks = c->quirks;
+  L.block = c->lim_block;
   return L;
 }
 
@@ -393,7 +421,7 @@ int enqueue_step64(rkdg_ctx* c, double* x, double dt, bool batch = false) {
     RhsParams P = rhs_params(c, 0, 0, i);
     if (batch) set_batch(c, P, i);
     CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,0, P, in, &ep, c->stream));
-    c->launches++;
+    c->launches += rhs_kernels(c, P);
     if (lim) {
       LimParams L = lim_params_for(c, batch);
       CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 0, L, out, nullptr, c->stream));
@@ -467,7 +495,7 @@ int enqueue_step32(rkdg_ctx* c, double dt, bool batch = false) {
     RhsParams P = rhs_params(c, 1, 0, i);
     if (batch) set_batch(c, P, i);
     CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,1, P, in, &ep, c->stream));
-    c->launches++;
+    c->launches += rhs_kernels(c, P);
     if (lim) {
       LimParams L = lim_params_for(c, batch);
       if (i < s - 1)
@@ -657,8 +685,21 @@ int rkdg_set_solver_quirks(rkdg_ctx* c, int flags) {
 
 int rkdg_set_tuning(rkdg_ctx* c, int key, int value) {
   if (!c) return RKDG_ERR_INVALID;
-  if (key == RKDG_TUNE_HEX_KERNEL && value >= 0 && value <= 2) {
+  if (key == RKDG_TUNE_HEX_KERNEL && value >= 0 && value <= 3) {
+    if (value == 3 && c->has_mesh) {
+      const int st = ensure_fslot(c);
+      if (st) return st;
+    }
     c->hex_variant = value;
+    return RKDG_OK;
+  }
+  const bool block_ok = value == 0 || (value >= 32 && value <= 256 && value % 32 == 0);
+  if (key == RKDG_TUNE_GENERIC_BLOCK && block_ok) {
+    c->gen_block = value;
+    return RKDG_OK;
+  }
+  if (key == RKDG_TUNE_LIMITER_BLOCK && block_ok) {
+    c->lim_block = value;
     return RKDG_OK;
   }
   return fail(c, RKDG_ERR_INVALID, "unknown tuning key or value");
@@ -907,6 +948,10 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     c->h_fcode[(size_t)lf2 * ne + e2] = lf1 | (1 << 3) | (pid << 4);
   }
   T.nperm = (int)perm_ids.size();
+  // the hexahedral kernels keep one byte per point permutation of a square
+  // face (at most its 8 orientations)
+  if (c->geom == RKDG_GEOM_CUBE && T.nperm > RKDG_HEX_MAX_PERM)
+    return fail(c, RKDG_ERR_UNSUPPORTED, "more hexahedral face orientations than a square face has");
   c->tab = T;
   // ---- upload ----
   const size_t nf = (size_t)nfpe * ne;
@@ -932,6 +977,10 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
   c->has_mesh = true;
   int st = refresh_fnbr(c);
   if (st) return st;
+  if (c->hex_variant == 3) {
+    const int st = ensure_fslot(c);
+    if (st) return st;
+  }
   return ensure_scratch(c);
 }
 
@@ -970,7 +1019,7 @@ int rkdg_rhs(rkdg_ctx* c, const double* x, double* y, double* mcs_out) {
     ep.out64 = y;
     RhsParams P = rhs_params(c, 0, 0, 0);
     CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,0, P, x, &ep, c->stream));
-    c->launches++;
+    c->launches += rhs_kernels(c, P);
   } else {
     CUDA_TRY(c, rkdg::launch_to_float(n, x, c->d_y32[0], c->stream));
     EpiParams<float> ep;
@@ -979,7 +1028,7 @@ int rkdg_rhs(rkdg_ctx* c, const double* x, double* y, double* mcs_out) {
     ep.out64 = y;
     RhsParams P = rhs_params(c, 1, 0, 0);
     CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,1, P, c->d_y32[0], &ep, c->stream));
-    c->launches += 2;
+    c->launches += 1 + rhs_kernels(c, P);
   }
   return read_mcs(c, 0, mcs_out);
 }
@@ -1339,7 +1388,7 @@ int plain_rhs(rkdg_ctx* c, const double* in, double* out) {
   ep.out64 = out;
   RhsParams P = rhs_params(c, 0, 0, 7);
   CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p, 0, P, in, &ep, c->stream));
-  c->launches++;
+  c->launches += rhs_kernels(c, P);
   return RKDG_OK;
 }
 
@@ -1518,6 +1567,117 @@ int rkdg_adjoint_run(rkdg_ctx* c, const double* x0, int nsteps, double dt, int e
 }
 
 long long rkdg_kernel_launches(rkdg_ctx* c) { return c ? c->launches : -1; }
+
+// Autotuner: launches every candidate shape of the stage kernel (and of the
+// limiter when one is active) on the caller's state, times them with CUDA
+// events on the context's stream and keeps the fastest.  Candidates: the
+// hexahedral kernel (warp per element with 8 elements per CTA, five-lane team
+// with 24, or the team face pass + element pass) or, on triangles and quads,
+// 64 / 128 / 256 elements per CTA.
+int rkdg_autotune(rkdg_ctx* c, const double* x, int* hex_kernel, int* generic_block,
+                  int* limiter_block) {
+  NEED_MESH(c);
+  if (!x) return fail(c, RKDG_ERR_INVALID, "null state pointer");
+  int st = ensure_scratch(c);
+  if (st) return st;
+  const long long n = c->ndofs * c->neq;
+  const int prec = c->precision == RKDG_FP64 ? 0 : 1;
+  const void* in = x;
+  if (prec) {
+    CUDA_TRY(c, rkdg::launch_to_float(n, x, c->d_y32[0], c->stream));
+    in = c->d_y32[0];
+    c->launches++;
+  }
+  cudaEvent_t ev[2];
+  CUDA_TRY(c, cudaEventCreate(&ev[0]));
+  if (cudaEventCreate(&ev[1]) != cudaSuccess) {
+    cudaEventDestroy(ev[0]);
+    return fail(c, RKDG_ERR_CUDA, "cudaEventCreate failed");
+  }
+  struct Events {
+    cudaEvent_t* e;
+    ~Events() {
+      cudaEventDestroy(e[0]);
+      cudaEventDestroy(e[1]);
+    }
+  } guard{ev};
+  constexpr int kWarm = 2, kReps = 5;
+  // mean time of one right-hand-side launch (plain epilogue into scratch)
+  auto time_rhs = [&](float* ms) -> int {
+    EpiParams<double> ep64;
+    EpiParams<float> ep32;
+    std::memset(&ep64, 0, sizeof ep64);
+    std::memset(&ep32, 0, sizeof ep32);
+    ep64.out64 = ep32.out64 = c->d_y64[0];
+    const void* ep = prec ? (const void*)&ep32 : (const void*)&ep64;
+    const RhsParams P = rhs_params(c, prec, 0, 0);
+    for (int r = 0; r < kWarm + kReps; ++r) {
+      if (r == kWarm) CUDA_TRY(c, cudaEventRecord(ev[0], c->stream));
+      CUDA_TRY(c, cudaMemsetAsync(c->d_mcs, 0, sizeof(unsigned long long), c->stream));
+      CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p, prec, P, in, ep, c->stream));
+      c->launches += rhs_kernels(c, P);
+    }
+    CUDA_TRY(c, cudaEventRecord(ev[1], c->stream));
+    CUDA_TRY(c, cudaEventSynchronize(ev[1]));
+    CUDA_TRY(c, cudaEventElapsedTime(ms, ev[0], ev[1]));
+    *ms /= kReps;
+    return read_mcs(c, 0, nullptr);  // reports a non-physical input state
+  };
+  if (c->geom == RKDG_GEOM_CUBE) {
+    if ((st = ensure_fslot(c))) return st;
+    int best = 0;
+    float tbest = 0.0f;
+    for (int v = 1; v <= 3; ++v) {
+      c->hex_variant = v;
+      float ms = 0.0f;
+      if ((st = time_rhs(&ms))) return st;
+      if (best == 0 || ms < tbest) best = v, tbest = ms;
+    }
+    c->hex_variant = best;
+    if (best != 3) {
+      dfree(c->d_fslot);
+      c->fslot_n = 0;
+    }
+  } else {
+    int best = 0;
+    float tbest = 0.0f;
+    for (int b = 64; b <= 256; b *= 2) {
+      c->gen_block = b;
+      float ms = 0.0f;
+      if ((st = time_rhs(&ms))) return st;
+      if (best == 0 || ms < tbest) best = b, tbest = ms;
+    }
+    c->gen_block = best;
+  }
+  if (c->limiter_active()) {
+    // the limiter rewrites its input: time it on a scratch copy
+    CUDA_TRY(c, rkdg::launch_means(c->geom, c->p, 0, c->ne, c->ndofs, c->d_tab, x, nullptr, c->d_means, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_y64[0], x, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    c->launches++;
+    int best = 0;
+    float tbest = 0.0f;
+    for (int b = 64; b <= 256; b *= 2) {
+      c->lim_block = b;
+      const LimParams L = lim_params(c);
+      for (int r = 0; r < kWarm + kReps; ++r) {
+        if (r == kWarm) CUDA_TRY(c, cudaEventRecord(ev[0], c->stream));
+        CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 0, L, c->d_y64[0], nullptr, c->stream));
+        c->launches++;
+      }
+      CUDA_TRY(c, cudaEventRecord(ev[1], c->stream));
+      CUDA_TRY(c, cudaEventSynchronize(ev[1]));
+      float ms = 0.0f;
+      CUDA_TRY(c, cudaEventElapsedTime(&ms, ev[0], ev[1]));
+      if (best == 0 || ms < tbest) best = b, tbest = ms;
+    }
+    c->lim_block = best;
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (hex_kernel) *hex_kernel = c->hex_variant;
+  if (generic_block) *generic_block = c->gen_block;
+  if (limiter_block) *limiter_block = c->lim_block;
+  return RKDG_OK;
+}
 
 // rkdg_limit with the cell means in the library's fixed device array: the
 // means kernel writes all neq * NE entries before the limiter kernel reads

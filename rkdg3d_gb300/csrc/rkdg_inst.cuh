@@ -9,28 +9,36 @@ namespace rkdg {
 
 constexpr int kGenericBlock = 128;
 
+// Threads per CTA: the tuned value (a multiple of 32 up to kGenericMaxBlock)
+// or the default.
+inline int generic_block(int b) {
+  return (b >= 32 && b <= kGenericMaxBlock && b % 32 == 0) ? b : kGenericBlock;
+}
+
 template <int G, int P>
 cudaError_t launch_rhs_t(int prec, const RhsParams& prm, const void* u, const void* ep,
                          cudaStream_t st) {
-  const int grid = (prm.ne + kGenericBlock - 1) / kGenericBlock;
+  const int blk = generic_block(prm.block);
+  const int grid = (prm.ne + blk - 1) / blk;
   if (prec == 0)
-    k_rhs_generic<G, P, double><<<grid, kGenericBlock, 0, st>>>(
-        prm, (const double*)u, *(const EpiParams<double>*)ep);
+    k_rhs_generic<G, P, double><<<grid, blk, 0, st>>>(prm, (const double*)u,
+                                                      *(const EpiParams<double>*)ep);
   else
-    k_rhs_generic<G, P, float><<<grid, kGenericBlock, 0, st>>>(
-        prm, (const float*)u, *(const EpiParams<float>*)ep);
+    k_rhs_generic<G, P, float><<<grid, blk, 0, st>>>(prm, (const float*)u,
+                                                     *(const EpiParams<float>*)ep);
   return cudaGetLastError();
 }
 
 template <int G, int P>
 cudaError_t launch_limit_t(int mode, const LimParams& prm, void* u, float* ulo, cudaStream_t st) {
-  const int grid = (prm.ne + kGenericBlock - 1) / kGenericBlock;
+  const int blk = generic_block(prm.block);
+  const int grid = (prm.ne + blk - 1) / blk;
   if (mode == 0)
-    k_limit_generic<G, P, double, false><<<grid, kGenericBlock, 0, st>>>(prm, (double*)u, nullptr);
+    k_limit_generic<G, P, double, false><<<grid, blk, 0, st>>>(prm, (double*)u, nullptr);
   else if (mode == 1)
-    k_limit_generic<G, P, float, false><<<grid, kGenericBlock, 0, st>>>(prm, (float*)u, nullptr);
+    k_limit_generic<G, P, float, false><<<grid, blk, 0, st>>>(prm, (float*)u, nullptr);
   else
-    k_limit_generic<G, P, float, true><<<grid, kGenericBlock, 0, st>>>(prm, (float*)u, ulo);
+    k_limit_generic<G, P, float, true><<<grid, blk, 0, st>>>(prm, (float*)u, ulo);
   return cudaGetLastError();
 }
 

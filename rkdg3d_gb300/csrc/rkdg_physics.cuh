@@ -282,9 +282,21 @@ __device__ __forceinline__ void inverse_rotate(R* s, const R* n) {
   }
 }
 
+// a^e for a > 0 (the TRRS pressures).  double and float go through the
+// base-2 logarithm and exponential: within a few ulp of pow() at a fraction of
+// its FP64 cost (the TRRS speeds are the most expensive pointwise piece of the
+// FP64 path); dual numbers keep pow().
 template <typename R>
 __device__ __forceinline__ R powr(R a, R e) {
   return pow(a, e);
+}
+template <>
+__device__ __forceinline__ double powr<double>(double a, double e) {
+  return exp2(e * log2(a));
+}
+template <>
+__device__ __forceinline__ float powr<float>(float a, float e) {
+  return exp2f(e * log2f(a));
 }
 
 // Wave-speed estimates on rotated states: TRRS ComputeToroCharSpeeds

@@ -39,7 +39,7 @@ IND_NOWHERE, IND_EVERYWHERE, IND_BJ = 0, 1, 2
 FUN_BJ, FUN_VENKATAKRISHNAN, FUN_MICHALAK = 0, 1, 2
 QUIRK_MULTIPLIER_ONCE = 1
 FP64, FP32_BULK = 0, 1
-TUNE_HEX_KERNEL = 1
+TUNE_HEX_KERNEL, TUNE_GENERIC_BLOCK, TUNE_LIMITER_BLOCK = 1, 2, 3
 
 # Butcher tableaux in MFEM lower-triangular packing.
 # True SSP-RK3 (Shu-Osher third order) in Butcher form.
@@ -181,6 +181,13 @@ class Context:
 
     def set_tuning(self, key: int, value: int):
         self._chk(self._L.rkdg_set_tuning(self.h, key, value))
+
+    def autotune(self, x) -> dict:
+        """Time the candidate launch shapes on state x and keep the fastest
+        (rkdg_autotune); returns the chosen tuning values."""
+        hk, gb, lb = C.c_int(), C.c_int(), C.c_int()
+        self._chk(self._L.rkdg_autotune(self.h, _ptr(x), C.byref(hk), C.byref(gb), C.byref(lb)))
+        return {"hex_kernel": hk.value, "generic_block": gb.value, "limiter_block": lb.value}
 
     def set_stream(self, stream_ptr: int | None):
         self._chk(self._L.rkdg_set_stream(self.h, stream_ptr))

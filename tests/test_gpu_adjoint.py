@@ -145,3 +145,61 @@ def test_adjoint_run_gradient(cuda):
         fd = (J(x0 + eps * v) - J(x0 - eps * v)) / (2 * eps)
         ad = float(np.dot(g, v))
         assert abs(ad - fd) <= 1e-5 * abs(fd), (ad, fd)
+
+
+def test_adjoint_gradient_full_size(cuda):
+    """Adjoint workload at full size: 32^3 periodic Q1 hexes, eight Gaussian
+    density pulses, HLLC, Venkatakrishnan, SSP-RK3 with dt fixed from CFL 0.2,
+    200 steps checkpointed every 20.  J = 1/2 ||rho(T) - rho_target(T)||^2 with
+    the target run from the seed-1 pulses.
+
+    The reference's limiter makes J only piecewise smooth: the min/max over
+    stencil values switch branches and the indicator's absolute +-1e-3
+    thresholds (indicator_bj.cpp:49-51) jump, and over 600 limited stages some
+    switch usually lies within a few 1e-8 of the state along a random
+    direction.  A direction is therefore judged only when two central
+    differences (eps = 4e-6 and 1e-6) agree with each other to 1e-5 -- no
+    switch inside the window -- and there the adjoint must agree to 1e-5.
+    RKDG_ADJOINT_DIRECTIONS sets the number of random directions (64 for the
+    full check; default 12)."""
+    import os
+    case = cases.gaussian_pulses(n=32, seed=0)
+    target = cases.gaussian_pulses(n=32, seed=1)
+    ctx = ctx_for(case)
+    X = ctx.node_coords()
+    x0 = cases.project(case, X)
+    nd = ctx.ndofs
+    nsteps, every = 200, 20
+    dt = case.cfl * ctx.hmin() / ctx.face_speed(dev(x0)) / (2 * case.order + 1)
+    yt = dev(cases.project(target, X))
+    ctx.run(yt, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps)
+    rho_t = yt.cpu().numpy()[:nd]
+
+    def J(xx):
+        y = dev(xx)
+        ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps)
+        r = y.cpu().numpy()[:nd] - rho_t
+        return 0.5 * float(np.dot(r, r))
+
+    y = dev(x0)
+    ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps)
+    xbar = np.zeros(ctx.n)
+    xbar[:nd] = y.cpu().numpy()[:nd] - rho_t
+    xb = dev(xbar)
+    xT = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    ctx.adjoint_run(dev(x0), nsteps, dt, every, xb, xT)
+    assert torch.allclose(xT, y, rtol=0, atol=1e-12)
+    g = xb.cpu().numpy()
+    ndir = int(os.environ.get("RKDG_ADJOINT_DIRECTIONS", "12"))
+    rng = np.random.default_rng(5)
+    judged, worst = 0, 0.0
+    for _ in range(ndir):
+        v = rng.normal(size=ctx.n) * 1e-2
+        ad = float(np.dot(g, v))
+        fd = [(J(x0 + e * v) - J(x0 - e * v)) / (2 * e) for e in (4e-6, 1e-6)]
+        if abs(fd[0] - fd[1]) > 1e-5 * abs(fd[1]):
+            continue  # a limiter switch inside the difference window
+        judged += 1
+        worst = max(worst, abs(ad - fd[1]) / abs(fd[1]))
+    assert judged >= ndir // 3, (judged, ndir)
+    assert worst <= 1e-5, worst

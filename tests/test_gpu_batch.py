@@ -91,3 +91,41 @@ def test_batch_mixed_close_to_fp64(cuda):
             continue
         e0, e1 = bc.offsets[p] * 4, bc.offsets[p + 1] * 4
         assert rel_l1(B[0, e0:e1], A[0, e0:e1]) < 1e-4, p
+
+
+def test_batch_full_size(cuda):
+    """The batched workload at full size: 256 Riemann problems on N_i x 4
+    strips, N_i ~ U{100..2000} (about 1.08 M elements), t_end 0.15, FP64, one
+    graph launch.  Sampled problems are bit-identical to the same problem run
+    alone; the two smallest are checked against the oracle."""
+    bc = cases.batched_riemann(nprob=256, nmin=100, nmax=2000, seed=0, t_end=0.15)
+    ctx = _ctx(bc)
+    x0 = bc.project(ctx.node_coords())
+    xd = torch.tensor(x0, dtype=torch.float64, device="cuda")
+    info = ctx.batch_run(xd, bc.t_end, bc.cfl, use_graph=True)
+    x = xd.cpu().numpy().reshape(4, -1)
+    nd = 4
+    sizes = np.diff(bc.offsets)
+    ok = np.flatnonzero(info["steps"] > 0)
+    assert ok.size > 200
+    rng = np.random.default_rng(0)
+    sample = set(rng.choice(ok, 3, replace=False).tolist())
+    sample.add(int(ok[np.argmax(sizes[ok])]))
+    smallest = ok[np.argsort(sizes[ok])[:2]].tolist()
+    for p in sorted(sample | set(smallest)):
+        c = bc.cases[p]
+        e0, e1 = bc.offsets[p], bc.offsets[p + 1]
+        xb = x[:, e0 * nd:e1 * nd]
+        single = Context(c.mesh, c.order, device=0, precision=FP64)
+        cases.configure_context(c, single)
+        xs = torch.tensor(cases.project(c, single.node_coords()), dtype=torch.float64, device="cuda")
+        isg = single.run(xs, c.t_end, c.cfl)
+        assert info["steps"][p] == isg["steps"], p
+        assert info["t"][p] == isg["t"], p
+        assert np.array_equal(xb, xs.cpu().numpy().reshape(4, -1)), p
+        if p in smallest:
+            orc = Oracle(c.mesh, c.order)
+            cases.configure_oracle(c, orc)
+            xr, ir = orc.run(cases.project(c, orc.node_coords()), c.t_end, c.cfl)
+            assert info["steps"][p] == ir["steps"], p
+            assert rel_l1(xb[0], xr[:orc.ndofs]) < 1e-8, p

@@ -19,9 +19,14 @@ def make(case, prec):
     return ctx
 
 
-def test_mixed_rhs_close_to_fp64(cuda):
+@pytest.mark.parametrize("variant", [0, 2, 3])
+def test_mixed_rhs_close_to_fp64(cuda, variant):
+    """FP32-bulk right-hand side (fused team kernel, or face pass + element
+    pass) against the plain FP64 one."""
+    from rkdg3d_gb300.solver import TUNE_HEX_KERNEL
     case = cases.pulse3d(n=6, order=2, steps=10)
     c64, c32 = make(case, FP64), make(case, FP32_BULK)
+    c32.set_tuning(TUNE_HEX_KERNEL, variant)
     x = torch.tensor(random_state(c64.node_coords(), seed=9, amp=0.05, vel=0.1), device="cuda",
                      dtype=torch.float64)
     y64 = torch.empty_like(x)

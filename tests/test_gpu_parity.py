@@ -106,11 +106,12 @@ def test_rhs_walls(cuda, geom, order, n, bc, rs, avg):
     assert abs(m - m_ref) <= 1e-13 * abs(m_ref)
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 2, 3])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("walled", [False, True])
 def test_rhs_hex_kernel_variants(cuda, variant, order, walled):
-    """Both hexahedral kernels (warp per element, five-lane team) in FP64."""
+    """The hexahedral kernels (warp per element, five-lane team, face pass +
+    element pass) in FP64."""
     from rkdg3d_gb300.solver import TUNE_HEX_KERNEL
     case = (walled_case(M.GEOM_CUBE, 3, order, RS_HLLC, AVG_EINFELDT, bc=BC_SLIP) if walled
             else periodic_case(M.GEOM_CUBE, 3, order, RS_LLF))
@@ -229,3 +230,34 @@ def test_conservation_periodic_hex(cuda):
         ctx.step(x, 2e-3)
     t1 = ctx.totals(x)
     assert np.all(np.abs(t1 - t0) <= 1e-13 * np.abs(t0).max())
+
+
+@pytest.mark.parametrize("geom,order", [(M.GEOM_SQUARE, 2), (M.GEOM_TRIANGLE, 1), (M.GEOM_CUBE, 1)])
+def test_autotune_keeps_parity(cuda, geom, order):
+    """The autotuner picks a launch shape; RHS and limiter still match the
+    oracle (block size never changes the arithmetic)."""
+    if geom == M.GEOM_TRIANGLE:
+        case = cases.Case("tri", M.tri_grid(8, 6, jitter=0.2), order, RS_HLLC, AVG_TRRS,
+                          bcs=[(a, BC_SLIP, None) for a in (1, 2, 3, 4)])
+    else:
+        case = periodic_case(geom, 4, order, RS_HLLC)
+    case.limiter = (LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 0)
+    ctx, orc = pair(case)
+    x = random_state(orc.node_coords(), seed=5)
+    before_y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    ctx.rhs(dev(x), before_y)
+    choice = ctx.autotune(dev(x))
+    if geom == M.GEOM_CUBE:
+        assert choice["hex_kernel"] in (1, 2, 3)
+    else:
+        assert choice["generic_block"] in (64, 128, 256)
+        assert choice["limiter_block"] in (64, 128, 256)
+    y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    ctx.rhs(dev(x), y)
+    y_ref, _ = orc.rhs(x)
+    assert rel_l1(y.cpu().numpy(), y_ref) < 1e-12
+    if geom != M.GEOM_CUBE:
+        assert torch.equal(y, before_y)
+    xd = dev(x)
+    ctx.limit(xd)
+    assert rel_l1(xd.cpu().numpy(), orc.limit(x)) < 1e-12
