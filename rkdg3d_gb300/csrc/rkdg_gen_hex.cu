@@ -59,12 +59,15 @@ static cudaError_t launch_hex_split(const RhsParams& prm, const R* u, const EpiP
   return launch_hex_team_mode<P, R, 2>(prm, u, ep, st);
 }
 
+// Defaults: Q1 -- face pass + element pass (each face's numerical flux once;
+// the fused kernel where the context holds no flux slots); Q2 -- the
+// warp-per-element kernel in FP64, the fused team kernel in FP32.
 template <>
 cudaError_t launch_rhs_t<5, 1>(int prec, const RhsParams& prm, const void* u, const void* ep,
                                cudaStream_t st) {
   if (prec == 0)
-    return launch_hex_team<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st);
-  return launch_hex_team<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+    return launch_hex_split<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st);
+  return launch_hex_split<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
 }
 template <>
 cudaError_t launch_rhs_t<5, 2>(int prec, const RhsParams& prm, const void* u, const void* ep,

@@ -263,7 +263,8 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
 // Kernels one right-hand-side launch issues (the split hexahedral variant
 // runs a face pass and an element pass).
 int rhs_kernels(const rkdg_ctx* c, const RhsParams& P) {
-  return (c->geom == RKDG_GEOM_CUBE && c->hex_variant == 3 && P.fslot && !P.faces_only) ? 2 : 1;
+  const bool split = c->hex_variant == 3 || (c->hex_variant == 0 && c->p == 1);
+  return (c->geom == RKDG_GEOM_CUBE && split && P.fslot && !P.faces_only) ? 2 : 1;
 }
 
 // Flux slots of the split hexahedral variant: [ne][6][neq][nqf] values of
@@ -977,7 +978,7 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
   c->has_mesh = true;
   int st = refresh_fnbr(c);
   if (st) return st;
-  if (c->hex_variant == 3) {
+  if (c->hex_variant == 3 || c->p == 1) {  // the split hexahedral kernels
     const int st = ensure_fslot(c);
     if (st) return st;
   }
