@@ -313,7 +313,7 @@ def run_ours(args, rank, world, local):
             "traffic": args.traffic_per_launch or TRAFFIC_BYTES_PER_ELEMENT_LAUNCH * ctx32.ne,
             "traffic_source": "ncu dram bytes, 48^3 capture scaled by elements"
                               if not args.traffic_per_launch else "command line",
-            "peak_source": peak_src, "kernel": "k_rhs_hex_team<2,float> (stage kernel, 3 launches per step)",
+            "peak_source": peak_src, "kernel": "k_rhs_hex_team<2,float,0> (fused stage kernel, 3 launches per step)",
             "algorithmic_bytes_per_launch": bps / STAGES}
 
     cpu = None
