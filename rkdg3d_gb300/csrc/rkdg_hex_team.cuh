@@ -227,18 +227,47 @@ __device__ __forceinline__ void team_lift_any(int lf, const R* f, const R* l1d, 
   }
 }
 
+// The values of one variable of an element ordered along its local face LFO,
+// nbv[(i0*N1 + i1)*N1 + jn] = u[node(jn along the normal, i0, i1)], with
+// compile-time offsets (GLOBAL: read-only global loads, else shared memory).
+template <int P, int LFO, bool GLOBAL, typename R>
+__device__ __forceinline__ void team_gather(const R* src, R (&nbv)[(P + 1) * (P + 1) * (P + 1)]) {
+  constexpr int N1 = P + 1, NAX = hex_face_axis(LFO);
+#pragma unroll
+  for (int i0 = 0; i0 < N1; ++i0)
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1)
+#pragma unroll
+      for (int jn = 0; jn < N1; ++jn) {
+        const R* a = src + hnode<N1>(NAX, jn, i0, i1);
+        nbv[(i0 * N1 + i1) * N1 + jn] = GLOBAL ? __ldg(a) : *a;
+      }
+}
+
+template <int P, bool GLOBAL, typename R>
+__device__ __forceinline__ void team_gather_any(int lfo, const R* src,
+                                                R (&nbv)[(P + 1) * (P + 1) * (P + 1)]) {
+  switch (lfo) {
+    case 0: team_gather<P, 0, GLOBAL>(src, nbv); break;
+    case 1: team_gather<P, 1, GLOBAL>(src, nbv); break;
+    case 2: team_gather<P, 2, GLOBAL>(src, nbv); break;
+    case 3: team_gather<P, 3, GLOBAL>(src, nbv); break;
+    case 4: team_gather<P, 4, GLOBAL>(src, nbv); break;
+    default: team_gather<P, 5, GLOBAL>(src, nbv); break;
+  }
+}
+
 // Phase 1 of one face (runtime index LF) for the team's variable k: the own
 // trace and, across an interior face, the neighbour's trace at the face
 // points, stored point-major (To[q*NEQ + k], Tn[q*NEQ + k]).  The own values
 // are read from the staged tile su (compile-time offsets, a small switch over
 // the face); the neighbour's values come from the staged tile when it is
-// there, else from global memory, through a node table.
+// there, else from global memory, with compile-time offsets per face.
 template <int P, typename R>
 __device__ __forceinline__ void team_traces(const int LF, const R* __restrict__ ug, long long NDa,
                                             int k, const R* su, R* xch,
-                                            const R* l1d, const R* lend,
-                                            const unsigned char (*nodet)[(P + 1) * (P + 1) * (P + 1)],
-                                            int nb, int code, const R* sU, int e0, int nel) {
+                                            const R* l1d, const R* lend, int nb, int code,
+                                            const R* sU, int e0, int nel) {
   using S = TeamSize<P>;
   constexpr int N1 = S::N1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, NF2 = S::NF2;
   R* To = xch;
@@ -247,16 +276,10 @@ __device__ __forceinline__ void team_traces(const int LF, const R* __restrict__ 
   // issue the neighbour's loads first; the own-side work hides their latency
   R nbv[ND];
   if (nb >= 0) {
-    const unsigned char* nt = nodet[lfo];  // [(i0*N1+i1)*N1 + jn]
-    if (nb >= e0 && nb < e0 + nel) {  // neighbour staged in this tile
-      const R* sn = sU + ((nb - e0) * NEQ + k) * ND;
-#pragma unroll
-      for (int i = 0; i < ND; ++i) nbv[i] = sn[nt[i]];
-    } else {
-      const R* ugn = ug + k * NDa + (long long)nb * ND;
-#pragma unroll
-      for (int i = 0; i < ND; ++i) nbv[i] = __ldg(ugn + nt[i]);
-    }
+    if (nb >= e0 && nb < e0 + nel)  // neighbour staged in this tile
+      team_gather_any<P, false>(lfo, sU + ((nb - e0) * NEQ + k) * ND, nbv);
+    else
+      team_gather_any<P, true>(lfo, ug + k * NDa + (long long)nb * ND, nbv);
   }
   {
     R v[N1 * N1];
@@ -370,7 +393,6 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ unsigned char sPerm[RKDG_HEX_MAX_PERM][NQF];
   __shared__ unsigned char sFab[6][NQF];
-  __shared__ unsigned char sNodeT[6][ND];  // node of (face, i0*N1+i1, jn)
   R* sm = reinterpret_cast<R*>(smraw);
   R* tL1 = sm;                  // [NQ1][N1]
   R* tLend = tL1 + NQ1 * N1;    // [2][N1]
@@ -393,10 +415,6 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
   for (int t = tid; t < min(T->nperm, RKDG_HEX_MAX_PERM) * NQF; t += blockDim.x)
     sPerm[t / NQF][t % NQF] = (unsigned char)T->perm[t / NQF][t % NQF];
   for (int t = tid; t < 6 * NQF; t += blockDim.x) sFab[t / NQF][t % NQF] = (unsigned char)T->fab[t / NQF][t % NQF];
-  for (int t = tid; t < 6 * ND; t += blockDim.x) {
-    const int lf = t / ND, r = (t % ND) / N1, jn = t % N1;
-    sNodeT[lf][t % ND] = (unsigned char)hnode<N1>(hex_face_axis(lf), jn, r / N1, r % N1);
-  }
 
   const int ne = prm.ne;
   const long long NDa = prm.ndofs;
@@ -441,7 +459,7 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
       const bool mine = nb != -1 && (MODE == 0 || ((sFcd[el][lf] >> 3) & 1) == 0);
       if (MODE == 1 && !__any_sync(0xffffffffu, mine)) continue;
       if (mine)
-        team_traces<P, R>(lf, u, NDa, k, su, xch, tL1, tLend, sNodeT, nb, sFcd[el][lf], sU, e0, nel);
+        team_traces<P, R>(lf, u, NDa, k, su, xch, tL1, tLend, nb, sFcd[el][lf], sU, e0, nel);
       __syncwarp();
       warp_fluxes<P, R, MODE>(lf, prm, lane, wel0, nel, wx, tWf, sPerm, sFab, sFnb, sFcd, e0, gamma,
                               cov, lmax);
