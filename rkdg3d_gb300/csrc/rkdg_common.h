@@ -72,6 +72,23 @@ struct BCSlot {
   double state[5];
 };
 
+// 1D operators of the tensor-product hexahedral team kernels (order <= 2),
+// passed by value inside the kernel parameters so that their entries are
+// constant-bank operands of the arithmetic instead of shared-memory loads.
+template <typename R>
+struct HexOps {
+  R l1d[12];   // [NQ1][N1] 1D basis at the face-rule points
+  R lend[6];   // [2][N1]   1D basis at 0 and 1
+  R d1[9];     // [N1][N1]  collocated derivative w_m l_j'(x_m)
+  R minv1[9];  // [N1][N1]  1D inverse mass
+  R w1[3];     // 1D node weights
+  R wf[16];    // face-rule weights
+};
+struct HexOpsPair {
+  HexOps<float> f;
+  HexOps<double> d;
+};
+
 // Per-element face table entry codes (fcode): bits 0-2 local face of the
 // other element, bit 3 = 1 if this element is the face's Elem2, bits 4..
 // permutation id.  fnbr: neighbour element id, -1 = boundary face with no
@@ -102,6 +119,7 @@ struct RhsParams {
   int* pfail;           // per-problem failure flag (non-physical state)
   int block;            // threads per CTA of the generic kernels (0: default)
   void* fslot;          // hexahedral face-pass flux slots [ne][6][neq][nqf] (or null)
+  HexOpsPair hops;      // hexahedra (order <= 2): 1D operators
 };
 
 // Stage epilogue.

@@ -27,6 +27,17 @@
 
 namespace rkdg {
 
+template <typename R>
+__device__ __forceinline__ const HexOps<R>& hex_ops(const HexOpsPair& h);
+template <>
+__device__ __forceinline__ const HexOps<float>& hex_ops<float>(const HexOpsPair& h) {
+  return h.f;
+}
+template <>
+__device__ __forceinline__ const HexOps<double>& hex_ops<double>(const HexOpsPair& h) {
+  return h.d;
+}
+
 template <int P>
 struct TeamSize {
   static constexpr int N1 = P + 1, NQ1 = P + 2, ND = N1 * N1 * N1, NQF = NQ1 * NQ1, NEQ = 5,
@@ -49,12 +60,10 @@ struct TeamSize {
   __host__ __device__ static constexpr int xstr() { return (xch<MODE>() + 11 + 31) & ~31; }
   template <int MODE>
   __host__ __device__ static constexpr int wstr() { return TPW * xstr<MODE>() + 32; }
-  static constexpr int TAB = NQ1 * N1 + 2 * N1 + 2 * N1 * N1 + N1 + NQF;
-  static constexpr int TAB_AL = (TAB + 3) & ~3;
   __host__ __device__ static constexpr int xoff(int t) { return 16 * (t & 1) + 5 * (t >> 1); }
   template <typename R, int MODE>
   static constexpr size_t smem_bytes() {
-    return sizeof(R) * (size_t)(TAB_AL + EPB * NEQ * ND + WARPS * wstr<MODE>());
+    return sizeof(R) * (size_t)(EPB * NEQ * ND + WARPS * wstr<MODE>());
   }
   // resident CTAs per SM the register allocation is bounded for
   template <typename R, int MODE>
@@ -386,32 +395,26 @@ __device__ __forceinline__ void warp_fluxes(const int LF, const RhsParams& prm, 
 // Runge-Kutta epilogue.
 template <int P, typename R, int MODE>
 __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>())
-    k_rhs_hex_team(const RhsParams prm, const R* __restrict__ u, const EpiParams<R> ep) {
+    k_rhs_hex_team(const __grid_constant__ RhsParams prm, const R* __restrict__ u,
+                   const EpiParams<R> ep) {
   using S = TeamSize<P>;
-  constexpr int N1 = S::N1, NQ1 = S::NQ1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, EPB = S::EPB;
+  constexpr int N1 = S::N1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, EPB = S::EPB;
   constexpr int XSTR = S::template xstr<MODE>(), WSTR = S::template wstr<MODE>();
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ unsigned char sPerm[RKDG_HEX_MAX_PERM][NQF];
   __shared__ unsigned char sFab[6][NQF];
   R* sm = reinterpret_cast<R*>(smraw);
-  R* tL1 = sm;                  // [NQ1][N1]
-  R* tLend = tL1 + NQ1 * N1;    // [2][N1]
-  R* tD1 = tLend + 2 * N1;      // [N1][N1]
-  R* tMinv = tD1 + N1 * N1;     // [N1][N1]
-  R* tW1 = tMinv + N1 * N1;     // [N1]
-  R* tWf = tW1 + N1;            // [NQF]
-  R* sU = sm + S::TAB_AL;       // [EPB][NEQ][ND]
+  const HexOps<R>& H = hex_ops<R>(prm.hops);  // 1D operators (kernel parameters)
+  const R* tL1 = H.l1d;         // [NQ1][N1]
+  const R* tLend = H.lend;      // [2][N1]
+  const R* tD1 = H.d1;          // [N1][N1]
+  const R* tMinv = H.minv1;     // [N1][N1]
+  const R* tW1 = H.w1;          // [N1]
+  const R* tWf = H.wf;          // [NQF]
+  R* sU = sm;                   // [EPB][NEQ][ND]
   R* sX = sU + EPB * NEQ * ND;  // [WARPS][WSTR] team exchange rows
   const RefTables* T = prm.tab;
   const int tid = threadIdx.x;
-  for (int t = tid; t < NQ1 * N1; t += blockDim.x) tL1[t] = (R)T->l1d[t / N1][t % N1];
-  for (int t = tid; t < 2 * N1; t += blockDim.x) tLend[t] = (R)T->lend[t / N1][t % N1];
-  for (int t = tid; t < N1 * N1; t += blockDim.x) {
-    tD1[t] = (R)T->d1[t / N1][t % N1];
-    tMinv[t] = (R)T->minv1[t / N1][t % N1];
-  }
-  for (int t = tid; t < N1; t += blockDim.x) tW1[t] = (R)T->w1[t];
-  for (int t = tid; t < NQF; t += blockDim.x) tWf[t] = (R)T->wf[t];
   for (int t = tid; t < min(T->nperm, RKDG_HEX_MAX_PERM) * NQF; t += blockDim.x)
     sPerm[t / NQF][t % NQF] = (unsigned char)T->perm[t / NQF][t % NQF];
   for (int t = tid; t < 6 * NQF; t += blockDim.x) sFab[t / NQF][t % NQF] = (unsigned char)T->fab[t / NQF][t % NQF];

@@ -257,6 +257,26 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   P.err = c->d_err;
   P.block = c->gen_block;
   P.fslot = c->d_fslot;
+  if (c->geom == RKDG_GEOM_CUBE && c->p <= 2) {
+    const int n1 = c->p + 1, nq1 = c->p + 2;
+    const RefTables& T = c->tab;
+    auto fill = [&](auto& H) {
+      for (int a = 0; a < nq1; ++a)
+        for (int j = 0; j < n1; ++j) H.l1d[a * n1 + j] = T.l1d[a][j];
+      for (int sd = 0; sd < 2; ++sd)
+        for (int j = 0; j < n1; ++j) H.lend[sd * n1 + j] = T.lend[sd][j];
+      for (int j = 0; j < n1; ++j) {
+        for (int m = 0; m < n1; ++m) {
+          H.d1[j * n1 + m] = T.d1[j][m];
+          H.minv1[j * n1 + m] = T.minv1[j][m];
+        }
+        H.w1[j] = T.w1[j];
+      }
+      for (int q = 0; q < nq1 * nq1; ++q) H.wf[q] = T.wf[q];
+    };
+    fill(P.hops.f);
+    fill(P.hops.d);
+  }
   return P;
 }
 
