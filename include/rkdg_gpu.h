@@ -218,13 +218,18 @@ int rkdg_adjoint_run(rkdg_ctx* ctx, const double* x0_dev, int nsteps, double dt,
 long long rkdg_kernel_launches(rkdg_ctx* ctx);
 
 /* ---- allocation-free limiter ----------------------------------------------
- * No counterpart in the reference.  Same result as rkdg_limit (bit for bit),
- * but the cell means it needs go to a fixed device array of
- * RKDG_LIMIT_STATIC_MAX_VALUES doubles (16 MiB) built into the library instead
- * of context memory; the call allocates nothing.  Meshes with
- * neq * NE > RKDG_LIMIT_STATIC_MAX_VALUES are rejected with RKDG_ERR_INVALID
- * and x is left untouched.  The array is shared by every context on a device:
- * calls that overlap in time on one device (other host threads, other
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory while they step -- a host code whose device memory is owned by its
+ * own memory manager or a framework's caching pool, or a time loop that must
+ * not stall the GPU (cudaMalloc / cudaFree can synchronise the device).  Same
+ * result as rkdg_limit (bit for bit), but the cell means it needs go to a
+ * fixed device array of RKDG_LIMIT_STATIC_MAX_VALUES doubles (16 MiB) built
+ * into the library instead of context memory; the call allocates nothing.
+ * Meshes with neq * NE > RKDG_LIMIT_STATIC_MAX_VALUES are rejected with
+ * RKDG_ERR_INVALID and x is left untouched.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture.  The array is shared by every context on a
+ * device: calls that overlap in time on one device (other host threads, other
  * streams) race on it and must be serialised by the caller. */
 #define RKDG_LIMIT_STATIC_MAX_VALUES (1u << 21)
 int rkdg_limit_static(rkdg_ctx* ctx, double* x_dev);

@@ -1,12 +1,19 @@
 // Fixed device scratch for rkdg_limit_static (include/rkdg_gpu.h).
 //
-// The cell means that the limiter reads live in one file-scope device array
-// of RKDG_LIMIT_STATIC_MAX_VALUES doubles (16 MiB), created with the module on
-// every device that loads the library.  Its device address is looked up once
-// per device, with that device current, and cached.  Every context on a device
-// shares the array, so two rkdg_limit_static calls in flight at the same time
-// on one device (two host threads, or two contexts on different streams)
-// overwrite each other's means.
+// Some callers may not allocate device memory while they step: a host code
+// whose device memory belongs to its own memory manager or to a framework's
+// caching pool, or a time loop that must not stall the device (cudaMalloc and
+// cudaFree can synchronise it).  For them the cell means that the limiter
+// reads live in one file-scope device array of RKDG_LIMIT_STATIC_MAX_VALUES
+// doubles (16 MiB), which every GPU that loads the library holds until the
+// process exits.  In host code the array's name is only a stand-in, not a
+// device address: the first rkdg_limit_static call on a device looks the
+// address up with cudaGetSymbolAddress (that device current) and caches it, so
+// that first call should come before any stream capture.  Every context on a
+// device shares the array, so two rkdg_limit_static calls in flight at the
+// same time on one device (two host threads, or two contexts on different
+// streams) overwrite each other's means; nothing in it needs to start at zero,
+// because the means kernel writes every entry the limiter then reads.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -18,7 +25,7 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 
-__device__ __align__(256) double g_static_means[RKDG_LIMIT_STATIC_MAX_VALUES];
+static __device__ __align__(256) double g_static_means[RKDG_LIMIT_STATIC_MAX_VALUES];
 
 std::mutex g_mutex;
 double* g_addr[kMaxDevices] = {};

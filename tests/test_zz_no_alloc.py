@@ -1,6 +1,11 @@
-"""rkdg_limit_static (cell means in the library's fixed device array, no
-allocation) against rkdg_limit (cell means in context memory): bit-identical
-on two calls in a row, and meshes beyond the fixed capacity are rejected."""
+"""rkdg_limit_static against rkdg_limit.
+
+rkdg_limit_static serves callers that may not allocate device memory while
+they step (their device memory belongs to another allocator, or their loop
+must not stall on cudaMalloc/cudaFree): it keeps the cell means in the
+library's fixed device array instead of context memory.  Checked here through
+the C ABI: bit-identical to rkdg_limit on two calls in a row, and meshes
+beyond the fixed capacity are rejected with x untouched."""
 import numpy as np
 import pytest
 import torch
