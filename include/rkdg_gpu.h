@@ -47,7 +47,16 @@ enum {
   RKDG_BC_OPEN = 1,             /* "outlet", boundary_integrator_open.cpp:9-12 */
   RKDG_BC_FIXED_ROTATED = 2,    /* BoundaryIntegratorConstant, boundary_integrator_constant.cpp:8-20 */
   RKDG_BC_SUPERSONIC_INLET = 3, /* boundary_integrator_supersonic_inlet.cpp:8-19 */
-  RKDG_BC_WALL = 4              /* boundary_integrator_wall.cpp:7-17 (same as slip) */
+  RKDG_BC_WALL = 4,             /* boundary_integrator_wall.cpp:7-17 (same as slip) */
+  RKDG_BC_SUBSONIC_INLET = 5,   /* boundary_integrator_subsonic_inlet.cpp:10-19:
+                                   2 * fixed - own in the rotated frame */
+  /* perfect-gas ghost states; state = {pTot, TTot} / {pFix, TTot} / {pFix} /
+   * {pTot, TFix} in its first entries (an array of neq values): */
+  RKDG_BC_SUBSONIC_INLET_TOTAL_PRESSURE = 6, /* ..._subsonic_inlet_total_pressure.cpp:10-40 */
+  RKDG_BC_SUBSONIC_INLET_FIXED_PRESSURE = 7, /* ..._subsonic_inlet_fixed_pressure.cpp:10-36 */
+  RKDG_BC_FIXED_PRESSURE_OUTLET = 8,         /* boundary_integrator_open_fixed_pressure.cpp:10-30 */
+  RKDG_BC_TOTAL_PRESSURE_OUTLET = 9          /* boundary_integrator_open_total_pressure.cpp:10-40;
+                                                m.n uses the normal's own components */
 };
 enum { RKDG_LIM_FINDIFF = 0, RKDG_LIM_MULTI = 1 };
 enum { RKDG_IND_NOWHERE = 0, RKDG_IND_EVERYWHERE = 1, RKDG_IND_BJ = 2 };

@@ -839,6 +839,63 @@ void compute_right_state(const ref_ctx* c, const BC& bc, const double* s1, doubl
     case 3:  // supersonic inlet, boundary_integrator_supersonic_inlet.cpp:8-19
       for (int i = 0; i < dim + 2; ++i) s2[i] = bc.state[i];
       break;
+    case 5:  // subsonic inlet, boundary_integrator_subsonic_inlet.cpp:10-19:
+             // 2 * fixed - own, in the rotated frame
+      rotate(dim, s2, nor);
+      for (int i = 0; i < dim + 2; ++i) s2[i] = 2.0 * bc.state[i] - s2[i];
+      inverse_rotate(dim, s2, nor);
+      break;
+    case 6:  // subsonicInletTotalPressure, ..._subsonic_inlet_total_pressure.cpp:10-40
+    case 7: {  // subsonicInletFixedPressure, ..._subsonic_inlet_fixed_pressure.cpp:10-36
+      const double g = c->P.gamma, R = c->P.R, TTot = bc.state[1];
+      double rhoU2 = 0;
+      for (int d = 0; d < dim; ++d) rhoU2 += s1[1 + d] * s1[1 + d];
+      rhoU2 /= s1[0];
+      const double MTTotSq = rhoU2 / s1[0] / g / R / TTot;
+      const double MSq = MTTotSq / (1.0 - 0.5 * (g - 1.0) * MTTotSq);
+      const double p = bc.type == 6
+                           ? bc.state[0] * std::pow(1.0 + 0.5 * (g - 1.0) * MSq, -g / (g - 1.0))
+                           : bc.state[0];
+      const double T = TTot / (1.0 + 0.5 * (g - 1.0) * MSq);
+      const double rho = p / R / T;
+      s2[neq - 1] = p / (g - 1.0) + 0.5 * rhoU2 / s1[0] * rho;
+      for (int d = 0; d < dim; ++d) s2[1 + d] = s1[1 + d] / s1[0] * rho;
+      s2[0] = rho;
+      break;
+    }
+    case 8: {  // fixedPressureOutlet, boundary_integrator_open_fixed_pressure.cpp:10-30
+      // (epsIn subtracts 0.5 |m|^2, not 0.5 |m|^2 / rho, as the reference does)
+      const double g = c->P.gamma, pFix = bc.state[0];
+      double rhoU2 = 0;
+      for (int d = 0; d < dim; ++d) rhoU2 += s1[1 + d] * s1[1 + d];
+      const double U2 = rhoU2 / s1[0] / s1[0];
+      const double epsIn = (s1[neq - 1] - 0.5 * rhoU2) / s1[0];
+      const double rho = pFix / (g - 1.0) / epsIn;
+      s2[neq - 1] = pFix / (g - 1.0) + 0.5 * rho * U2;
+      for (int d = 0; d < dim; ++d) s2[1 + d] = s1[1 + d] / s1[0] * rho;
+      s2[0] = rho;
+      break;
+    }
+    case 9: {  // totalPressureFixedTemperatureOutlet, ..._open_total_pressure.cpp:10-40
+      // The reference forms m.n from nor[1..dim] (one past the normal's last
+      // component); here m.n uses nor[0..dim-1].
+      const double g = c->P.gamma, R = c->P.R, pTot = bc.state[0], TFix = bc.state[1];
+      double rho2U2 = 0, rhoN = 0;
+      for (int d = 0; d < dim; ++d) {
+        rho2U2 += s1[1 + d] * s1[1 + d];
+        rhoN += s1[1 + d] * nor[d];
+      }
+      const double U2 = rho2U2 / s1[0] / s1[0];
+      const double epsIn = rhoN > 0 ? (s1[neq - 1] - 0.5 * rho2U2) / s1[0] : R / (g - 1.0) * TFix;
+      const double M = std::sqrt(rho2U2 / s1[0] / s1[0]) / sound_speed(c->P, s1);  // ComputeM
+      double p = M > 1 ? pTot * std::pow(1.0 + 0.5 * (g - 1.0) * M * M, -g / (g - 1.0)) : pTot;
+      const double rho = M > 1 ? p / (g - 1.0) / epsIn : p / (0.5 * U2 + (g - 1.0) * epsIn);
+      p = M > 1 ? p : p - 0.5 * U2 * rho;
+      s2[neq - 1] = p / (g - 1.0) + 0.5 * rho * U2;
+      for (int d = 0; d < dim; ++d) s2[1 + d] = s1[1 + d] * (rho / s1[0]);
+      s2[0] = rho;
+      break;
+    }
   }
 }
 
@@ -1155,13 +1212,21 @@ int ref_set_physics(ref_ctx* c, int rsolver, int averaging, double gamma, double
 }
 
 int ref_set_bc(ref_ctx* c, int attr, int type, const double* state) {
-  if (type < 0 || type > 4) return REF_ERR_INVALID;
+  if (type < 0 || type > 9) return REF_ERR_INVALID;
+  if (!state && (type == 2 || type == 3 || type >= 5)) return REF_ERR_INVALID;
   BC bc;
   bc.type = type;
   if (state)
     for (int i = 0; i < c->neq; ++i) bc.state[i] = state[i];
   c->bcs[attr] = bc;
   rebuild_items(c);
+  return REF_OK;
+}
+
+int ref_right_state(ref_ctx* c, int attr, const double* s1, const double* nor, double* s2) {
+  auto it = c->bcs.find(attr);
+  if (it == c->bcs.end() || !s1 || !nor || !s2) return REF_ERR_INVALID;
+  compute_right_state(c, it->second, s1, s2, nor);
   return REF_OK;
 }
 

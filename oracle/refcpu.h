@@ -57,8 +57,16 @@ int ref_set_physics(ref_ctx* c, int rsolver, int averaging, double gamma,
                     double covolume, double gas_constant);
 /* bc type: 0 slip, 1 open (outlet), 2 fixed state in the rotated frame
  * (BoundaryIntegratorConstant), 3 supersonic inlet (global-frame state),
- * 4 wall (same as slip).  state = conservative variables (neq) or NULL. */
+ * 4 wall (same as slip), 5 subsonic inlet (fixed rotated-frame state),
+ * 6 subsonicInletTotalPressure {pTot, TTot}, 7 subsonicInletFixedPressure
+ * {pFix, TTot}, 8 fixedPressureOutlet {pFix}, 9
+ * totalPressureFixedTemperatureOutlet {pTot, TFix}.  state (neq values) =
+ * conservative variables (types 2, 3, 5), the listed parameters in its first
+ * entries (6-9), or NULL. */
 int ref_set_bc(ref_ctx* c, int attr, int type, const double* state);
+/* computeRightState of attribute attr's boundary condition for the state s1
+ * and the unit outward normal nor (test hook). */
+int ref_right_state(ref_ctx* c, int attr, const double* s1, const double* nor, double* s2);
 /* limiter: 0 FinDiff, 1 Multi; indicator: 0 Nowhere, 1 Everywhere, 2 BJ family;
  * function: 0 BJ, 1 Venkatakrishnan, 2 Michalak; quirks bit0: apply the
  * multiplier once instead of nd times. */

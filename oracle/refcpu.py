@@ -40,6 +40,7 @@ def lib():
         L.ref_destroy.argtypes = [C.c_void_p]
         L.ref_set_physics.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double]
         L.ref_set_bc.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp]
+        L.ref_right_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
         L.ref_set_limiter.argtypes = [C.c_void_p] + [C.c_int] * 5
         L.ref_set_tableau.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
         L.ref_set_threads.argtypes = [C.c_int]
@@ -119,8 +120,21 @@ class Oracle:
         self._chk(lib().ref_set_physics(self.h, rsolver, averaging, gamma, covolume, gas_constant))
 
     def set_bc(self, attr, bctype, state=None):
-        st = None if state is None else np.ascontiguousarray(state, dtype=np.float64)
+        """state: conservative variables, or the boundary condition's
+        parameters in its first entries; padded to five values."""
+        st = None
+        if state is not None:
+            st = np.zeros(5, dtype=np.float64)
+            v = np.asarray(state, dtype=np.float64).ravel()
+            st[:v.size] = v
         self._chk(lib().ref_set_bc(self.h, attr, bctype, _d(st) if st is not None else None))
+
+    def right_state(self, attr, s1, nor):
+        s1 = np.ascontiguousarray(s1, dtype=np.float64)
+        nor = np.ascontiguousarray(nor, dtype=np.float64)
+        s2 = np.zeros_like(s1)
+        self._chk(lib().ref_right_state(self.h, attr, _d(s1), _d(nor), _d(s2)))
+        return s2
 
     def set_limiter(self, limiter=0, indicator=0, function=2, last_hope=1, quirks=0):
         self._chk(lib().ref_set_limiter(self.h, limiter, indicator, function, last_hope, quirks))

@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(64)
       }
       if (nb < 0) {
         const BCSlot& bc = prm.bc[-2 - nb];
-        right_state<DIM>(bc.type, bc.state, s1, s2, n);
+        right_state<DIM>(bc.type, bc.state, s1, s2, n, gamma, cov, (decltype(gamma))prm.rgas);
       }
       D F[NEQ];
       riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg);

@@ -102,6 +102,7 @@ struct RhsParams {
   const void* egeo;     // [dim*dim+1][ne]   adj(J) (row r, col d), 1/det J
   const RefTables* tab;
   double gamma, covolume;
+  double rgas;          // specific gas constant (subsonic inlet / outlet BCs)
   int rs, avg;
   int faces_only;       // 1: face terms only (A.Mult for the initial dt)
   int quirks;           // bit 0: negative HLLC speed is not an error

@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
           }
         } else {
           const BCSlot& bc = prm.bc[-2 - nb];
-          right_state<DIM>(bc.type, bc.state, s1, s2, n);
+          right_state<DIM>(bc.type, bc.state, s1, s2, n, gamma, cov, (decltype(gamma))prm.rgas);
         }
         R F[NEQ];
         const R sp = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e, pb);

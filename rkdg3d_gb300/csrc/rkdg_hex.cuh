@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
           for (int k = 0; k < NEQ; ++k) s1[k] = sTO[k * NQF + q];
           const BCSlot& bc = prm.bc[-2 - nb];
-          right_state<3>(bc.type, bc.state, s1, s2, n);
+          right_state<3>(bc.type, bc.state, s1, s2, n, gamma, cov, (R)prm.rgas);
         }
         R F[NEQ];
         const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e);

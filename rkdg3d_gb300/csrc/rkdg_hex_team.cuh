@@ -364,7 +364,7 @@ __device__ __forceinline__ void warp_fluxes(const int LF, const RhsParams& prm, 
 #pragma unroll
       for (int kk = 0; kk < NEQ; ++kk) s1[kk] = To[own * NEQ + kk];
       const BCSlot& bc = prm.bc[-2 - nb];
-      right_state<3>(bc.type, bc.state, s1, s2, n);
+      right_state<3>(bc.type, bc.state, s1, s2, n, gamma, cov, (R)prm.rgas);
     }
     R F[NEQ];
     const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e0 + el);

@@ -247,6 +247,7 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   P.tab = c->d_tab;
   P.gamma = c->gamma;
   P.covolume = c->cov;
+  P.rgas = c->gasR;
   P.rs = c->rs;
   P.avg = c->avg;
   P.faces_only = faces_only;
@@ -637,9 +638,9 @@ int rkdg_set_physics(rkdg_ctx* c, int rsolver, int averaging, double gamma, doub
 
 int rkdg_set_bc(rkdg_ctx* c, int attr, int type, const double* state) {
   if (!c) return RKDG_ERR_INVALID;
-  if (type < 0 || type > 4 || attr < 1) return fail(c, RKDG_ERR_INVALID, "invalid boundary condition");
-  if ((type == RKDG_BC_FIXED_ROTATED || type == RKDG_BC_SUPERSONIC_INLET) && !state)
-    return fail(c, RKDG_ERR_INVALID, "fixed-state boundary needs a state");
+  if (type < 0 || type > 9 || attr < 1) return fail(c, RKDG_ERR_INVALID, "invalid boundary condition");
+  if ((type == RKDG_BC_FIXED_ROTATED || type == RKDG_BC_SUPERSONIC_INLET || type >= 5) && !state)
+    return fail(c, RKDG_ERR_INVALID, "this boundary condition needs a state or its parameters");
   if (!c->bcs.count(attr) && (int)c->bcs.size() >= RKDG_MAX_BC)
     return fail(c, RKDG_ERR_INVALID, "too many boundary attributes");
   BCSlot bc;

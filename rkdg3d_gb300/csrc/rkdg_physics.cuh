@@ -439,7 +439,7 @@ __device__ __forceinline__ R riemann(R* s1, R* s2, const R* n, R* flux, R gamma,
 // computeRightState of the boundary integrators.
 template <int DIM, typename R>
 __device__ __forceinline__ void right_state(int type, const double* st, const R* s1, R* s2,
-                                            const R* n) {
+                                            const R* n, R gamma, R b, R rg) {
   constexpr int NEQ = DIM + 2;
 #pragma unroll
   for (int i = 0; i < NEQ; ++i) s2[i] = s1[i];
@@ -454,6 +454,69 @@ __device__ __forceinline__ void right_state(int type, const double* st, const R*
   } else if (type == 3) {  // supersonic inlet, global frame
 #pragma unroll
     for (int i = 0; i < NEQ; ++i) s2[i] = (R)st[i];
+  } else if (type == 5) {  // subsonic inlet: 2 * fixed - own, rotated frame
+    rotate<DIM>(s2, n);
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) s2[i] = R(2) * (R)st[i] - s2[i];
+    inverse_rotate<DIM>(s2, n);
+  } else if (type == 6 || type == 7) {
+    // subsonicInletTotalPressure / subsonicInletFixedPressure
+    // (boundary_integrator_subsonic_inlet_{total,fixed}_pressure.cpp:10-40):
+    // perfect-gas ghost state at the inlet's total temperature
+    const R TTot = (R)st[1];
+    R rhoU2 = R(0);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) rhoU2 += s1[1 + d] * s1[1 + d];
+    rhoU2 = fdv(rhoU2, s1[0]);
+    const R MTTotSq = fdv(fdv(fdv(fdv(rhoU2, s1[0]), gamma), rg), TTot);
+    const R MSq = fdv(MTTotSq, R(1) - R(0.5) * (gamma - R(1)) * MTTotSq);
+    const R base = R(1) + R(0.5) * (gamma - R(1)) * MSq;
+    const R p = type == 6 ? (R)st[0] * powr(base, -fdv(gamma, gamma - R(1))) : (R)st[0];
+    const R T = fdv(TTot, base);
+    const R rho = fdv(fdv(p, rg), T);
+    s2[NEQ - 1] = fdv(p, gamma - R(1)) + R(0.5) * fdv(rhoU2, s1[0]) * rho;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) s2[1 + d] = fdv(s1[1 + d], s1[0]) * rho;
+    s2[0] = rho;
+  } else if (type == 8) {
+    // fixedPressureOutlet (boundary_integrator_open_fixed_pressure.cpp:10-30);
+    // epsIn subtracts 0.5 |m|^2 (not 0.5 |m|^2 / rho), as the reference does
+    const R pFix = (R)st[0];
+    R rhoU2 = R(0);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) rhoU2 += s1[1 + d] * s1[1 + d];
+    const R U2 = fdv(fdv(rhoU2, s1[0]), s1[0]);
+    const R epsIn = fdv(s1[NEQ - 1] - R(0.5) * rhoU2, s1[0]);
+    const R rho = fdv(fdv(pFix, gamma - R(1)), epsIn);
+    s2[NEQ - 1] = fdv(pFix, gamma - R(1)) + R(0.5) * rho * U2;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) s2[1 + d] = fdv(s1[1 + d], s1[0]) * rho;
+    s2[0] = rho;
+  } else if (type == 9) {
+    // totalPressureFixedTemperatureOutlet (boundary_integrator_open_total_
+    // pressure.cpp:10-40); m.n from the normal's own components (the
+    // reference indexes one past them)
+    const R pTot = (R)st[0], TFix = (R)st[1];
+    R rho2U2 = R(0), rhoN = R(0);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      rho2U2 += s1[1 + d] * s1[1 + d];
+      rhoN += s1[1 + d] * n[d];
+    }
+    const R U2 = fdv(fdv(rho2U2, s1[0]), s1[0]);
+    const R epsIn = rhoN > R(0) ? fdv(s1[NEQ - 1] - R(0.5) * rho2U2, s1[0])
+                                : fdv(rg, gamma - R(1)) * TFix;
+    const R M = fdv(fsq(U2), sound_speed_p<DIM>(s1, pressure<DIM>(s1, gamma, b), gamma, b));
+    const bool sup = M > R(1);
+    R p = sup ? pTot * powr(R(1) + R(0.5) * (gamma - R(1)) * M * M, -fdv(gamma, gamma - R(1)))
+              : pTot;
+    const R rho = sup ? fdv(fdv(p, gamma - R(1)), epsIn)
+                      : fdv(p, R(0.5) * U2 + (gamma - R(1)) * epsIn);
+    if (!sup) p = p - R(0.5) * U2 * rho;
+    s2[NEQ - 1] = fdv(p, gamma - R(1)) + R(0.5) * rho * U2;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) s2[1 + d] = s1[1 + d] * fdv(rho, s1[0]);
+    s2[0] = rho;
   }
 }
 

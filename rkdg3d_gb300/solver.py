@@ -34,6 +34,9 @@ RKDG_ERR_UNPHYSICAL = 2
 RS_RUSANOV, RS_LLF, RS_HLL, RS_HLLC = 0, 1, 2, 3
 AVG_TRRS, AVG_EINFELDT = 0, 1
 BC_SLIP, BC_OPEN, BC_FIXED_ROTATED, BC_SUPERSONIC_INLET, BC_WALL = 0, 1, 2, 3, 4
+# parameters in state: {pTot, TTot}, {pFix, TTot}, {pFix}, {pTot, TFix}
+(BC_SUBSONIC_INLET, BC_SUBSONIC_INLET_TOTAL_PRESSURE, BC_SUBSONIC_INLET_FIXED_PRESSURE,
+ BC_FIXED_PRESSURE_OUTLET, BC_TOTAL_PRESSURE_OUTLET) = 5, 6, 7, 8, 9
 LIM_FINDIFF, LIM_MULTI = 0, 1
 IND_NOWHERE, IND_EVERYWHERE, IND_BJ = 0, 1, 2
 FUN_BJ, FUN_VENKATAKRISHNAN, FUN_MICHALAK = 0, 1, 2
@@ -156,7 +159,13 @@ class Context:
                                            physics.covolume, physics.gas_constant))
 
     def set_bc(self, attr: int, bctype: int, state=None):
-        arr = None if state is None else np.ascontiguousarray(state, dtype=np.float64)
+        """state: conservative variables, or the boundary condition's
+        parameters in its first entries (padded to five values)."""
+        arr = None
+        if state is not None:
+            arr = np.zeros(5, dtype=np.float64)
+            v = np.asarray(state, dtype=np.float64).ravel()
+            arr[:v.size] = v
         self._chk(self._L.rkdg_set_bc(self.h, attr, bctype,
                                       arr.ctypes.data_as(_capi._dp) if arr is not None else None))
         self._keep_bc = arr

@@ -68,6 +68,30 @@ def test_rhs_vjp_fd(cuda, geom, order, rs, walled):
     fd_check(apply, vjp, x, seed=1)
 
 
+@pytest.mark.parametrize("bc,params", [(6, [1.2, 1.1]), (7, [0.9, 1.1]), (8, [0.95]),
+                                       (9, [1.1, 1.0])])
+@pytest.mark.parametrize("geom", [M.GEOM_SQUARE, M.GEOM_CUBE])
+def test_rhs_vjp_pressure_bcs_fd(cuda, bc, params, geom):
+    """Subsonic inlets and pressure outlets (their ghost states through dual
+    numbers) on every side of a box."""
+    case = walled_case(geom, 3, 1, RS_HLLC, bc=bc)
+    case.bcs = [(a, bc, params) for a, _, _ in case.bcs]
+    ctx = ctx_for(case)
+    x = random_state(ctx.node_coords(), seed=4, amp=0.1, vel=0.2)
+
+    def apply(xx):
+        y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.rhs(dev(xx), y)
+        return y.cpu().numpy()
+
+    def vjp(w):
+        out = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.rhs_vjp(dev(x), dev(w), out)
+        return out.cpu().numpy()
+
+    fd_check(apply, vjp, x, seed=2)
+
+
 @pytest.mark.parametrize("fun", [FUN_VENKATAKRISHNAN, FUN_MICHALAK])
 @pytest.mark.parametrize("geom", [M.GEOM_SQUARE, M.GEOM_CUBE])
 def test_limit_vjp_fd(cuda, fun, geom):

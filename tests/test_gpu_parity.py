@@ -11,8 +11,11 @@ import torch
 from oracle.refcpu import Oracle
 from rkdg3d_gb300 import cases
 from rkdg3d_gb300 import mesh as M
-from rkdg3d_gb300.solver import (AVG_EINFELDT, AVG_TRRS, BC_FIXED_ROTATED, BC_OPEN, BC_SLIP,
-                                 BC_SUPERSONIC_INLET, FUN_BJ, FUN_MICHALAK, FUN_VENKATAKRISHNAN,
+from rkdg3d_gb300.solver import (AVG_EINFELDT, AVG_TRRS, BC_FIXED_PRESSURE_OUTLET,
+                                 BC_FIXED_ROTATED, BC_OPEN, BC_SLIP, BC_SUBSONIC_INLET,
+                                 BC_SUBSONIC_INLET_FIXED_PRESSURE,
+                                 BC_SUBSONIC_INLET_TOTAL_PRESSURE, BC_SUPERSONIC_INLET,
+                                 BC_TOTAL_PRESSURE_OUTLET, FUN_BJ, FUN_MICHALAK, FUN_VENKATAKRISHNAN,
                                  IND_BJ, IND_EVERYWHERE, IND_NOWHERE, LIM_FINDIFF, LIM_MULTI,
                                  RS_HLL, RS_HLLC, RS_LLF, RS_RUSANOV, TABLEAU_REFERENCE_RK3,
                                  TABLEAU_SSPRK3, Context)
@@ -86,17 +89,27 @@ def test_rhs_periodic(cuda, rs, geom, order, n):
     assert abs(m - m_ref) <= 1e-13 * m_ref
 
 
+# parameters of the pressure / temperature boundary conditions
+BC_PARAMS = {BC_SUBSONIC_INLET_TOTAL_PRESSURE: [1.2, 1.1], BC_SUBSONIC_INLET_FIXED_PRESSURE: [0.9, 1.1],
+             BC_FIXED_PRESSURE_OUTLET: [0.95], BC_TOTAL_PRESSURE_OUTLET: [1.1, 1.0]}
+
+
 @pytest.mark.parametrize("geom,order,n", [(M.GEOM_SQUARE, 1, 5), (M.GEOM_SQUARE, 2, 4),
                                           (M.GEOM_TRIANGLE, 1, 5), (M.GEOM_TRIANGLE, 2, 4),
                                           (M.GEOM_CUBE, 1, 3), (M.GEOM_CUBE, 2, 2)])
-@pytest.mark.parametrize("bc", [BC_SLIP, BC_OPEN, BC_FIXED_ROTATED, BC_SUPERSONIC_INLET])
+@pytest.mark.parametrize("bc", [BC_SLIP, BC_OPEN, BC_FIXED_ROTATED, BC_SUPERSONIC_INLET,
+                                BC_SUBSONIC_INLET, BC_SUBSONIC_INLET_TOTAL_PRESSURE,
+                                BC_SUBSONIC_INLET_FIXED_PRESSURE, BC_FIXED_PRESSURE_OUTLET,
+                                BC_TOTAL_PRESSURE_OUTLET])
 @pytest.mark.parametrize("rs,avg", [(RS_HLLC, AVG_EINFELDT), (RS_HLL, AVG_TRRS), (RS_RUSANOV, 0)])
 def test_rhs_walls(cuda, geom, order, n, bc, rs, avg):
     case = walled_case(geom, n, order, rs, avg, covolume=0.005, bc=bc)
     dim = case.dim
-    if bc in (BC_FIXED_ROTATED, BC_SUPERSONIC_INLET):
+    if bc in (BC_FIXED_ROTATED, BC_SUPERSONIC_INLET, BC_SUBSONIC_INLET):
         st = cases.supersonic_inlet_state(1.1, 0.3, -0.2, 0.1, 0.9, 1.4, dim)
         case.bcs = [(a, bc, st) for a, _, _ in case.bcs]
+    elif bc in BC_PARAMS:
+        case.bcs = [(a, bc, BC_PARAMS[bc]) for a, _, _ in case.bcs]
     ctx, orc = pair(case)
     x = random_state(ctx.node_coords(), b=0.005, seed=7)
     y_ref, m_ref = orc.rhs(x)

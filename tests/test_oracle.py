@@ -188,3 +188,67 @@ def test_golden_vectors(name):
     assert rel_l1(o.limit(x), g[f"{name}/limited"]) < 1e-14
     xs, _ = o.step(x, dt)
     assert rel_l1(xs, g[f"{name}/step"]) < 1e-14
+
+
+def _bc_oracle(dim, bctype, params, gamma=1.4, R=1.0):
+    geom, n = (M.GEOM_CUBE, 3) if dim == 3 else (M.GEOM_SQUARE, 3)
+    case = walled_case(geom, n, 1, 0)
+    orc = Oracle(case.mesh, case.order)
+    orc.set_physics(0, 0, gamma, 0.0, R)
+    orc.set_bc(1, bctype, params)
+    return orc
+
+
+def _prim(s, gamma, dim):
+    rho = s[0]
+    u = s[1:1 + dim] / rho
+    p = (gamma - 1) * (s[-1] - 0.5 * rho * u @ u)
+    return rho, u, p
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_bc_subsonic_inlets_known_answers(dim):
+    """subsonicInlet{Total,Fixed}Pressure: the ghost state keeps the velocity,
+    sits at T = TTot / (1 + (g-1)/2 M^2) with M^2 = MT^2 / (1 - (g-1)/2 MT^2),
+    MT^2 = |u|^2 / (g R TTot), and has p = pFix, or p = pTot (T/TTot)^(g/(g-1))."""
+    g, R = 1.4, 0.7
+    s1 = cases.conservative([np.array([1.1]), *[np.array([v]) for v in (0.2, -0.1, 0.15)[:dim]],
+                             np.array([0.9])], g, 0.0).ravel()
+    nor = np.zeros(dim)
+    nor[0] = -1.0
+    for bctype, pv, TTot in ((6, 1.3, 1.2), (7, 0.8, 1.2)):
+        s2 = _bc_oracle(dim, bctype, [pv, TTot], g, R).right_state(1, s1, nor)
+        rho2, u2, p2 = _prim(s2, g, dim)
+        u1 = s1[1:1 + dim] / s1[0]
+        assert np.allclose(u2, u1, rtol=1e-14, atol=0)
+        mt2 = u1 @ u1 / (g * R * TTot)
+        m2 = mt2 / (1 - 0.5 * (g - 1) * mt2)
+        T = TTot / (1 + 0.5 * (g - 1) * m2)
+        assert p2 / (rho2 * R) == pytest.approx(T, rel=1e-13)
+        want = pv * (T / TTot) ** (g / (g - 1)) if bctype == 6 else pv
+        assert p2 == pytest.approx(want, rel=1e-13)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_bc_outlets_known_answers(dim):
+    """fixedPressureOutlet: ghost pressure pFix at the interior velocity.
+    totalPressureFixedTemperatureOutlet, subsonic: p + rho |u|^2 / 2 = pTot at
+    the interior velocity.  subsonicInlet: own + ghost = 2 * fixed in the
+    rotated frame (for a normal along x: componentwise)."""
+    g = 1.4
+    s1 = cases.conservative([np.array([0.9]), *[np.array([v]) for v in (0.3, 0.1, -0.2)[:dim]],
+                             np.array([1.1])], g, 0.0).ravel()
+    nor = np.zeros(dim)
+    nor[0] = 1.0
+    u1 = s1[1:1 + dim] / s1[0]
+    s2 = _bc_oracle(dim, 8, [0.7]).right_state(1, s1, nor)
+    rho2, u2, p2 = _prim(s2, g, dim)
+    assert p2 == pytest.approx(0.7, rel=1e-13)
+    assert np.allclose(u2, u1, rtol=1e-14, atol=0)
+    s2 = _bc_oracle(dim, 9, [1.3, 1.0]).right_state(1, s1, nor)
+    rho2, u2, p2 = _prim(s2, g, dim)
+    assert np.allclose(u2, u1, rtol=1e-14, atol=0)
+    assert p2 + 0.5 * rho2 * u2 @ u2 == pytest.approx(1.3, rel=1e-13)
+    fixed = np.array([1.0, 0.2, 0.05, 0.0, 2.6])[[0, *range(1, 1 + dim), 4]]
+    s2 = _bc_oracle(dim, 5, fixed).right_state(1, s1, nor)
+    assert np.allclose(s1 + s2, 2 * fixed, rtol=1e-14, atol=1e-15)
