@@ -61,8 +61,13 @@ enum {
 enum { RKDG_LIM_FINDIFF = 0, RKDG_LIM_MULTI = 1 };
 enum { RKDG_IND_NOWHERE = 0, RKDG_IND_EVERYWHERE = 1, RKDG_IND_BJ = 2 };
 enum { RKDG_FUN_BJ = 0, RKDG_FUN_VENKATAKRISHNAN = 1, RKDG_FUN_MICHALAK = 2 };
-/* quirk flags of rkdg_set_limiter: 0 reproduces the shipped reference. */
-enum { RKDG_QUIRK_MULTIPLIER_ONCE = 1 };
+/* flags of rkdg_set_limiter: 0 reproduces the shipped reference.
+ * RKDG_QUIRK_MULTIPLIER_ONCE applies the multiplier once instead of nd times;
+ * RKDG_LIMITER_LINEARIZE is the reference's "linearize" option of the Multi
+ * limiter (limiter_multiplier.cpp:101-178, case_manager.cpp:551-554): quads
+ * and hexes of order 1 (its point rule has fewer points than nodes above
+ * order 1: RKDG_ERR_UNSUPPORTED), a no-op on triangles. */
+enum { RKDG_QUIRK_MULTIPLIER_ONCE = 1, RKDG_LIMITER_LINEARIZE = 2 };
 enum { RKDG_FP64 = 0, RKDG_FP32_BULK = 1 };
 
 /* Mesh as the host (MFEM) sees it after every adapt.  elem_vertices are

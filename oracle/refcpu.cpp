@@ -1381,11 +1381,38 @@ int ref_means(ref_ctx* c, const double* x, double* means) {
   return REF_OK;
 }
 
+// LimiterMultiplier::linearize, limiter_multiplier.cpp:101-178: every
+// variable becomes mean + (reference-space gradient at the centre) . (x_j - c)
+// at the points of the element rule of order p+1 (the nodes for p = 1, the
+// only order where that rule has nd points).
+void linearize(const ref_ctx* c, const double* um, double* el) {
+  const int nd = c->nd, neq = c->neq, dim = c->dim;
+  const double cen[3] = {0.5, 0.5, 0.5};
+  double dphi[125 * 3];
+  c->fe.dshape(cen, dphi);
+  const Rule r = rule_geom(c->geom, c->p + 1);
+  for (int k = 0; k < neq; ++k) {
+    double g[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d)
+      for (int j = 0; j < nd; ++j) g[d] += el[k * nd + j] * dphi[j * dim + d];
+    for (int j = 0; j < nd; ++j) {
+      const double* ip = &r.x[j * dim];
+      double v = um[k] - g[0] * (cen[0] - ip[0]) - g[1] * (cen[1] - ip[1]);
+      if (dim == 3) v -= g[2] * (cen[2] - ip[2]);
+      el[k * nd + j] = v;
+    }
+  }
+}
+
 // Limiter::update, limiter.cpp:22-94, with IndicatorBJ::checkDiscontinuity
 // (indicator_bj.cpp:88-200), updateYMin (15-86), LimiterMultiplier::limit
 // (limiter_multiplier.cpp:12-99), LimiterFinDiff::limit (limiter_findiff.cpp:3-33).
 int ref_limit(ref_ctx* c, double* x) {
   const int nd = c->nd, neq = c->neq, dim = c->dim, ne = c->ne;
+  if ((c->quirks & 2) && c->lim == 1 && c->geom != REF_GEOM_TRIANGLE && c->p != 1) {
+    c->err = "linearize needs order 1 (its rule has fewer points than nodes)";
+    return REF_ERR_INVALID;
+  }
   const long long ND = c->ndofs;
   c->means.assign((size_t)ne * neq, 0.0);
   means_of(c, x, c->means.data());
@@ -1470,9 +1497,12 @@ int ref_limit(ref_ctx* c, double* x) {
     for (int k = 0; k < neq; ++k) um[k] = mean[k * (long long)ne + e];
     if (c->lim == 1) {  // LimiterMultiplier::limit
       int reps = (c->quirks & 1) ? 1 : nd;  // shadowed iDof loop (Q4)
+      const bool lin = (c->quirks & 2) && c->geom != REF_GEOM_TRIANGLE;
       for (int k = 0; k < neq; ++k)
-        for (int r = 0; r < reps; ++r)
+        for (int r = 0; r < reps; ++r) {
+          if (lin) linearize(c, um, el);  // limiter_multiplier.cpp:29-30
           for (int j = 0; j < nd; ++j) el[k * nd + j] = um[k] + minValue * (el[k * nd + j] - um[k]);
+        }
       if (c->last_hope) {
         double shape[125];
         for (int v = 0; v < nverts; ++v) {

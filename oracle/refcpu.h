@@ -69,7 +69,8 @@ int ref_set_bc(ref_ctx* c, int attr, int type, const double* state);
 int ref_right_state(ref_ctx* c, int attr, const double* s1, const double* nor, double* s2);
 /* limiter: 0 FinDiff, 1 Multi; indicator: 0 Nowhere, 1 Everywhere, 2 BJ family;
  * function: 0 BJ, 1 Venkatakrishnan, 2 Michalak; quirks bit0: apply the
- * multiplier once instead of nd times. */
+ * multiplier once instead of nd times; bit1: the "linearize" option of the
+ * Multi limiter (quads and hexes of order 1; a no-op on triangles). */
 int ref_set_limiter(ref_ctx* c, int limiter, int indicator, int function,
                     int last_hope, int quirks);
 int ref_set_tableau(ref_ctx* c, int s, const double* a, const double* b,

@@ -64,6 +64,12 @@ struct RefTables {
   // canonical face point q -> tensor index a + nq1*b (a along the lower
   // tangential axis, b along the upper one)
   int fab[RKDG_MAX_NFPE][RKDG_MAX_NQF];
+  // limiter "linearize" option (tensor elements, order 1): reference-space
+  // gradients of the basis at the element centre and the points of the
+  // element rule of order p+1
+  double dcen[RKDG_MAX_ND][3];
+  double xlin[RKDG_MAX_ND][3];
+  int lin_ok;
 };
 
 // Boundary condition slot.

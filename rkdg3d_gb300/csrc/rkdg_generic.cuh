@@ -465,6 +465,34 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
     minValue = yMin[0];
   }
   if (prm.limiter == 1) {
+    if constexpr (G != 2) {
+      if (prm.quirks & 2) {
+        // linearize (limiter_multiplier.cpp:101-178): mean + centre gradient
+        // . (x_j - c); a linear state is its own linearisation, so once here
+        // equals the reference's application before every multiplier pass
+#pragma unroll
+        for (int k = 0; k < NEQ; ++k) {
+          double g[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+          for (int d = 0; d < DIM; ++d)
+#pragma unroll
+            for (int j = 0; j < ND; ++j) {
+              double v = (double)el[k][j];
+              if constexpr (DS) v += (double)lo[k][j];
+              g[d] += v * T->dcen[j][d];
+            }
+          const double m = prm.means[(long long)k * ne + e];
+#pragma unroll
+          for (int j = 0; j < ND; ++j) {
+            double v = m;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) v -= g[d] * (0.5 - T->xlin[j][d]);
+            el[k][j] = (R)v;
+            if constexpr (DS) lo[k][j] = (float)(v - (double)(float)v);
+          }
+        }
+      }
+    }
     const int reps = (prm.quirks & 1) ? 1 : ND;
 #pragma unroll
     for (int k = 0; k < NEQ; ++k)

@@ -661,6 +661,10 @@ int rkdg_set_limiter(rkdg_ctx* c, int limiter, int indicator, int function, int 
   if (!c) return RKDG_ERR_INVALID;
   if (limiter < 0 || limiter > 1 || indicator < 0 || indicator > 2 || function < 0 || function > 2)
     return fail(c, RKDG_ERR_INVALID, "invalid limiter configuration");
+  if ((quirk_flags & RKDG_LIMITER_LINEARIZE) && limiter == RKDG_LIM_MULTI && c->has_mesh &&
+      c->geom != RKDG_GEOM_TRIANGLE && !c->tab.lin_ok)
+    return fail(c, RKDG_ERR_UNSUPPORTED,
+                "linearize needs order 1 (its rule of order p+1 has fewer points than nodes)");
   c->lim = limiter;
   c->ind = indicator;
   c->fun = function;
@@ -1003,6 +1007,10 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     const int st = ensure_fslot(c);
     if (st) return st;
   }
+  if ((c->quirks & RKDG_LIMITER_LINEARIZE) && c->lim == RKDG_LIM_MULTI &&
+      c->geom != RKDG_GEOM_TRIANGLE && !c->tab.lin_ok)
+    return fail(c, RKDG_ERR_UNSUPPORTED,
+                "linearize needs order 1 (its rule of order p+1 has fewer points than nodes)");
   return ensure_scratch(c);
 }
 
@@ -1489,6 +1497,9 @@ int adjoint_ready(rkdg_ctx* c) {
   if (!rkdg::adjoint_supported(c->geom, c->p))
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint kernels for this element type / order");
   if (c->nprob > 0) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for batched problems");
+  if ((c->quirks & RKDG_LIMITER_LINEARIZE) && c->limiter_active() && c->lim == RKDG_LIM_MULTI &&
+      c->geom != RKDG_GEOM_TRIANGLE)
+    return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for the linearize limiter option");
   return RKDG_OK;
 }
 

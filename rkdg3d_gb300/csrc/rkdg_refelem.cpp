@@ -321,6 +321,17 @@ bool build_ref_tables(int geom, int p, RefTables& T, std::vector<FacePoint>* fpt
     for (int i = 0; i < nd; ++i)
       for (int j = 0; j < nd; ++j) T.Minv[i][j] = Mi[i * nd + j];
   }
+  // linearize option of the Multi limiter (limiter_multiplier.cpp:101-178)
+  if (geom != 2) {
+    const double cen[3] = {0.5, 0.5, 0.5};
+    B.eval(cen, phi.data(), dphi.data());
+    for (int j = 0; j < nd; ++j)
+      for (int d = 0; d < dim; ++d) T.dcen[j][d] = dphi[j * dim + d];
+    Pts r = elem_rule(geom, p + 1);
+    T.lin_ok = r.n >= nd ? 1 : 0;
+    for (int j = 0; j < nd && j < r.n; ++j)
+      for (int d = 0; d < dim; ++d) T.xlin[j][d] = r.x[j * dim + d];
+  }
   // cell-mean weights
   {
     Pts r = elem_rule(geom, p + orderW);

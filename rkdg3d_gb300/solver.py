@@ -43,6 +43,8 @@ FUN_BJ, FUN_VENKATAKRISHNAN, FUN_MICHALAK = 0, 1, 2
 QUIRK_MULTIPLIER_ONCE = 1
 FP64, FP32_BULK = 0, 1
 TUNE_HEX_KERNEL, TUNE_GENERIC_BLOCK, TUNE_LIMITER_BLOCK = 1, 2, 3
+# flags of set_limiter(quirks=...)
+QUIRK_MULTIPLIER_ONCE, LIMITER_LINEARIZE = 1, 2
 
 # Butcher tableaux in MFEM lower-triangular packing.
 # True SSP-RK3 (Shu-Osher third order) in Butcher form.

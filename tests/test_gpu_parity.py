@@ -274,3 +274,29 @@ def test_autotune_keeps_parity(cuda, geom, order):
     xd = dev(x)
     ctx.limit(xd)
     assert rel_l1(xd.cpu().numpy(), orc.limit(x)) < 1e-12
+
+
+@pytest.mark.parametrize("geom", [M.GEOM_SQUARE, M.GEOM_CUBE, M.GEOM_TRIANGLE])
+@pytest.mark.parametrize("quirks", [2, 3])
+def test_limiter_linearize_parity(cuda, geom, quirks):
+    """The Multi limiter's linearize option (limiter_multiplier.cpp:101-178),
+    order 1, with the multiplier applied nd times or once."""
+    case = (walled_case(geom, 4, 1, RS_HLLC, bc=BC_SLIP) if geom != M.GEOM_CUBE
+            else periodic_case(geom, 3, 1, RS_HLLC))
+    case.limiter = (LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, quirks)
+    ctx, orc = pair(case)
+    x = random_state(orc.node_coords(), seed=8, amp=0.2)
+    xl_ref = orc.limit(x)
+    xd = dev(x)
+    ctx.limit(xd)
+    assert rel_l1(xd.cpu().numpy(), xl_ref) < 1e-12
+    if geom != M.GEOM_TRIANGLE:
+        assert rel_l1(xl_ref, x) > 1e-6  # the option changed the state
+
+
+def test_limiter_linearize_rejects_order_2(cuda):
+    from rkdg3d_gb300.solver import RkdgError
+    case = periodic_case(M.GEOM_SQUARE, 4, 2, RS_HLLC)
+    ctx = Context(case.mesh, case.order, device=0)
+    with pytest.raises(RkdgError):
+        ctx.set_limiter(LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 2)

@@ -252,3 +252,20 @@ def test_bc_outlets_known_answers(dim):
     fixed = np.array([1.0, 0.2, 0.05, 0.0, 2.6])[[0, *range(1, 1 + dim), 4]]
     s2 = _bc_oracle(dim, 5, fixed).right_state(1, s1, nor)
     assert np.allclose(s1 + s2, 2 * fixed, rtol=1e-14, atol=1e-15)
+
+
+def test_linearize_keeps_means_and_is_linear():
+    """Multi + linearize on Q1 quads (Nowhere indicator: multiplier 1): the
+    means stay, and every variable becomes linear in the reference
+    coordinates (the bilinear coefficient vanishes)."""
+    case = periodic_case(M.GEOM_SQUARE, 4, 1, 0)
+    orc = Oracle(case.mesh, case.order)
+    cases.configure_oracle(case, orc)
+    orc.set_limiter(1, 0, 2, 0, 2)
+    x = random_state(orc.node_coords(), seed=2)
+    y = orc.limit(x)
+    assert np.allclose(orc.means(y), orc.means(x), rtol=0, atol=1e-14)
+    v = y.reshape(orc.neq, -1, 4)  # nodes (x0,y0), (x1,y0), (x0,y1), (x1,y1)
+    assert np.allclose(v[..., 0] - v[..., 1] - v[..., 2] + v[..., 3], 0.0, atol=1e-13)
+    orc.set_limiter(1, 0, 2, 0, 0)
+    assert not np.allclose(orc.limit(x), y)
