@@ -59,7 +59,11 @@ enum {
                                                 m.n uses the normal's own components */
 };
 enum { RKDG_LIM_FINDIFF = 0, RKDG_LIM_MULTI = 1 };
-enum { RKDG_IND_NOWHERE = 0, RKDG_IND_EVERYWHERE = 1, RKDG_IND_BJ = 2 };
+/* RKDG_IND_SHU: IndicatorShu (indicator_shu.cpp:13-74) with the extrapolated
+ * stencil averages of averager.cpp:154-273; FinDiff limiter only (with Multi
+ * the reference multiplies by a per-cell factor the Shu indicator never
+ * writes: RKDG_ERR_UNSUPPORTED). */
+enum { RKDG_IND_NOWHERE = 0, RKDG_IND_EVERYWHERE = 1, RKDG_IND_BJ = 2, RKDG_IND_SHU = 3 };
 enum { RKDG_FUN_BJ = 0, RKDG_FUN_VENKATAKRISHNAN = 1, RKDG_FUN_MICHALAK = 2 };
 /* flags of rkdg_set_limiter: 0 reproduces the shipped reference.
  * RKDG_QUIRK_MULTIPLIER_ONCE applies the multiplier once instead of nd times;

@@ -1232,8 +1232,8 @@ int ref_right_state(ref_ctx* c, int attr, const double* s1, const double* nor, d
 
 int ref_set_limiter(ref_ctx* c, int limiter, int indicator, int function, int last_hope,
                     int quirks) {
-  if (limiter < 0 || limiter > 1 || indicator < 0 || indicator > 2 || function < 0 ||
-      function > 2)
+  if (limiter < 0 || limiter > 1 || indicator < 0 || indicator > 3 || function < 0 ||
+      function > 2 || (indicator == 3 && limiter == 1))
     return REF_ERR_INVALID;
   c->lim = limiter;
   c->ind = indicator;
@@ -1381,6 +1381,60 @@ int ref_means(ref_ctx* c, const double* x, double* means) {
   return REF_OK;
 }
 
+// IndicatorShu::checkDiscontinuity, indicator_shu.cpp:13-74, with the
+// extrapolated averages of Averager::computeStencilExtrapAverages and
+// assembleShiftedElementMatrix (averager.cpp:154-273): for each stencil cell k
+// (the cell, then ElementToElementTable neighbours) the rule of order
+// p + OrderW on the troubled cell e, mapped to physical space by e and back to
+// k's reference space, weights k's polynomial by |J_k| w_q; divided by
+// int_psi(k) = the integral of 1 over k.
+void shu_indicator(const ref_ctx* c, const double* x, const double* mean, int e, double* val) {
+  const int nd = c->nd, neq = c->neq, dim = c->dim, ne = c->ne;
+  const long long ND = c->ndofs;
+  const Rule r = rule_geom(c->geom, c->p + 0 + c->orderW);
+  double maxF[5], sumD[5], ume[5];
+  for (int k = 0; k < neq; ++k) {
+    maxF[k] = -1e9;
+    sumD[k] = 0.0;
+    ume[k] = mean[k * (long long)ne + e];
+  }
+  std::vector<int> st(1, e);
+  for (int nb : c->el_el[e]) st.push_back(nb);
+  double shape[125];
+  for (int kc : st) {
+    double Jk[9], x0[3], zero[3] = {0, 0, 0}, Kinv[9];
+    elem_map(c, kc, zero, x0, Jk);
+    const double dk = det(dim, Jk);
+    adjugate(dim, Jk, Kinv);
+    for (int i = 0; i < dim * dim; ++i) Kinv[i] /= dk;
+    double loc[5] = {0, 0, 0, 0, 0};
+    for (int q = 0; q < r.n; ++q) {
+      double xp[3], ipr[3] = {0, 0, 0};
+      elem_map(c, e, &r.x[q * dim], xp, nullptr);  // TransTroubled.Transform
+      for (int i = 0; i < dim; ++i)                 // Trans.TransformBack
+        for (int m = 0; m < dim; ++m) ipr[i] += Kinv[i * dim + m] * (xp[m] - x0[m]);
+      c->fe.shape(ipr, shape);
+      const double w = dk * r.w[q];
+      for (int k = 0; k < neq; ++k) {
+        double v = 0;
+        for (int j = 0; j < nd; ++j) v += shape[j] * x[k * ND + (long long)kc * nd + j];
+        loc[k] += w * v;
+      }
+    }
+    const double psi = c->ops[c->op_of[kc]].int_psi;
+    for (int k = 0; k < neq; ++k) {
+      const double ex = loc[k] / psi;
+      maxF[k] = std::fabs(ume[k]) > maxF[k] ? std::fabs(ume[k]) : maxF[k];
+      sumD[k] += std::fabs(ume[k] - ex);
+    }
+  }
+  const double Ck = 0.03, eps = 1e-6;
+  for (int k = 0; k < neq; ++k)
+    val[k] = (std::fabs(maxF[k]) < eps && std::fabs(sumD[k]) < eps)
+                 ? 1.0
+                 : std::min(1.0, Ck * maxF[k] / (sumD[k] + eps));
+}
+
 // LimiterMultiplier::linearize, limiter_multiplier.cpp:101-178: every
 // variable becomes mean + (reference-space gradient at the centre) . (x_j - c)
 // at the points of the element rule of order p+1 (the nodes for p = 1, the
@@ -1433,6 +1487,9 @@ int ref_limit(ref_ctx* c, double* x) {
     } else if (c->ind == 1) {  // IndicatorEverywhere
       for (int k = 0; k < neq; ++k) elind[k] = 0.0;
       minValue = 0.0;
+    } else if (c->ind == 3) {  // IndicatorShu (FinDiff only)
+      shu_indicator(c, x, mean, e, elind);
+      minValue = 1.0;
     } else {
       double mI[5], MI[5], um[5];
       for (int k = 0; k < neq; ++k) {

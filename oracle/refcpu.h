@@ -67,7 +67,8 @@ int ref_set_bc(ref_ctx* c, int attr, int type, const double* state);
 /* computeRightState of attribute attr's boundary condition for the state s1
  * and the unit outward normal nor (test hook). */
 int ref_right_state(ref_ctx* c, int attr, const double* s1, const double* nor, double* s2);
-/* limiter: 0 FinDiff, 1 Multi; indicator: 0 Nowhere, 1 Everywhere, 2 BJ family;
+/* limiter: 0 FinDiff, 1 Multi; indicator: 0 Nowhere, 1 Everywhere, 2 BJ family,
+ * 3 Shu (FinDiff only: with Multi the reference reads a factor Shu never sets);
  * function: 0 BJ, 1 Venkatakrishnan, 2 Michalak; quirks bit0: apply the
  * multiplier once instead of nd times; bit1: the "linearize" option of the
  * Multi limiter (quads and hexes of order 1; a no-op on triangles). */

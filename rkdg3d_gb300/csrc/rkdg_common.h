@@ -10,6 +10,7 @@
 #define RKDG_MAX_NQL 4    // limiter face rule (order 2): 2 (segment) or 2x2
 #define RKDG_MAX_NV 8
 #define RKDG_MAX_PERM 64
+#define RKDG_MAX_NQS 27   // Shu indicator rule (hex Q2: 3x3x3)
 #define RKDG_HEX_MAX_PERM 8  // orientations of a square face
 #define RKDG_MAX_BC 32
 
@@ -70,6 +71,17 @@ struct RefTables {
   double dcen[RKDG_MAX_ND][3];
   double xlin[RKDG_MAX_ND][3];
   int lin_ok;
+  // Shu indicator: the element rule of order p + OrderW (the extrapolated
+  // averages of averager.cpp:154-273) and what evaluating the nodal basis at
+  // arbitrary reference points needs: the 1D GL nodes (tensor elements) or
+  // the monomial expansion phi_j = sum_m tcoef[m][j] x^tmono[m][0] y^tmono[m][1]
+  // (triangles)
+  int nqs;
+  double xs[RKDG_MAX_NQS][3];
+  double ws[RKDG_MAX_NQS];
+  double x1n[8];
+  int tmono[RKDG_MAX_ND][2];
+  double tcoef[RKDG_MAX_ND][RKDG_MAX_ND];
 };
 
 // Boundary condition slot.
@@ -168,6 +180,7 @@ struct LimParams {
   long long ndofs;
   const int* fnbr;
   const RefTables* tab;
+  const double* eaff;   // [dim*dim + dim][ne]: J (row i, col r) and vertex 0
   const double* means;  // [neq][ne]
   double gamma, covolume;
   int limiter, indicator, function, last_hope, quirks;

@@ -343,6 +343,177 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
 }
 
 // ---- limiter ------------------------------------------------------------------
+// Nodal basis of the reference element at an arbitrary reference point (the
+// tensor GL Lagrange basis, or the triangle basis from its monomial expansion).
+template <int G, int P>
+__device__ __forceinline__ void basis_at(const RefTables* T, const double* xi,
+                                         double (&phi)[El<G, P>::ND]) {
+  using E = El<G, P>;
+  constexpr int DIM = E::DIM, ND = E::ND;
+  if constexpr (G == 2) {
+    double px[P + 1], py[P + 1];
+    px[0] = py[0] = 1.0;
+#pragma unroll
+    for (int a = 1; a <= P; ++a) {
+      px[a] = px[a - 1] * xi[0];
+      py[a] = py[a - 1] * xi[1];
+    }
+#pragma unroll
+    for (int j = 0; j < ND; ++j) phi[j] = 0.0;
+#pragma unroll
+    for (int m = 0; m < ND; ++m) {
+      const double mv = px[T->tmono[m][0]] * py[T->tmono[m][1]];
+#pragma unroll
+      for (int j = 0; j < ND; ++j) phi[j] += T->tcoef[m][j] * mv;
+    }
+  } else {
+    constexpr int N1 = P + 1;
+    double l[DIM][N1];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+      for (int i = 0; i < N1; ++i) {
+        double v = 1.0;
+#pragma unroll
+        for (int m = 0; m < N1; ++m)
+          if (m != i) v *= (xi[d] - T->x1n[m]) / (T->x1n[i] - T->x1n[m]);
+        l[d][i] = v;
+      }
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      double v = l[0][j % N1] * l[1][(j / N1) % N1];
+      if constexpr (DIM == 3) v *= l[2][j / (N1 * N1)];
+      phi[j] = v;
+    }
+  }
+}
+
+// IndicatorShu::checkDiscontinuity (indicator_shu.cpp:13-74) for element e:
+// for every cell k of the stencil (e, then its face neighbours) the average
+// over e of k's polynomial extrapolated there (Averager::
+// computeStencilExtrapAverages, averager.cpp:154-273: the element rule of
+// order p + OrderW on e mapped into k's reference frame), and
+//   value = min(1, Ck max|mean_e| / (sum_k |mean_e - extrap_k| + eps)),
+// Ck = 0.03, eps = 1e-6, or 1 where both are below eps.  The maximum runs over
+// the stencil but reads e's own mean every time, as the reference does.
+template <int G, int P, bool DS, typename R>
+__device__ __forceinline__ void shu_indicator(const LimParams& prm, const R* __restrict__ u,
+                                              const float* __restrict__ ulo, int e,
+                                              R (&val)[El<G, P>::NEQ]) {
+  using E = El<G, P>;
+  constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NFPE = E::NFPE;
+  const RefTables* T = prm.tab;
+  const int ne = prm.ne;
+  const long long NDa = prm.ndofs;
+  const double* ea = prm.eaff;
+  double Je[DIM][DIM], xe[DIM], ume[NEQ], sum[NEQ];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) Je[i][r] = ea[(long long)(i * DIM + r) * ne + e];
+    xe[i] = ea[(long long)(DIM * DIM + i) * ne + e];
+  }
+#pragma unroll
+  for (int k = 0; k < NEQ; ++k) {
+    ume[k] = prm.means[(long long)k * ne + e];
+    sum[k] = 0.0;
+  }
+  double wsum = 0.0;
+  for (int q = 0; q < T->nqs; ++q) wsum += T->ws[q];
+  for (int s = -1; s < NFPE; ++s) {
+    const int kc = s < 0 ? e : prm.fnbr[s * ne + e];
+    if (kc < 0) continue;  // boundary faces are not in the stencil
+    // e's reference point xi -> k's reference point A xi + b
+    double A[DIM][DIM], b[DIM];
+    if (kc == e) {
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) {
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) A[i][r] = i == r ? 1.0 : 0.0;
+        b[i] = 0.0;
+      }
+    } else {
+      double Jk[DIM][DIM], Ki[DIM][DIM], dx[DIM];
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) {
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) Jk[i][r] = ea[(long long)(i * DIM + r) * ne + kc];
+        dx[i] = xe[i] - ea[(long long)(DIM * DIM + i) * ne + kc];
+      }
+      if constexpr (DIM == 2) {
+        const double id = 1.0 / (Jk[0][0] * Jk[1][1] - Jk[0][1] * Jk[1][0]);
+        Ki[0][0] = Jk[1][1] * id;
+        Ki[0][1] = -Jk[0][1] * id;
+        Ki[1][0] = -Jk[1][0] * id;
+        Ki[1][1] = Jk[0][0] * id;
+      } else {
+        const double c00 = Jk[1][1] * Jk[2][2] - Jk[1][2] * Jk[2][1];
+        const double c01 = Jk[0][2] * Jk[2][1] - Jk[0][1] * Jk[2][2];
+        const double c02 = Jk[0][1] * Jk[1][2] - Jk[0][2] * Jk[1][1];
+        const double id = 1.0 / (Jk[0][0] * c00 + Jk[1][0] * c01 + Jk[2][0] * c02);
+        Ki[0][0] = c00 * id;
+        Ki[0][1] = c01 * id;
+        Ki[0][2] = c02 * id;
+        Ki[1][0] = (Jk[1][2] * Jk[2][0] - Jk[1][0] * Jk[2][2]) * id;
+        Ki[1][1] = (Jk[0][0] * Jk[2][2] - Jk[0][2] * Jk[2][0]) * id;
+        Ki[1][2] = (Jk[0][2] * Jk[1][0] - Jk[0][0] * Jk[1][2]) * id;
+        Ki[2][0] = (Jk[1][0] * Jk[2][1] - Jk[1][1] * Jk[2][0]) * id;
+        Ki[2][1] = (Jk[0][1] * Jk[2][0] - Jk[0][0] * Jk[2][1]) * id;
+        Ki[2][2] = (Jk[0][0] * Jk[1][1] - Jk[0][1] * Jk[1][0]) * id;
+      }
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) {
+        b[i] = 0.0;
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) {
+          double a = 0.0;
+#pragma unroll
+          for (int m = 0; m < DIM; ++m) a += Ki[i][m] * Je[m][r];
+          A[i][r] = a;
+          b[i] += Ki[i][r] * dx[r];
+        }
+      }
+    }
+    // W_j = mean over e of k's basis function j
+    double W[ND];
+#pragma unroll
+    for (int j = 0; j < ND; ++j) W[j] = 0.0;
+    for (int q = 0; q < T->nqs; ++q) {
+      double xk[DIM];
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) {
+        double v = b[i];
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) v += A[i][r] * T->xs[q][r];
+        xk[i] = v;
+      }
+      double phi[ND];
+      basis_at<G, P>(T, xk, phi);
+      const double wq = T->ws[q] / wsum;
+#pragma unroll
+      for (int j = 0; j < ND; ++j) W[j] += wq * phi[j];
+    }
+#pragma unroll
+    for (int k = 0; k < NEQ; ++k) {
+      double ex = 0.0;
+#pragma unroll
+      for (int j = 0; j < ND; ++j) {
+        const long long idx = k * NDa + (long long)kc * ND + j;
+        double v = (double)u[idx];
+        if constexpr (DS) v += (double)ulo[idx];
+        ex += v * W[j];
+      }
+      sum[k] += fabs(ume[k] - ex);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NEQ; ++k) {
+    const double mx = fabs(ume[k]);
+    const double v = (mx < 1e-6 && sum[k] < 1e-6) ? 1.0 : fmin(1.0, 0.03 * mx / (sum[k] + 1e-6));
+    val[k] = (R)v;
+  }
+}
+
 // Limiter::update for one element (limiter.cpp:22-94): stencil = the element
 // and its face neighbours (ElementToElementTable, limiter.cpp:115-123), the
 // BJ-family indicator at the order-2 points of its interior faces
@@ -406,6 +577,9 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
     minValue = R(0);
 #pragma unroll
     for (int k = 0; k < NEQ; ++k) elind[k] = R(0);
+  } else if (prm.indicator == 3) {
+    shu_indicator<G, P, DS>(prm, u, ulo, e, elind);
+    minValue = R(1);  // FinDiff only: the Multi limiter is rejected with Shu
   } else {
     R mI[NEQ], MI[NEQ], yMin[NEQ];
 #pragma unroll

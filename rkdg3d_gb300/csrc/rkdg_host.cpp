@@ -65,6 +65,8 @@ struct rkdg_ctx {
   double* d_fgeo64 = nullptr;
   float* d_fgeo32 = nullptr;
   double* d_egeo64 = nullptr;
+  double* d_eaff = nullptr;  // [dim*dim + dim][ne] J and vertex 0 (Shu indicator)
+  std::vector<double> h_eaff;
   float* d_egeo32 = nullptr;
   double* d_wdet = nullptr;
   unsigned long long* d_mcs = nullptr;  // 8 slots
@@ -144,6 +146,7 @@ void free_mesh(rkdg_ctx* c) {
   dfree(c->d_egeo64);
   dfree(c->d_egeo32);
   dfree(c->d_wdet);
+  dfree(c->d_eaff);
   dfree(c->d_means);
   dfree(c->d_partial);
   for (auto& p : c->d_k64) dfree(p);
@@ -317,6 +320,7 @@ LimParams lim_params(rkdg_ctx* c) {
   L.ndofs = c->ndofs;
   L.fnbr = c->d_fnbr;
   L.tab = c->d_tab;
+  L.eaff = c->d_eaff;
   L.means = c->d_means;
   L.gamma = c->gamma;
   L.covolume = c->cov;
@@ -659,8 +663,12 @@ int rkdg_set_bc(rkdg_ctx* c, int attr, int type, const double* state) {
 int rkdg_set_limiter(rkdg_ctx* c, int limiter, int indicator, int function, int last_hope,
                      int quirk_flags) {
   if (!c) return RKDG_ERR_INVALID;
-  if (limiter < 0 || limiter > 1 || indicator < 0 || indicator > 2 || function < 0 || function > 2)
+  if (limiter < 0 || limiter > 1 || indicator < 0 || indicator > 3 || function < 0 || function > 2)
     return fail(c, RKDG_ERR_INVALID, "invalid limiter configuration");
+  if (indicator == RKDG_IND_SHU && limiter == RKDG_LIM_MULTI)
+    return fail(c, RKDG_ERR_UNSUPPORTED,
+                "Shu indicator with the Multi limiter: the reference multiplies by a cell "
+                "factor the Shu indicator never sets");
   if ((quirk_flags & RKDG_LIMITER_LINEARIZE) && limiter == RKDG_LIM_MULTI && c->has_mesh &&
       c->geom != RKDG_GEOM_TRIANGLE && !c->tab.lin_ok)
     return fail(c, RKDG_ERR_UNSUPPORTED,
@@ -762,6 +770,7 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
   c->ndofs = (long long)ne * nd;
   // ---- element geometry (affine elements) ----
   c->h_egeo.assign((size_t)(dim * dim + 1) * ne, 0.0);
+  c->h_eaff.assign((size_t)(dim * dim + dim) * ne, 0.0);
   c->h_wdet.assign(ne, 0.0);
   c->h_ehmin.assign(ne, 0.0);
   c->h_nodes.assign((size_t)dim * c->ndofs, 0.0);
@@ -812,6 +821,8 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     for (int rd = 0; rd < dim * dim; ++rd) c->h_egeo[(size_t)rd * ne + e] = adj[rd];
     c->h_egeo[(size_t)(dim * dim) * ne + e] = 1.0 / det;
     c->h_wdet[e] = det * refvol;
+    for (int rd = 0; rd < dim * dim; ++rd) c->h_eaff[(size_t)rd * ne + e] = J[rd];
+    for (int i = 0; i < dim; ++i) c->h_eaff[(size_t)(dim * dim + i) * ne + e] = X[i];
     double Jp[9];
     std::memcpy(Jp, J, sizeof Jp);
     if (geom == 2) {  // relative to the equilateral reference triangle
@@ -998,6 +1009,9 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
   CUDA_TRY(c, cudaMemcpy(c->d_egeo32, e32.data(), e32.size() * sizeof(float), cudaMemcpyHostToDevice));
   CUDA_TRY(c, dalloc(c->d_wdet, (size_t)ne));
   CUDA_TRY(c, cudaMemcpy(c->d_wdet, c->h_wdet.data(), ne * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, dalloc(c->d_eaff, c->h_eaff.size()));
+  CUDA_TRY(c, cudaMemcpy(c->d_eaff, c->h_eaff.data(), c->h_eaff.size() * sizeof(double),
+                         cudaMemcpyHostToDevice));
   CUDA_TRY(c, dalloc(c->d_means, (size_t)neq * ne));
   CUDA_TRY(c, dalloc(c->d_partial, (size_t)neq * 1024));
   c->has_mesh = true;
@@ -1500,6 +1514,8 @@ int adjoint_ready(rkdg_ctx* c) {
   if ((c->quirks & RKDG_LIMITER_LINEARIZE) && c->limiter_active() && c->lim == RKDG_LIM_MULTI &&
       c->geom != RKDG_GEOM_TRIANGLE)
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for the linearize limiter option");
+  if (c->ind == RKDG_IND_SHU && c->limiter_active())
+    return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for the Shu indicator");
   return RKDG_OK;
 }
 

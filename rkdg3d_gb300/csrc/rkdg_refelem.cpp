@@ -332,6 +332,23 @@ bool build_ref_tables(int geom, int p, RefTables& T, std::vector<FacePoint>* fpt
     for (int j = 0; j < nd && j < r.n; ++j)
       for (int d = 0; d < dim; ++d) T.xlin[j][d] = r.x[j * dim + d];
   }
+  // Shu indicator: extrapolation rule and basis data
+  {
+    Pts r = elem_rule(geom, p + orderW);
+    if (r.n > RKDG_MAX_NQS) return false;
+    T.nqs = r.n;
+    for (int q = 0; q < r.n; ++q) {
+      for (int d = 0; d < dim; ++d) T.xs[q][d] = r.x[q * dim + d];
+      T.ws[q] = r.w[q];
+    }
+    for (int i = 0; i < (int)B.x1.size() && i < 8; ++i) T.x1n[i] = B.x1[i];
+    if (geom == 2)
+      for (int m = 0; m < nd; ++m) {
+        T.tmono[m][0] = B.ex[m];
+        T.tmono[m][1] = B.ey[m];
+        for (int j = 0; j < nd; ++j) T.tcoef[m][j] = B.cinv[m * nd + j];
+      }
+  }
   // cell-mean weights
   {
     Pts r = elem_rule(geom, p + orderW);

@@ -38,7 +38,7 @@ BC_SLIP, BC_OPEN, BC_FIXED_ROTATED, BC_SUPERSONIC_INLET, BC_WALL = 0, 1, 2, 3, 4
 (BC_SUBSONIC_INLET, BC_SUBSONIC_INLET_TOTAL_PRESSURE, BC_SUBSONIC_INLET_FIXED_PRESSURE,
  BC_FIXED_PRESSURE_OUTLET, BC_TOTAL_PRESSURE_OUTLET) = 5, 6, 7, 8, 9
 LIM_FINDIFF, LIM_MULTI = 0, 1
-IND_NOWHERE, IND_EVERYWHERE, IND_BJ = 0, 1, 2
+IND_NOWHERE, IND_EVERYWHERE, IND_BJ, IND_SHU = 0, 1, 2, 3
 FUN_BJ, FUN_VENKATAKRISHNAN, FUN_MICHALAK = 0, 1, 2
 QUIRK_MULTIPLIER_ONCE = 1
 FP64, FP32_BULK = 0, 1

@@ -300,3 +300,36 @@ def test_limiter_linearize_rejects_order_2(cuda):
     ctx = Context(case.mesh, case.order, device=0)
     with pytest.raises(RkdgError):
         ctx.set_limiter(LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 2)
+
+
+@pytest.mark.parametrize("geom,order", [(M.GEOM_SQUARE, 1), (M.GEOM_SQUARE, 2),
+                                        (M.GEOM_TRIANGLE, 1), (M.GEOM_TRIANGLE, 2),
+                                        (M.GEOM_CUBE, 1), (M.GEOM_CUBE, 2)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_limiter_shu_parity(cuda, geom, order, prec):
+    """Shu indicator + FinDiff (indicator_shu.cpp:13-74 with the extrapolated
+    averages of averager.cpp:154-273) against the oracle: FP64 to 1e-12; the
+    FP32-bulk limiter (float-pair state) takes the same decisions on this
+    state."""
+    from rkdg3d_gb300.solver import IND_SHU
+    case = (walled_case(geom, 4, order, RS_HLLC, bc=BC_SLIP) if geom != M.GEOM_CUBE
+            else periodic_case(geom, 3, order, RS_HLLC))
+    case.limiter = (LIM_FINDIFF, IND_SHU, FUN_MICHALAK, 1, 0)
+    ctx, orc = pair(case)
+    if prec:
+        ctx.set_precision(1)
+    X = orc.node_coords()
+    x = random_state(X, seed=6, amp=0.1) * np.tile(np.where(X[0] < 0.4, 1.0, 0.4), orc.neq)
+    xl_ref = orc.limit(x)
+    assert rel_l1(xl_ref, x) > 1e-4  # some cells fell back to their means
+    xd = dev(x)
+    ctx.limit(xd)
+    assert rel_l1(xd.cpu().numpy(), xl_ref) < (1e-12 if prec == 0 else 1e-6)
+
+
+def test_shu_with_multi_is_rejected(cuda):
+    from rkdg3d_gb300.solver import IND_SHU, RkdgError
+    case = periodic_case(M.GEOM_SQUARE, 4, 1, RS_HLLC)
+    ctx = Context(case.mesh, case.order, device=0)
+    with pytest.raises(RkdgError):
+        ctx.set_limiter(LIM_MULTI, IND_SHU, FUN_MICHALAK, 1, 0)

@@ -269,3 +269,25 @@ def test_linearize_keeps_means_and_is_linear():
     assert np.allclose(v[..., 0] - v[..., 1] - v[..., 2] + v[..., 3], 0.0, atol=1e-13)
     orc.set_limiter(1, 0, 2, 0, 0)
     assert not np.allclose(orc.limit(x), y)
+
+
+@pytest.mark.parametrize("geom,order", [(M.GEOM_SQUARE, 1), (M.GEOM_SQUARE, 2),
+                                        (M.GEOM_TRIANGLE, 1), (M.GEOM_TRIANGLE, 2),
+                                        (M.GEOM_CUBE, 1)])
+def test_shu_indicator_known_answers(geom, order):
+    """Shu indicator + FinDiff: a globally linear state extrapolates exactly
+    (every stencil difference vanishes) and is left alone; a jump makes the
+    cells beside it fall back to their means while the means stay."""
+    case = walled_case(geom, 4, order, 0, bc=BC_SLIP)
+    orc = Oracle(case.mesh, case.order)
+    cases.configure_oracle(case, orc)
+    orc.set_limiter(0, 3, 2, 1, 0)
+    X = orc.node_coords()
+    lin = cases.conservative([1.0 + 0.1 * X[0] + 0.05 * X[1], *[0.02 * X[0] for _ in range(X.shape[0])],
+                              1.0 + 0.03 * X[1]], 1.4, 0.0)
+    assert np.allclose(orc.limit(lin), lin, rtol=0, atol=1e-14)
+    jump = cases.conservative([np.where(X[0] < 0.4, 1.0, 0.2), *[0 * X[0] for _ in range(X.shape[0])],
+                               np.where(X[0] < 0.4, 1.0, 0.1)], 1.4, 0.0)
+    y = orc.limit(jump)
+    assert not np.allclose(y, jump)
+    assert np.allclose(orc.means(y), orc.means(jump), rtol=0, atol=1e-13)
