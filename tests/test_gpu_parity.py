@@ -105,8 +105,13 @@ BC_PARAMS = {BC_SUBSONIC_INLET_TOTAL_PRESSURE: [1.2, 1.1], BC_SUBSONIC_INLET_FIX
 def test_rhs_walls(cuda, geom, order, n, bc, rs, avg):
     case = walled_case(geom, n, order, rs, avg, covolume=0.005, bc=bc)
     dim = case.dim
-    if bc in (BC_FIXED_ROTATED, BC_SUPERSONIC_INLET, BC_SUBSONIC_INLET):
+    if bc in (BC_FIXED_ROTATED, BC_SUPERSONIC_INLET):
         st = cases.supersonic_inlet_state(1.1, 0.3, -0.2, 0.1, 0.9, 1.4, dim)
+        case.bcs = [(a, bc, st) for a, _, _ in case.bcs]
+    elif bc == BC_SUBSONIC_INLET:
+        # a subsonic inflow state in the face frame (2 * fixed - own stays physical)
+        vel = [np.array([-0.1]), np.array([0.05])] + ([np.array([0.02])] if dim == 3 else [])
+        st = cases.conservative([np.array([1.0]), *vel, np.array([1.0])], 1.4, 0.0).ravel()
         case.bcs = [(a, bc, st) for a, _, _ in case.bcs]
     elif bc in BC_PARAMS:
         case.bcs = [(a, bc, BC_PARAMS[bc]) for a, _, _ in case.bcs]
