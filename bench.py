@@ -349,6 +349,142 @@ def run_ours(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def run_config(args, local):
+    """The other configurations of the workload set, one JSON line each (the
+    headline line is the C2 pulse of run_ours):
+      c1  Sod 200x4 Q1, HLLC + Einfeldt, BJ limiter, SSP-RK3 CFL 0.3 to t = 0.2
+      c3  double Mach reflection, 524,288 jittered P1 triangles, HLL + TRRS,
+          Venkatakrishnan, SSP-RK3 CFL 0.25 (the first --config-steps steps)
+      c4  256 batched Riemann problems on N x 4 strips, one graph launch, to t = 0.15
+      c5  adjoint: 32^3 Q1 Gaussian pulses, HLLC + Venkatakrishnan, 200 fixed-dt
+          steps forward, then the checkpointed adjoint run (every 20 steps)
+    FP64 and FP32-bulk runs of the same workload with the density / energy error
+    of the latter against the former, and the FP64 oracle on a bounded sample."""
+    import torch
+    from oracle import refcpu
+    from rkdg3d_gb300 import cases
+    from rkdg3d_gb300.solver import FP32_BULK, FP64, Context
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    threads = os.cpu_count() or 1
+    w = args.config
+
+    def timed(fn):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize(dev)
+        return r, time.perf_counter() - t0
+
+    def context(case, prec):
+        ctx = Context(case.mesh, case.order, device=local, precision=prec)
+        cases.configure_context(case, ctx)
+        ctx.set_stream(stream.cuda_stream)
+        return ctx
+
+    def errors(a, b, nd):
+        ra, rb, Ea, Eb = a[:nd], b[:nd], a[-nd:], b[-nd:]
+        return {"rho_rel_l1": float(np.abs(ra - rb).sum() / np.abs(rb).sum()),
+                "rho_linf": float(np.abs(ra - rb).max()),
+                "E_rel_l1": float(np.abs(Ea - Eb).sum() / np.abs(Eb).sum()),
+                "E_linf": float(np.abs(Ea - Eb).max())}
+
+    line = {"config": w, "unit": UNIT, "data": "synthetic", "n_gpus": 1}
+    if w in ("c1", "c3"):
+        case = cases.sod() if w == "c1" else cases.double_mach()
+        kw = {} if w == "c1" else {"max_steps": args.config_steps}
+        out = {}
+        for name, prec in (("fp64", FP64), ("fp32_bulk", FP32_BULK)):
+            ctx = context(case, prec)
+            x0 = torch.tensor(cases.project(case, ctx.node_coords()), dtype=torch.float64, device=dev)
+            x = x0.clone()
+            ctx.run(x, case.t_end, case.cfl, max_steps=2)  # warm-up
+            x = x0.clone()
+            info, sec = timed(lambda: ctx.run(x, case.t_end, case.cfl, **kw))
+            out[name] = (x.cpu().numpy(), info, sec)
+            line[name] = {"value": ctx.n * STAGES * info["steps"] / sec, "steps": info["steps"],
+                          "ms_per_step": 1e3 * sec / info["steps"], "t": info["t"]}
+            n, nd = ctx.n, ctx.ndofs
+        line["unknowns"] = n
+        line["error_fp32_bulk_vs_fp64"] = errors(out["fp32_bulk"][0], out["fp64"][0], nd)
+        orc = refcpu.Oracle(case.mesh, case.order)
+        cases.configure_oracle(case, orc)
+        xo = cases.project(case, orc.node_coords())
+        ksteps = out["fp64"][1]["steps"] if w == "c1" else 2
+        refcpu.set_threads(threads)
+        t0 = time.perf_counter()
+        orc.run(xo, case.t_end, case.cfl, max_steps=ksteps)
+        sec = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": orc.n * STAGES * ksteps / sec, "cores": threads,
+                                "kind": "port", "sample": f"{ksteps} RK steps, FP64 oracle"}
+    elif w == "c4":
+        bc = cases.batched_riemann()
+        for name, prec in (("fp64", FP64), ("fp32_bulk", FP32_BULK)):
+            ctx = Context(bc.mesh, bc.order, device=local, precision=prec)
+            cases.configure_batch(bc, ctx)
+            ctx.set_stream(stream.cuda_stream)
+            x0 = torch.tensor(bc.project(ctx.node_coords()), dtype=torch.float64, device=dev)
+            x = x0.clone()
+            ctx.batch_run(x, bc.t_end, bc.cfl, max_steps=2)  # warm-up (graph build)
+            x = x0.clone()
+            info, sec = timed(lambda: ctx.batch_run(x, bc.t_end, bc.cfl))
+            steps = np.abs(np.asarray(info["steps"]))
+            per_problem = np.diff(bc.offsets) * 4 * 4  # Q1 quads: 4 nodes x 4 variables
+            units = float((per_problem * steps).sum()) * STAGES
+            line[name] = {"value": units / sec, "seconds": sec, "problems": len(steps),
+                          "failed": int((np.asarray(info["steps"]) < 0).sum()),
+                          "max_steps": int(steps.max())}
+            if name == "fp64":
+                a64 = x.cpu().numpy()
+                nd = ctx.ndofs
+            else:
+                line["error_fp32_bulk_vs_fp64"] = errors(x.cpu().numpy(), a64, nd)
+        line["unknowns"] = int(ctx.n)
+        small = int(np.argmin(np.diff(bc.offsets)))
+        c = bc.cases[small]
+        orc = refcpu.Oracle(c.mesh, c.order)
+        cases.configure_oracle(c, orc)
+        refcpu.set_threads(threads)
+        t0 = time.perf_counter()
+        try:
+            _, ir = orc.run(cases.project(c, orc.node_coords()), c.t_end, c.cfl)
+            sec = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": orc.n * STAGES * ir["steps"] / sec, "cores": threads,
+                                    "kind": "port",
+                                    "sample": f"the smallest problem ({np.diff(bc.offsets)[small]} "
+                                              "elements) run alone, FP64 oracle"}
+        except refcpu.OracleError as ex:
+            line["cpu_baseline"] = {"unavailable": str(ex)[:80]}
+    elif w == "c5":
+        case = cases.gaussian_pulses(n=32, seed=0)
+        ctx = context(case, FP64)
+        x0 = torch.tensor(cases.project(case, ctx.node_coords()), dtype=torch.float64, device=dev)
+        dt = case.cfl * ctx.hmin() / ctx.face_speed(x0) / (2 * case.order + 1)
+        x = x0.clone()
+        ctx.run(x, 1e30, dt0=dt, dt_mode=2, max_steps=2)
+        x = x0.clone()
+        _, sec_f = timed(lambda: ctx.run(x, 1e30, dt0=dt, dt_mode=2, max_steps=200))
+        xbar = torch.zeros_like(x)
+        xbar[:ctx.ndofs] = x[:ctx.ndofs] - x0[:ctx.ndofs]
+        xT = torch.empty_like(x)
+        _, sec_a = timed(lambda: ctx.adjoint_run(x0, 200, dt, 20, xbar, xT))
+        line["fp64"] = {"value": ctx.n * STAGES * 200 / sec_f, "forward_seconds": sec_f,
+                        "adjoint_seconds": sec_a, "adjoint_over_forward": sec_a / sec_f}
+        line["unknowns"] = ctx.n
+        orc = refcpu.Oracle(case.mesh, case.order)
+        cases.configure_oracle(case, orc)
+        refcpu.set_threads(threads)
+        xo = cases.project(case, orc.node_coords())
+        t0 = time.perf_counter()
+        orc.run(xo, 1e30, dt0=dt, dt_mode=2, max_steps=2)
+        sec = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": orc.n * STAGES * 2 / sec, "cores": threads,
+                                "kind": "port", "sample": "2 RK steps, FP64 oracle"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,6 +497,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--hex-kernel", type=int, default=0,
                     help="RKDG_TUNE_HEX_KERNEL of the FP32-bulk context (0: library default)")
+    ap.add_argument("--config", default="c2", choices=["c2", "c1", "c3", "c4", "c5"],
+                    help="c2: the headline pulse (default); c1/c3/c4/c5: the other "
+                         "configurations, one JSON line each")
+    ap.add_argument("--config-steps", type=int, default=200,
+                    help="RK steps of the c3 runs (first steps of the t = 0.2 run)")
     ap.add_argument("--traffic-per-launch", type=float, default=None,
                     help="DRAM bytes per stage launch from an ncu capture (profiles/)")
     args = ap.parse_args()
@@ -369,6 +510,9 @@ def main():
     rank, world, local = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.config != "c2":
+        if rank == 0:
+            run_config(args, local)
     else:
         run_ours(args, rank, world, local)
     if world > 1:
