@@ -51,7 +51,10 @@ def _headers_digest() -> str:
 
 def _compile(nvcc: str, src: str, flags) -> str:
     obj = os.path.join(OBJDIR, src + ".o")
-    cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+    # -ftz=true: FP32 arithmetic flushes subnormals (below 1.2e-38) to zero,
+    # which drops the subnormal fix-ups of the reciprocal / square-root
+    # approximations; the FP32-bulk path never carries values that small
+    cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-ftz=true", "-Xcompiler", "-fPIC",
            "-I", INCLUDE, "-I", CSRC, *flags, "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
