@@ -52,9 +52,9 @@ def workload_config(case, n_elem_side):
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element per
 # stage launch of k_rhs_hex_team<2,float>: mean of the three stage launches of
-# one RK step captured with ncu on the 48^3 pulse (330.0 MB / 110,592
+# one RK step captured with ncu on the 48^3 pulse (329.4 MB / 110,592
 # elements); traffic scales with the element count.
-TRAFFIC_BYTES_PER_ELEMENT_LAUNCH = 2984.0
+TRAFFIC_BYTES_PER_ELEMENT_LAUNCH = 2978.0
 
 
 def algorithmic_bytes_per_step(N, ne, precision):
