@@ -338,3 +338,55 @@ def test_shu_with_multi_is_rejected(cuda):
     ctx = Context(case.mesh, case.order, device=0)
     with pytest.raises(RkdgError):
         ctx.set_limiter(LIM_MULTI, IND_SHU, FUN_MICHALAK, 1, 0)
+
+
+@pytest.mark.parametrize("geom,order,prec,variant", [(M.GEOM_SQUARE, 1, 0, 0), (M.GEOM_TRIANGLE, 2, 1, 0),
+                                                     (M.GEOM_CUBE, 2, 1, 0), (M.GEOM_CUBE, 2, 0, 0),
+                                                     (M.GEOM_CUBE, 1, 0, 0), (M.GEOM_CUBE, 1, 1, 2)])
+def test_nonphysical_state_is_reported(cuda, geom, order, prec, variant):
+    """Where the reference prints the elements and exits on a non-physical
+    state (face_integrator.cpp:214-218), every kernel path returns
+    RKDG_ERR_UNPHYSICAL naming an element of that face; the context stays
+    usable afterwards."""
+    from rkdg3d_gb300.solver import TUNE_HEX_KERNEL, UnphysicalStateError
+    from oracle.refcpu import OracleError
+    case = (walled_case(geom, 4, order, RS_HLLC, bc=BC_SLIP) if geom == M.GEOM_TRIANGLE
+            else periodic_case(geom, 3 if geom == M.GEOM_CUBE else 4, order, RS_HLLC))
+    ctx, orc = pair(case)
+    if prec:
+        ctx.set_precision(1)
+    if variant:
+        ctx.set_tuning(TUNE_HEX_KERNEL, variant)
+    x = random_state(orc.node_coords(), seed=3)
+    bad = x.copy()
+    e, nd, n = 5, ctx.nd, ctx.ndofs
+    bad[(ctx.neq - 1) * n + e * nd:(ctx.neq - 1) * n + (e + 1) * nd] = -1.0  # negative energy
+    with pytest.raises(OracleError):
+        orc.rhs(bad)
+    y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    with pytest.raises(UnphysicalStateError) as ei:
+        ctx.rhs(dev(bad), y)
+    neigh = set(np.flatnonzero([e in row for row in _face_neighbours(ctx.mesh)]).tolist()) | {e}
+    assert ei.value.where in neigh, (ei.value.where, neigh)
+    m = ctx.rhs(dev(x), y)  # still usable
+    y_ref, m_ref = orc.rhs(x)
+    tol = RHS_TOL if prec == 0 else 1e-5
+    assert rel_l1(y.cpu().numpy(), y_ref) < tol
+
+
+def _face_neighbours(mesh):
+    """Element -> elements sharing a vertex set of a face (periodic seams share ids)."""
+    from collections import defaultdict
+    geom = mesh.geom
+    faces = {M.GEOM_TRIANGLE: [(0, 1), (1, 2), (2, 0)], M.GEOM_SQUARE: [(0, 1), (1, 2), (2, 3), (3, 0)],
+             M.GEOM_CUBE: [(0, 1, 2, 3), (0, 1, 5, 4), (1, 2, 6, 5), (2, 3, 7, 6), (3, 0, 4, 7),
+                           (4, 5, 6, 7)]}[geom]
+    owners = defaultdict(list)
+    for e, ev in enumerate(mesh.elem_vertices):
+        for f in faces:
+            owners[tuple(sorted(ev[list(f)]))].append(e)
+    rows = [set() for _ in range(mesh.num_elements)]
+    for els in owners.values():
+        for a in els:
+            rows[a].update(els)
+    return rows
