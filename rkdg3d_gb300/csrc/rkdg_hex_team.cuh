@@ -134,6 +134,34 @@ __device__ __forceinline__ void team_contract_g_any(int lf, const R* __restrict_
 template <int P, int ST, typename R>
 __device__ __forceinline__ void team_interp(const R (&v)[(P + 1) * (P + 1)], const R* l1d, R* dst) {
   constexpr int N1 = P + 1, NQ1 = P + 2;
+  if constexpr (std::is_same<R, float>::value && NQ1 % 2 == 0) {
+    // packed FP32 (two face-point rows per instruction); each component is
+    // the same fused chain as the scalar form below, so results are identical
+    float2 w[NQ1 / 2][N1];
+#pragma unroll
+    for (int pa = 0; pa < NQ1 / 2; ++pa)
+#pragma unroll
+      for (int i1 = 0; i1 < N1; ++i1) {
+        float2 s = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int i0 = 0; i0 < N1; ++i0)
+          s = __ffma2_rn(make_float2(l1d[(2 * pa) * N1 + i0], l1d[(2 * pa + 1) * N1 + i0]),
+                         make_float2(v[i0 * N1 + i1], v[i0 * N1 + i1]), s);
+        w[pa][i1] = s;
+      }
+#pragma unroll
+    for (int b = 0; b < NQ1; ++b)
+#pragma unroll
+      for (int pa = 0; pa < NQ1 / 2; ++pa) {
+        float2 s = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int i1 = 0; i1 < N1; ++i1)
+          s = __ffma2_rn(make_float2(l1d[b * N1 + i1], l1d[b * N1 + i1]), w[pa][i1], s);
+        dst[(2 * pa + NQ1 * b) * ST] = s.x;
+        dst[(2 * pa + 1 + NQ1 * b) * ST] = s.y;
+      }
+    return;
+  }
   R w[NQ1][N1];
 #pragma unroll
   for (int a = 0; a < NQ1; ++a)
