@@ -132,8 +132,11 @@ int rkdg_set_precision(rkdg_ctx* ctx, int precision);
 /* Kernel tuning knobs (no counterpart in the reference; set by hand or by
  * rkdg_autotune).  RKDG_TUNE_HEX_KERNEL: 0 default, 1 warp per element,
  * 2 five-lane team per element, 3 five-lane team face pass (each face once,
- * into per-element flux slots the context allocates) + element pass
- * (hexahedra).  RKDG_TUNE_GENERIC_BLOCK /
+ * into per-element flux slots the context allocates) + element pass,
+ * 4 five-lane team over Morton-ordered groups of 24 elements whose faces
+ * inside the group are evaluated once (order <= 2 hexahedra; the plain team
+ * kernel when the mesh's face graph needs more than 8 rounds).
+ * RKDG_TUNE_GENERIC_BLOCK /
  * RKDG_TUNE_LIMITER_BLOCK: elements (threads) per CTA of the triangle/quad
  * right-hand-side kernel and of the limiter, 0 (default 128) or a multiple of
  * 32 up to 256. */

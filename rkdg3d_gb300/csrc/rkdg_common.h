@@ -107,6 +107,31 @@ struct HexOpsPair {
   HexOps<double> d;
 };
 
+// Schedule of one CTA of the shared-face hexahedral team kernel: the CTA's
+// 24 element slots (a compact group of elements in Morton order of their
+// centres) and the rounds in which the slots visit their six faces.  A face
+// whose two elements sit in the same CTA is visited by both in the same
+// round and evaluated once; a face to an element outside the CTA needs that
+// element's trace from global memory (a "job").
+#define RKDG_TEAM_SLOTS 24
+#define RKDG_TEAM_MAX_ROUNDS 8
+struct HexTeamSched {
+  int el[RKDG_TEAM_SLOTS];                                // element of each slot (-1: none)
+  unsigned char rlf[RKDG_TEAM_SLOTS][RKDG_TEAM_MAX_ROUNDS];  // local face of round r (0xFF: none)
+  unsigned char part[RKDG_TEAM_SLOTS][6];                 // slot across an in-CTA face (0xFF: none)
+  // faces the CTA evaluates in round r, one word each: bits 0-4 slot, 5-7
+  // its local face, 8-12 slot across an in-CTA face (31: none), 13 Elem2
+  // side, 14-16 local face across, 17-19 point permutation id, 20 the face
+  // has a neighbour element (0: boundary)
+  unsigned int fd[RKDG_TEAM_MAX_ROUNDS][RKDG_TEAM_SLOTS];
+  unsigned char jb[RKDG_TEAM_MAX_ROUNDS][RKDG_TEAM_SLOTS];   // slots with an out-of-CTA neighbour in round r
+  unsigned char nfl[RKDG_TEAM_MAX_ROUNDS], njb[RKDG_TEAM_MAX_ROUNDS];
+  // normal axis shared by every face visited in round r and by the faces
+  // across them (-1: mixed; the kernel then branches per face)
+  signed char rax[RKDG_TEAM_MAX_ROUNDS];
+  int nr;                                                 // rounds used by this CTA
+};
+
 // Per-element face table entry codes (fcode): bits 0-2 local face of the
 // other element, bit 3 = 1 if this element is the face's Elem2, bits 4..
 // permutation id.  fnbr: neighbour element id, -1 = boundary face with no
@@ -138,6 +163,7 @@ struct RhsParams {
   int* pfail;           // per-problem failure flag (non-physical state)
   int block;            // threads per CTA of the generic kernels (0: default)
   void* fslot;          // hexahedral face-pass flux slots [ne][6][neq][nqf] (or null)
+  const HexTeamSched* hsched;  // shared-face hexahedral kernel: one entry per CTA (or null)
   HexOpsPair hops;      // hexahedra (order <= 2): 1D operators
 };
 

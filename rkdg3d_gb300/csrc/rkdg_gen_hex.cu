@@ -59,21 +59,34 @@ static cudaError_t launch_hex_split(const RhsParams& prm, const R* u, const EpiP
   return launch_hex_team_mode<P, R, 2>(prm, u, ep, st);
 }
 
-// Defaults: Q1 -- face pass + element pass (each face's numerical flux once;
-// the fused kernel where the context holds no flux slots); Q2 -- the
-// warp-per-element kernel in FP64, the fused team kernel in FP32.
+// Shared-face rounds (each face inside a CTA evaluated once); the fused
+// kernel where the context holds no schedule.
+template <int P, typename R>
+static cudaError_t launch_hex_shared(const RhsParams& prm, const R* u, const EpiParams<R>& ep,
+                                     cudaStream_t st) {
+  if (!prm.hsched) return launch_hex_team_mode<P, R, 0>(prm, u, ep, st);
+  return launch_hex_team_mode<P, R, 3>(prm, u, ep, st);
+}
+
+// Defaults (64^3 periodic pulse on a GB300, per RK step): FP32 -- the fused
+// team kernel (Q1 1.39 ms against 1.57 split and 1.42 shared-face; Q2 3.20
+// ms against 3.25 shared-face); FP64 Q1 -- face pass + element pass, whose
+// FP64 fluxes are evaluated once per face (21.6 ms against 27.4 shared-face
+// and 36.3 fused; the fused kernel where the context holds no flux slots);
+// FP64 Q2 -- shared-face rounds (55.7 ms against 68.3 fused and 125.5 warp
+// per element).
 template <>
 cudaError_t launch_rhs_t<5, 1>(int prec, const RhsParams& prm, const void* u, const void* ep,
                                cudaStream_t st) {
   if (prec == 0)
     return launch_hex_split<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st);
-  return launch_hex_split<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+  return launch_hex_team<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
 }
 template <>
 cudaError_t launch_rhs_t<5, 2>(int prec, const RhsParams& prm, const void* u, const void* ep,
                                cudaStream_t st) {
   if (prec == 0)
-    return launch_hex_sf<2, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st);
+    return launch_hex_shared<2, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st);
   return launch_hex_team<2, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
 }
 
@@ -86,9 +99,17 @@ template cudaError_t launch_means_t<5, 2>(int, int, long long, const RefTables*,
 
 // The hexahedral right-hand-side kernels, selectable for tests and the
 // autotuner (0 = default choice above, 1 = warp-per-element sum
-// factorisation, 2 = team kernel, 3 = face pass + element pass).
+// factorisation, 2 = team kernel, 3 = face pass + element pass, 4 = team
+// kernel with shared-face rounds).
 cudaError_t launch_hex_variant(int variant, int p, int prec, const RhsParams& prm, const void* u,
                                const void* ep, cudaStream_t st) {
+  if (variant == 4) {
+    if (p == 1)
+      return prec == 0 ? launch_hex_shared<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)
+                       : launch_hex_shared<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+    return prec == 0 ? launch_hex_shared<2, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)
+                     : launch_hex_shared<2, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+  }
   if (variant == 3) {
     if (p == 1)
       return prec == 0 ? launch_hex_split<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)

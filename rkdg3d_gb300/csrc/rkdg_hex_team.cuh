@@ -47,12 +47,14 @@ struct TeamSize {
   // 32-word rows; team t of a warp starts xoff(t) words into its row so that
   // the team-parallel stores (30 lanes) and the warp-parallel flux reads (two
   // teams of 16 points) fall in distinct banks
-  // MODE 0 (fused right-hand side) needs both; MODE 1 (face pass) the two
+  // MODE 0 (fused right-hand side) needs both; MODE 3 (shared-face rounds)
+  // both plus the slot's 24 face-geometry values; MODE 1 (face pass) the two
   // traces only; MODE 2 (element pass) the volume fluxes only.
   static constexpr int XF = 3 * NEQ * NQF, XV = 3 * NEQ * ND;
   template <int MODE>
   __host__ __device__ static constexpr int xch() {
-    return MODE == 1 ? 2 * NEQ * NQF : (MODE == 2 ? XV : (XF > XV ? XF : XV));
+    return MODE == 1 ? 2 * NEQ * NQF
+                     : (MODE == 2 ? XV : (MODE == 3 ? (XF + 24 > XV ? XF + 24 : XV) : (XF > XV ? XF : XV)));
   }
   // row stride: a multiple of 32 words with room for the offsets (team t + 1
   // may start up to 11 words earlier within its row than team t)
@@ -61,10 +63,17 @@ struct TeamSize {
   template <int MODE>
   __host__ __device__ static constexpr int wstr() { return TPW * xstr<MODE>() + 32; }
   __host__ __device__ static constexpr int xoff(int t) { return 16 * (t & 1) + 5 * (t >> 1); }
+  // MODE 3 keeps the CTA's schedule and the slots' exchange-row offsets
+  // behind the exchange rows
+  static constexpr size_t SCHED_BYTES = (sizeof(HexTeamSched) + 15) / 16 * 16;
   template <typename R, int MODE>
   static constexpr size_t smem_bytes() {
-    return sizeof(R) * (size_t)(EPB * NEQ * ND + WARPS * wstr<MODE>());
+    return sizeof(R) * (size_t)(EPB * NEQ * ND + WARPS * wstr<MODE>()) +
+           (MODE == 3 ? SCHED_BYTES + sizeof(int) * EPB : 0);
   }
+  // MODE 3: a slot's face normals and |J_f| (6 x 4 values) sit in its
+  // exchange row behind the two traces and the fluxes until the volume phase
+  static constexpr int XG = 3 * NEQ * NQF;
   // resident CTAs per SM the register allocation is bounded for
   template <typename R, int MODE>
   __host__ __device__ static constexpr int min_ctas() {
@@ -264,6 +273,57 @@ __device__ __forceinline__ void team_lift_any(int lf, const R* f, const R* l1d, 
   }
 }
 
+// Axis-templated forms with the face's side (0: at 0, 1: at 1 along the
+// normal axis NAX) at run time: the same instructions for both faces of an
+// axis, so that teams of a warp visiting opposite faces of one axis do not
+// diverge.  Same arithmetic, in the same order, as the LF-templated forms.
+template <int P, int NAX, typename R>
+__device__ __forceinline__ void team_contract_s_ax(int sd, const R* su, const R* lend,
+                                                   R (&v)[(P + 1) * (P + 1)]) {
+  constexpr int N1 = P + 1;
+  R le[N1];
+#pragma unroll
+  for (int jn = 0; jn < N1; ++jn) le[jn] = sd ? lend[N1 + jn] : lend[jn];
+#pragma unroll
+  for (int i0 = 0; i0 < N1; ++i0)
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1) {
+      R s = R(0);
+#pragma unroll
+      for (int jn = 0; jn < N1; ++jn) s += le[jn] * su[hnode<N1>(NAX, jn, i0, i1)];
+      v[i0 * N1 + i1] = s;
+    }
+}
+
+template <int P, int NAX, int ST, typename R>
+__device__ __forceinline__ void team_lift_ax(int sd, const R* f, const R* l1d, const R* lend,
+                                             R (&acc)[(P + 1) * (P + 1) * (P + 1)]) {
+  constexpr int N1 = P + 1, NQ1 = P + 2;
+  R le[N1];
+#pragma unroll
+  for (int jn = 0; jn < N1; ++jn) le[jn] = sd ? lend[N1 + jn] : lend[jn];
+  R w[N1][NQ1];
+#pragma unroll
+  for (int i0 = 0; i0 < N1; ++i0)
+#pragma unroll
+    for (int b = 0; b < NQ1; ++b) {
+      R s = R(0);
+#pragma unroll
+      for (int a = 0; a < NQ1; ++a) s += l1d[a * N1 + i0] * f[(a + NQ1 * b) * ST];
+      w[i0][b] = s;
+    }
+#pragma unroll
+  for (int i0 = 0; i0 < N1; ++i0)
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1) {
+      R s = R(0);
+#pragma unroll
+      for (int b = 0; b < NQ1; ++b) s += l1d[b * N1 + i1] * w[i0][b];
+#pragma unroll
+      for (int jn = 0; jn < N1; ++jn) acc[hnode<N1>(NAX, jn, i0, i1)] += le[jn] * s;
+    }
+}
+
 // The values of one variable of an element ordered along its local face LFO,
 // nbv[(i0*N1 + i1)*N1 + jn] = u[node(jn along the normal, i0, i1)], with
 // compile-time offsets (GLOBAL: read-only global loads, else shared memory).
@@ -416,11 +476,152 @@ __device__ __forceinline__ void warp_fluxes(const int LF, const RhsParams& prm, 
   }
 }
 
+// MODE 3: the rounds of the CTA's schedule (HexTeamSched).  In round r each
+// slot's team forms its own trace at its round-r face (To of its exchange
+// row); the CTA's threads, five per job, form the traces of the out-of-CTA
+// neighbours listed for the round (Tn of the listed slot's row); after a
+// barrier the CTA evaluates each listed face once, all threads over all
+// points, in Elem1, Elem2 order (face_integrator.cpp:11-276), writing
+// sign * w_q * |J_f| * Fhat to the evaluating slot's Fh and, across an
+// in-CTA face, the opposite-signed value to the partner's Fh; after a second
+// barrier each team lifts its face.  A face inside the CTA thus costs one
+// trace per side and one numerical flux, where the fused kernel (MODE 0)
+// forms both traces and the flux once per side.
+template <int P, typename R>
+__device__ __forceinline__ void shared_rounds(const RhsParams& prm, const R* __restrict__ u,
+                                              long long NDa, const HexTeamSched& S, R* sX,
+                                              const int* rowoff, R* xch,
+                                              const R* su, int el, bool act, int k, const R* l1d,
+                                              const R* lend, const R* wf,
+                                              const unsigned char (*perm)[(P + 2) * (P + 2)],
+                                              const unsigned char (*fab)[(P + 2) * (P + 2)],
+                                              const int (*sfnb)[6], const unsigned char (*sfcd)[6],
+                                              R gamma, R cov, R& lmax,
+                                              R (&acc)[(P + 1) * (P + 1) * (P + 1)]) {
+  using T = TeamSize<P>;
+  constexpr int N1 = T::N1, ND = T::ND, NQF = T::NQF, NEQ = T::NEQ, NF2 = T::NF2, TPW = T::TPW;
+  constexpr int XG = T::XG;
+  auto row = [&](int sl) { return sX + rowoff[sl]; };
+  const int tid = threadIdx.x;
+  const int jb = tid / NEQ, jk = tid - NEQ * jb;  // this thread's job: (listed slot, variable)
+  const int ne = prm.ne;
+#pragma unroll 1
+  for (int r = 0; r < S.nr; ++r) {
+    const int lf = act ? S.rlf[el][r] : 0xFF;
+    const bool mine = lf != 0xFF && sfnb[el][lf] != -1;
+    const bool job = jb < S.njb[r];
+    const int ax = S.rax[r];  // uniform over the CTA: axis-templated code, side at run time
+    int jsl = 0, jlfo = 0;
+    R nbv[ND];
+    if (job) {  // issue the neighbour's loads first; the own trace hides their latency
+      jsl = S.jb[r][jb];
+      const int jlf = S.rlf[jsl][r];
+      jlfo = sfcd[jsl][jlf] & 7;
+      const R* src = u + jk * NDa + (long long)sfnb[jsl][jlf] * ND;
+      switch (ax) {  // the gather order depends on the face's axis only
+        case 0: team_gather<P, 2, true>(src, nbv); break;
+        case 1: team_gather<P, 1, true>(src, nbv); break;
+        case 2: team_gather<P, 0, true>(src, nbv); break;
+        default: team_gather_any<P, true>(jlfo, src, nbv); break;
+      }
+    }
+    if (mine) {
+      R v[NF2];
+      switch (ax) {
+        case 0: team_contract_s_ax<P, 0>(hex_face_side(lf), su, lend, v); break;
+        case 1: team_contract_s_ax<P, 1>(hex_face_side(lf), su, lend, v); break;
+        case 2: team_contract_s_ax<P, 2>(hex_face_side(lf), su, lend, v); break;
+        default: team_contract_s_any<P>(lf, su, lend, v); break;
+      }
+      team_interp<P, NEQ>(v, l1d, xch + k);
+    }
+    if (job) {
+      const int sdn = hex_face_side(jlfo);
+      R v[NF2];
+#pragma unroll
+      for (int i = 0; i < NF2; ++i) {
+        R s = R(0);
+#pragma unroll
+        for (int jn = 0; jn < N1; ++jn) s += lend[sdn * N1 + jn] * nbv[i * N1 + jn];
+        v[i] = s;
+      }
+      team_interp<P, NEQ>(v, l1d, row(jsl) + NEQ * NQF + jk);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int pt = tid; pt < S.nfl[r] * NQF; pt += blockDim.x) {
+      const int f = pt / NQF, q = pt - f * NQF;
+      const unsigned d = S.fd[r][f];
+      const int fs = d & 31, flf = (d >> 5) & 7, prt = (d >> 8) & 31, side = (d >> 13) & 1;
+      const int lfo = (d >> 14) & 7, pid = (d >> 17) & 7;
+      const bool interior = (d >> 20) & 1;
+      int nb = 0;
+      if (!interior) {
+        nb = sfnb[fs][flf];  // boundary condition slot of the context's current set
+        if (nb == -1) continue;
+      }
+      R* To = row(fs);
+      const R* Tn = prt != 31 ? row(prt) : To + NEQ * NQF;
+      const R* g = To + XG + flf * 4;
+      R n[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) n[c] = g[c];
+      const R jac = g[3];
+      R s1[NEQ], s2[NEQ];
+      int own = fab[flf][q], other = 0;
+      if (interior) {
+        const int q2 = perm[pid][q];
+        const int a1 = side ? fab[lfo][q] : fab[flf][q];
+        const int a2 = side ? fab[flf][q2] : fab[lfo][q2];
+        const R* T1 = side ? Tn : To;
+        const R* T2 = side ? To : Tn;
+#pragma unroll
+        for (int kk = 0; kk < NEQ; ++kk) {
+          s1[kk] = T1[a1 * NEQ + kk];
+          s2[kk] = T2[a2 * NEQ + kk];
+        }
+        if (side) own = a2;
+        other = a2;
+      } else {
+#pragma unroll
+        for (int kk = 0; kk < NEQ; ++kk) s1[kk] = To[own * NEQ + kk];
+        const BCSlot& bc = prm.bc[-2 - nb];
+        right_state<3>(bc.type, bc.state, s1, s2, n, gamma, cov, (R)prm.rgas);
+      }
+      R F[NEQ];
+      const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), S.el[fs]);
+      lmax = fmax(lmax, sp);
+      const R w = wf[q] * jac;
+      const R wo = side ? w : -w;
+      R* Fh = To + 2 * NEQ * NQF;
+#pragma unroll
+      for (int kk = 0; kk < NEQ; ++kk) Fh[own * NEQ + kk] = wo * F[kk];
+      if (prt != 31) {  // the partner is the face's Elem2
+        R* Fp = row(prt) + 2 * NEQ * NQF;
+#pragma unroll
+        for (int kk = 0; kk < NEQ; ++kk) Fp[other * NEQ + kk] = w * F[kk];
+      }
+    }
+    __syncthreads();
+    if (mine && !prm.faces_only) {
+      const R* fh = xch + 2 * NEQ * NQF + k;
+      switch (ax) {
+        case 0: team_lift_ax<P, 0, NEQ>(hex_face_side(lf), fh, l1d, lend, acc); break;
+        case 1: team_lift_ax<P, 1, NEQ>(hex_face_side(lf), fh, l1d, lend, acc); break;
+        case 2: team_lift_ax<P, 2, NEQ>(hex_face_side(lf), fh, l1d, lend, acc); break;
+        default: team_lift_any<P, NEQ>(lf, fh, l1d, lend, acc); break;
+      }
+    }
+  }
+}
+
 // MODE 0: the whole right-hand side of the CTA's elements (every face
 // evaluated by both its elements).  MODE 1 + MODE 2 (two launches): a face pass
 // that evaluates each face once into per-element flux slots, then an element
 // pass that lifts the six slots and adds the volume term, inverse mass and
-// Runge-Kutta epilogue.
+// Runge-Kutta epilogue.  MODE 3: the CTA's slots hold the elements its
+// schedule names, and faces inside the CTA are evaluated once
+// (shared_rounds); volume term and epilogue as MODE 0.
 template <int P, typename R, int MODE>
 __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>())
     k_rhs_hex_team(const __grid_constant__ RhsParams prm, const R* __restrict__ u,
@@ -443,24 +644,38 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
   R* sX = sU + EPB * NEQ * ND;  // [WARPS][WSTR] team exchange rows
   const RefTables* T = prm.tab;
   const int tid = threadIdx.x;
+  const int ne = prm.ne;
+  const int e0 = blockIdx.x * EPB;
+  HexTeamSched* sS = nullptr;    // MODE 3: this CTA's schedule
+  int* sRowOff = nullptr;        // MODE 3: exchange-row offset of each slot
+  if constexpr (MODE == 3) {
+    sS = reinterpret_cast<HexTeamSched*>(sX + S::WARPS * WSTR);
+    sRowOff = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(sS) + S::SCHED_BYTES);
+    const int* src = reinterpret_cast<const int*>(prm.hsched + blockIdx.x);
+    for (int t = tid; t < (int)(sizeof(HexTeamSched) / 4); t += blockDim.x)
+      reinterpret_cast<int*>(sS)[t] = src[t];
+    if (tid < EPB) sRowOff[tid] = (tid / S::TPW) * WSTR + (tid % S::TPW) * XSTR + S::xoff(tid % S::TPW);
+    __syncthreads();
+  }
+  // element of slot el: consecutive elements, or the schedule's (MODE 3)
+  auto eid = [&](int el) { return MODE == 3 ? sS->el[el] : e0 + el; };
   for (int t = tid; t < min(T->nperm, RKDG_HEX_MAX_PERM) * NQF; t += blockDim.x)
     sPerm[t / NQF][t % NQF] = (unsigned char)T->perm[t / NQF][t % NQF];
   for (int t = tid; t < 6 * NQF; t += blockDim.x) sFab[t / NQF][t % NQF] = (unsigned char)T->fab[t / NQF][t % NQF];
 
-  const int ne = prm.ne;
   const long long NDa = prm.ndofs;
-  const int e0 = blockIdx.x * EPB;
   const int nel = min(EPB, ne - e0);
   __shared__ int sFnb[EPB][6];
   __shared__ unsigned char sFcd[EPB][6];  // pid << 4 | side << 3 | other local face
   for (int t = tid; t < nel * 6; t += blockDim.x) {
     const int lf = t / nel, el = t % nel;
-    sFnb[el][lf] = prm.fnbr[lf * ne + e0 + el];
-    sFcd[el][lf] = (unsigned char)prm.fcode[lf * ne + e0 + el];
+    sFnb[el][lf] = prm.fnbr[lf * ne + eid(el)];
+    sFcd[el][lf] = (unsigned char)prm.fcode[lf * ne + eid(el)];
   }
   for (int k = 0; k < NEQ; ++k)
     for (int t = tid; t < nel * ND; t += blockDim.x)
-      sU[((t / ND) * NEQ + k) * ND + (t % ND)] = u[k * NDa + (long long)e0 * ND + t];
+      sU[((t / ND) * NEQ + k) * ND + (t % ND)] =
+          u[k * NDa + (MODE == 3 ? (long long)sS->el[t / ND] * ND + t % ND : (long long)e0 * ND + t)];
   __syncthreads();
 
   const int warp = tid >> 5, lane = tid & 31;
@@ -472,7 +687,7 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
   const unsigned mask = act ? (0x1Fu << (team * NEQ)) : 0u;
   const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
   R lmax = R(0);
-  const int e = e0 + el;
+  const int e = act ? eid(el) : 0;
   const int k = tl;
   const int wel0 = warp * S::TPW;
   R* wx = sX + warp * WSTR;
@@ -481,7 +696,14 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
   R acc[ND];
 #pragma unroll
   for (int i = 0; i < ND; ++i) acc[i] = R(0);
-  if constexpr (MODE != 2) {
+  if constexpr (MODE == 3) {
+    if (act) {  // the slot's face geometry into its exchange row
+      const R* fg = (const R*)prm.fgeo;
+      for (int i = k; i < 24; i += NEQ) xch[S::XG + i] = __ldg(fg + (long long)i * ne + e);
+    }
+    shared_rounds<P, R>(prm, u, NDa, *sS, sX, sRowOff, xch, su, el, act, k, tL1, tLend, tWf, sPerm,
+                        sFab, sFnb, sFcd, gamma, cov, lmax, acc);
+  } else if constexpr (MODE != 2) {
     // the warp steps through the six faces together: traces per team, the
     // numerical fluxes over all 32 lanes, the lifting per team again (MODE 0)
 #pragma unroll 1
@@ -644,7 +866,7 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
           const int g = c0 + c * blockDim.x;
           const int gg = g < total ? g : c0;
           const int k = gg / (nel * ND), t = gg % (nel * ND);
-          idx[c] = k * NDa + (long long)e0 * ND + t;
+          idx[c] = k * NDa + (MODE == 3 ? (long long)sS->el[t / ND] * ND + t % ND : (long long)e0 * ND + t);
           y[c] = sU[((t / ND) * NEQ + k) * ND + (t % ND)];
           if constexpr (std::is_same<R, double>::value) {
             bh[c] = ep.base ? ep.base[idx[c]] : R(0);
@@ -699,7 +921,8 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
         for (int t = tid; t < nel * ND; t += blockDim.x) {
           const int s = ((t / ND) * NEQ + k) * ND + (t % ND);
           R hi, lo;
-          epi_value2<R>(ep, k * NDa + (long long)e0 * ND + t, sU[s], hi, lo);
+          epi_value2<R>(ep, k * NDa + (MODE == 3 ? (long long)sS->el[t / ND] * ND + t % ND : (long long)e0 * ND + t),
+                        sU[s], hi, lo);
           if (need_means) {
             sU[s] = hi;
             sX[s] = lo;
@@ -712,7 +935,7 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
       for (int t = tid; t < nel * NEQ; t += blockDim.x) {
         double m = 0.0;
         for (int i = 0; i < ND; ++i) m += T->wmean[i] * ((double)sU[t * ND + i] + (double)sX[t * ND + i]);
-        ep.means[(long long)(t % NEQ) * ne + e0 + t / NEQ] = m;
+        ep.means[(long long)(t % NEQ) * ne + eid(t / NEQ)] = m;
       }
     }
   }

@@ -19,11 +19,13 @@
 #include <vector>
 
 #include "rkdg_common.h"
+#include "rkdg_hexsched.h"
 #include "rkdg_launch.h"
 #include "rkdg_refelem.h"
 
 using rkdg::BCSlot;
 using rkdg::EpiParams;
+using rkdg::HexTeamSched;
 using rkdg::LimParams;
 using rkdg::RefTables;
 using rkdg::RhsParams;
@@ -48,6 +50,8 @@ struct rkdg_ctx {
   int gen_block = 0;    // RKDG_TUNE_GENERIC_BLOCK
   double* d_fslot = nullptr;  // face-pass flux slots (split hexahedral variant)
   size_t fslot_n = 0;
+  HexTeamSched* d_hsched = nullptr;  // per-CTA schedules of the shared-face hexahedral kernel
+  int hsched_rounds = 0;
   int lim_block = 0;    // RKDG_TUNE_LIMITER_BLOCK
   int solver_quirks = 0;
   // mesh (host copies)
@@ -172,6 +176,8 @@ void free_mesh(rkdg_ctx* c) {
   c->adj_n = 0;
   dfree(c->d_fslot);
   c->fslot_n = 0;
+  dfree(c->d_hsched);
+  c->hsched_rounds = 0;
   c->nprob = 0;
   c->has_mesh = false;
 }
@@ -261,6 +267,7 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   P.err = c->d_err;
   P.block = c->gen_block;
   P.fslot = c->d_fslot;
+  P.hsched = c->d_hsched;
   if (c->geom == RKDG_GEOM_CUBE && c->p <= 2) {
     const int n1 = c->p + 1, nq1 = c->p + 2;
     const RefTables& T = c->tab;
@@ -285,9 +292,10 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
 }
 
 // Kernels one right-hand-side launch issues (the split hexahedral variant
-// runs a face pass and an element pass).
+// runs a face pass and an element pass; it is the FP64 Q1 default).
 int rhs_kernels(const rkdg_ctx* c, const RhsParams& P) {
-  const bool split = c->hex_variant == 3 || (c->hex_variant == 0 && c->p == 1);
+  const bool fp64 = P.fgeo == (const void*)c->d_fgeo64;
+  const bool split = c->hex_variant == 3 || (c->hex_variant == 0 && c->p == 1 && fp64);
   return (c->geom == RKDG_GEOM_CUBE && split && P.fslot && !P.faces_only) ? 2 : 1;
 }
 
@@ -719,7 +727,7 @@ int rkdg_set_solver_quirks(rkdg_ctx* c, int flags) {
 
 int rkdg_set_tuning(rkdg_ctx* c, int key, int value) {
   if (!c) return RKDG_ERR_INVALID;
-  if (key == RKDG_TUNE_HEX_KERNEL && value >= 0 && value <= 3) {
+  if (key == RKDG_TUNE_HEX_KERNEL && value >= 0 && value <= 4) {
     if (value == 3 && c->has_mesh) {
       const int st = ensure_fslot(c);
       if (st) return st;
@@ -1014,6 +1022,14 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
                          cudaMemcpyHostToDevice));
   CUDA_TRY(c, dalloc(c->d_means, (size_t)neq * ne));
   CUDA_TRY(c, dalloc(c->d_partial, (size_t)neq * 1024));
+  if (c->geom == RKDG_GEOM_CUBE && c->p <= 2) {
+    std::vector<HexTeamSched> hs;
+    if (rkdg::build_hex_sched(ne, nvpe, m->elem_coords, c->h_fnbr, c->h_fcode, hs, &c->hsched_rounds)) {
+      CUDA_TRY(c, dalloc(c->d_hsched, hs.size()));
+      CUDA_TRY(c, cudaMemcpy(c->d_hsched, hs.data(), hs.size() * sizeof(HexTeamSched),
+                             cudaMemcpyHostToDevice));
+    }
+  }
   c->has_mesh = true;
   int st = refresh_fnbr(c);
   if (st) return st;
@@ -1676,7 +1692,7 @@ int rkdg_autotune(rkdg_ctx* c, const double* x, int* hex_kernel, int* generic_bl
     if ((st = ensure_fslot(c))) return st;
     int best = 0;
     float tbest = 0.0f;
-    for (int v = 1; v <= 3; ++v) {
+    for (int v = 1; v <= (c->d_hsched ? 4 : 3); ++v) {
       c->hex_variant = v;
       float ms = 0.0f;
       if ((st = time_rhs(&ms))) return st;

@@ -124,12 +124,12 @@ def test_rhs_walls(cuda, geom, order, n, bc, rs, avg):
     assert abs(m - m_ref) <= 1e-13 * abs(m_ref)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("walled", [False, True])
 def test_rhs_hex_kernel_variants(cuda, variant, order, walled):
     """The hexahedral kernels (warp per element, five-lane team, face pass +
-    element pass) in FP64."""
+    element pass, team kernel with shared-face rounds) in FP64."""
     from rkdg3d_gb300.solver import TUNE_HEX_KERNEL
     case = (walled_case(M.GEOM_CUBE, 3, order, RS_HLLC, AVG_EINFELDT, bc=BC_SLIP) if walled
             else periodic_case(M.GEOM_CUBE, 3, order, RS_LLF))
@@ -145,6 +145,41 @@ def test_rhs_hex_kernel_variants(cuda, variant, order, walled):
     xd = dev(x)
     ctx.step(xd, 1e-3)
     assert rel_l1(xd.cpu().numpy(), xs_ref) < RHS_TOL
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("order,n,bc", [(2, 8, None), (2, 3, None), (2, 8, BC_SLIP),
+                                        (1, 16, BC_FIXED_PRESSURE_OUTLET)])
+def test_rhs_hex_shared_faces(cuda, prec, order, n, bc):
+    """Shared-face rounds on meshes of several CTAs (faces inside a CTA
+    evaluated once, the others through neighbour traces from global memory;
+    3^3 periodic: rings of three elements inside a CTA need a seventh round
+    that mixes face axes): right-hand side, face-only speed and one step
+    against the oracle.  Dyadic spacings: with the reference's rotation
+    (cos psi = sqrt(1 - n_z^2), quirk Q14) a unit normal one ulp off +-z
+    changes the flux by ~1e-8, and the oracle forms normals per point as
+    MFEM does where the library forms one per face."""
+    from rkdg3d_gb300.solver import TUNE_HEX_KERNEL
+    case = (periodic_case(M.GEOM_CUBE, n, order, RS_HLL) if bc is None
+            else walled_case(M.GEOM_CUBE, n, order, RS_HLLC, AVG_EINFELDT, bc=bc))
+    if bc in BC_PARAMS:
+        case.bcs = [(a, bc, BC_PARAMS[bc]) for a, _, _ in case.bcs]
+    ctx, orc = pair(case)
+    if prec:
+        ctx.set_precision(1)
+    ctx.set_tuning(TUNE_HEX_KERNEL, 4)
+    tol = RHS_TOL if prec == 0 else 1e-5
+    x = random_state(ctx.node_coords(), seed=23)
+    y_ref, m_ref = orc.rhs(x)
+    y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    m = ctx.rhs(dev(x), y)
+    assert rel_l1(y.cpu().numpy(), y_ref) < tol
+    assert abs(m - m_ref) <= (1e-13 if prec == 0 else 1e-6) * m_ref
+    assert abs(ctx.face_speed(dev(x)) - orc.face_speed(x)) <= (1e-13 if prec == 0 else 1e-6) * m_ref
+    xs_ref, _ = orc.step(x, 1e-3)
+    xd = dev(x)
+    ctx.step(xd, 1e-3)
+    assert rel_l1(xd.cpu().numpy(), xs_ref) < tol
 
 
 def test_node_coords_match_oracle(cuda):
@@ -266,7 +301,7 @@ def test_autotune_keeps_parity(cuda, geom, order):
     ctx.rhs(dev(x), before_y)
     choice = ctx.autotune(dev(x))
     if geom == M.GEOM_CUBE:
-        assert choice["hex_kernel"] in (1, 2, 3)
+        assert choice["hex_kernel"] in (1, 2, 3, 4)
     else:
         assert choice["generic_block"] in (64, 128, 256)
         assert choice["limiter_block"] in (64, 128, 256)
@@ -342,7 +377,8 @@ def test_shu_with_multi_is_rejected(cuda):
 
 @pytest.mark.parametrize("geom,order,prec,variant", [(M.GEOM_SQUARE, 1, 0, 0), (M.GEOM_TRIANGLE, 2, 1, 0),
                                                      (M.GEOM_CUBE, 2, 1, 0), (M.GEOM_CUBE, 2, 0, 0),
-                                                     (M.GEOM_CUBE, 1, 0, 0), (M.GEOM_CUBE, 1, 1, 2)])
+                                                     (M.GEOM_CUBE, 1, 0, 0), (M.GEOM_CUBE, 1, 1, 2),
+                                                     (M.GEOM_CUBE, 2, 1, 4), (M.GEOM_CUBE, 1, 0, 4)])
 def test_nonphysical_state_is_reported(cuda, geom, order, prec, variant):
     """Where the reference prints the elements and exits on a non-physical
     state (face_integrator.cpp:214-218), every kernel path returns
