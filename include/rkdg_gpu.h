@@ -107,7 +107,16 @@ int rkdg_set_physics(rkdg_ctx* ctx, int rsolver, int averaging, double gamma,
 /* Replaces FE_Evolution::UpdateInverseMassMatrix / UpdateAfluxPointer
  * (fe_evolution.hpp:78-81) and the integrator set-up of main.cpp:148-164:
  * builds every device face / element / stencil table.  Idempotent; call it
- * after every AMR adapt (main.cpp:610-611). */
+ * after every AMR adapt (main.cpp:610-611).  Nonconforming meshes (hanging
+ * vertices left by the reference's NC refinement, any number of levels):
+ * a face that no second element shares and no boundary face lists is
+ * integrated as MFEM does -- each slave face from its fine element against
+ * the coarse element across, the master face not at all.  Such a face must
+ * lie inside a face of the element across it, or be covered by such faces,
+ * else RKDG_ERR_INVALID (a hole; also a hanging face across a periodic seam).
+ * On a mesh with hanging faces the right-hand side, steps and runs are
+ * available; an active limiter, batched problems and the adjoint return
+ * RKDG_ERR_UNSUPPORTED. */
 int rkdg_upload_mesh(rkdg_ctx* ctx, const rkdg_mesh_desc* mesh);
 /* Deviations from the shipped reference, off by default.
  * RKDG_QUIRK_HLLC_NEGATIVE_SPEED_OK: the reference treats any negative face

@@ -615,6 +615,7 @@ struct Face {
   int e1 = -1, lf1 = -1, e2 = -1, lf2 = -1;
   int fv[4] = {-1, -1, -1, -1};  // face vertex ids in elem1's local order
   double ref2[4][3];             // elem2 reference coords of fv[k]
+  bool master = false;           // coarse side of nonconforming faces (not integrated)
 };
 
 struct ElemOps {
@@ -1045,6 +1046,125 @@ void means_of(const ref_ctx* c, const double* x, double* means) {
 
 extern "C" {
 
+// Nonconforming faces (restating MFEM's NCMesh face lists, which the
+// reference gets from EnsureNCMesh + refinement, case_manager.cpp:269,
+// main.cpp:564-696): a face that no second element shares and no boundary
+// element lists is either a slave -- it lies inside a face of an element on
+// the other side -- or that master face.  NonlinearForm::Mult integrates
+// each slave face as an interior face with Elem1 = the slave's (fine)
+// element and Elem2 = the master's element, whose points are the slave
+// face's points mapped into it (Mesh::GetFaceElementTransformations with the
+// NC point matrix); master faces are skipped (GetInteriorFaceTransformations
+// returns NULL for them).  Every element is affine here, so the mapped
+// reference coordinates of the slave's corners give all its points.
+namespace {
+void inverse_map(const ref_ctx* c, int e, const double* x, double* xi) {
+  const int dim = c->dim;
+  double xc[3], J[9], xi_c[3];
+  for (int i = 0; i < 3; ++i) xi_c[i] = c->geom == REF_GEOM_TRIANGLE ? 1.0 / 3.0 : 0.5;
+  elem_map(c, e, xi_c, xc, J);
+  double d[3] = {0, 0, 0};
+  for (int i = 0; i < dim; ++i) d[i] = x[i] - xc[i];
+  if (dim == 2) {
+    const double det = J[0] * J[3] - J[1] * J[2];
+    xi[0] = xi_c[0] + (J[3] * d[0] - J[1] * d[1]) / det;
+    xi[1] = xi_c[1] + (-J[2] * d[0] + J[0] * d[1]) / det;
+    xi[2] = 0;
+  } else {
+    double A[9];  // adjugate / det
+    A[0] = J[4] * J[8] - J[5] * J[7];
+    A[1] = J[2] * J[7] - J[1] * J[8];
+    A[2] = J[1] * J[5] - J[2] * J[4];
+    A[3] = J[5] * J[6] - J[3] * J[8];
+    A[4] = J[0] * J[8] - J[2] * J[6];
+    A[5] = J[2] * J[3] - J[0] * J[5];
+    A[6] = J[3] * J[7] - J[4] * J[6];
+    A[7] = J[1] * J[6] - J[0] * J[7];
+    A[8] = J[0] * J[4] - J[1] * J[3];
+    const double det = J[0] * A[0] + J[1] * A[3] + J[2] * A[6];
+    for (int r = 0; r < 3; ++r) xi[r] = xi_c[r] + (A[r * 3] * d[0] + A[r * 3 + 1] * d[1] + A[r * 3 + 2] * d[2]) / det;
+  }
+}
+
+// physical corner k (elem1 local face order) of face f
+void face_corner(const ref_ctx* c, const Face& f, int k, double* x) {
+  const int lv = local_face_vertex(c->geom, f.lf1, k);
+  for (int i = 0; i < c->dim; ++i) x[i] = c->ec[((size_t)f.e1 * c->nvpe + lv) * c->dim + i];
+}
+
+double face_measure(const ref_ctx* c, const Face& f) {
+  double a[3], b[3], d[3];
+  face_corner(c, f, 0, a);
+  face_corner(c, f, 1, b);
+  if (c->dim == 2) return std::hypot(b[0] - a[0], b[1] - a[1]);
+  face_corner(c, f, 3, d);
+  double u[3], v[3];
+  for (int i = 0; i < 3; ++i) u[i] = b[i] - a[i], v[i] = d[i] - a[i];
+  return std::sqrt(std::pow(u[1] * v[2] - u[2] * v[1], 2) + std::pow(u[2] * v[0] - u[0] * v[2], 2) +
+                   std::pow(u[0] * v[1] - u[1] * v[0], 2));
+}
+}  // namespace
+
+bool classify_nc_faces(ref_ctx* c) {
+  const int nvf = c->nvpf, dim = c->dim;
+  std::vector<char> bdr(c->faces.size(), 0);
+  for (int f : c->bdr_face) bdr[f] = 1;
+  std::vector<int> lone;
+  for (int f = 0; f < (int)c->faces.size(); ++f)
+    if (c->faces[f].e2 < 0 && !bdr[f]) lone.push_back(f);
+  std::vector<double> covered(c->faces.size(), 0.0);
+  std::vector<char> is_slave(c->faces.size(), 0);
+  for (int sf : lone) {
+    Face& S = c->faces[sf];
+    for (int mf : lone) {
+      const Face& Mf = c->faces[mf];
+      if (mf == sf || Mf.e1 == S.e1) continue;
+      // the slave's corners in the master element's reference space, on its face
+      const double* r0 = ref_vertex(c->geom, local_face_vertex(c->geom, Mf.lf1, 0));
+      const double* r1 = ref_vertex(c->geom, local_face_vertex(c->geom, Mf.lf1, 1));
+      const double* r3 = ref_vertex(c->geom, local_face_vertex(c->geom, Mf.lf1, nvf - 1));
+      double xi[4][3];
+      bool inside = true;
+      for (int k = 0; k < nvf && inside; ++k) {
+        double x[3];
+        face_corner(c, S, k, x);
+        inverse_map(c, Mf.e1, x, xi[k]);
+        double p[3], s0 = 0, s1 = 0, n0 = 0, n1 = 0;
+        for (int i = 0; i < dim; ++i) {
+          s0 += (xi[k][i] - r0[i]) * (r1[i] - r0[i]);
+          n0 += (r1[i] - r0[i]) * (r1[i] - r0[i]);
+          s1 += (xi[k][i] - r0[i]) * (r3[i] - r0[i]);
+          n1 += (r3[i] - r0[i]) * (r3[i] - r0[i]);
+        }
+        s0 /= n0;
+        s1 = dim == 3 ? s1 / n1 : 0.0;
+        double res = 0;
+        for (int i = 0; i < dim; ++i) {
+          p[i] = r0[i] + s0 * (r1[i] - r0[i]) + (dim == 3 ? s1 * (r3[i] - r0[i]) : 0.0);
+          res = std::max(res, std::fabs(p[i] - xi[k][i]));
+        }
+        const double tol = 1e-9;
+        inside = res < tol && s0 > -tol && s0 < 1 + tol && s1 > -tol && s1 < 1 + tol;
+      }
+      if (!inside) continue;
+      S.e2 = Mf.e1;
+      S.lf2 = Mf.lf1;
+      for (int k = 0; k < nvf; ++k)
+        for (int i = 0; i < 3; ++i) S.ref2[k][i] = i < dim ? xi[k][i] : 0.0;
+      is_slave[sf] = 1;
+      covered[mf] += face_measure(c, S);
+      break;
+    }
+  }
+  for (int f : lone) {
+    if (is_slave[f]) continue;
+    const double m = face_measure(c, c->faces[f]);
+    if (!(std::fabs(covered[f] - m) <= 1e-9 * m)) return false;  // neither slave nor covered master
+    c->faces[f].master = true;
+  }
+  return true;
+}
+
 ref_ctx* ref_create(int dim, int geom, int order, int num_elements, const int* elem_vertices,
                     const double* elem_coords, int num_bdr, const int* bdr_vertices,
                     const int* bdr_attr) {
@@ -1126,6 +1246,10 @@ ref_ctx* ref_create(int dim, int geom, int order, int num_elements, const int* e
       return nullptr;
     }
     c->bdr_face[bi] = it->second;
+  }
+  if (!classify_nc_faces(c)) {
+    delete c;
+    return nullptr;
   }
   // ElementToElementTable
   c->el_el.assign(c->ne, {});

@@ -164,7 +164,27 @@ struct RhsParams {
   int block;            // threads per CTA of the generic kernels (0: default)
   void* fslot;          // hexahedral face-pass flux slots [ne][6][neq][nqf] (or null)
   const HexTeamSched* hsched;  // shared-face hexahedral kernel: one entry per CTA (or null)
+  // nonconforming meshes: element -> row of xface (-1: none) and the face
+  // terms of the hanging faces, [row][neq][nd] in the kernel's precision,
+  // added to the element's face + volume terms before the inverse mass
+  const int* ncidx;
+  const void* xface;
   HexOpsPair hops;      // hexahedra (order <= 2): 1D operators
+};
+
+// Hanging (nonconforming) faces of an adapted mesh.  Each slave face is
+// integrated from its fine element (Elem1, the face's own points and normal)
+// against the master face's coarse element (Elem2), evaluated at the slave
+// points mapped into it; master faces carry no integrator of their own.
+struct NcParams {
+  int nnc, nqf, nd, neq, nel;
+  const int* face;      // [nnc][3]: fine element, its local face, coarse element
+  const double* bnc;    // [nnc][nqf][nd]: coarse element's basis at the mapped points
+  void* flux;           // [nnc][nqf][neq]: w_q |J_f| Fhat (kernel precision)
+  const int* elem;      // [nel] elements with hanging-face terms
+  const int* ptr;       // [nel + 1] CSR rows of ent
+  const int* ent;       // 2 * slave face + side (0: fine, 1: coarse)
+  void* xface;          // [nel][neq][nd] (kernel precision)
 };
 
 // Stage epilogue.

@@ -322,6 +322,16 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
             for (int j = 0; j < ND; ++j) acc[k][j] += sD[r][j][m] * gc;
           }
       }
+      if (prm.ncidx) {  // hanging faces of a nonconforming mesh
+        const int ix = prm.ncidx[e];
+        if (ix >= 0) {
+          const R* xf = (const R*)prm.xface + (long long)ix * NEQ * ND;
+#pragma unroll
+          for (int k = 0; k < NEQ; ++k)
+#pragma unroll
+            for (int j = 0; j < ND; ++j) acc[k][j] += xf[k * ND + j];
+        }
+      }
 #pragma unroll
       for (int k = 0; k < NEQ; ++k) {
         R y[ND];

@@ -322,7 +322,10 @@ __global__ void __launch_bounds__(256)
             sG[(r * NEQ + k) * ND + j] = adj[r][0] * F[k][0] + adj[r][1] * F[k][1] + adj[r][2] * F[k][2];
       }
       __syncwarp();
-      // collocated (phi, grad phi), one direction at a time
+      // collocated (phi, grad phi), one direction at a time; plus the face
+      // terms of hanging faces (nonconforming meshes)
+      const R* xf = nullptr;
+      if (prm.ncidx && prm.ncidx[e] >= 0) xf = (const R*)prm.xface + (long long)prm.ncidx[e] * NEQ * ND;
       for (int o = lane; o < NEQ * ND; o += 32) {
         const int k = o / ND, j = o % ND;
         const int jx = j % N1, jy = (j / N1) % N1, jz = j / (N1 * N1);
@@ -334,6 +337,7 @@ __global__ void __launch_bounds__(256)
           zz += tD1[jz * N1 + m] * sG[(2 * NEQ + k) * ND + jx + N1 * (jy + N1 * m)];
         }
         sAcc[o] += tW1[jy] * tW1[jz] * zx + tW1[jx] * tW1[jz] * zy + tW1[jx] * tW1[jy] * zz;
+        if (xf) sAcc[o] += xf[o];
       }
       __syncwarp();
       // inverse mass: three 1D sweeps (x into sG, y back into sAcc, z in registers)

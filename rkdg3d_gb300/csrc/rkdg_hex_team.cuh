@@ -808,6 +808,14 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
             for (int m = 0; m < N1; ++m) s += tD1[jz * N1 + m] * g[jx + N1 * (jy + N1 * m)];
             acc[jx + N1 * (jy + N1 * jz)] += tW1[jx] * tW1[jy] * s;
           }
+      if (prm.ncidx) {  // hanging faces of a nonconforming mesh
+        const int ix = prm.ncidx[e];
+        if (ix >= 0) {
+          const R* xf = (const R*)prm.xface + ((long long)ix * NEQ + k) * ND;
+#pragma unroll
+          for (int i = 0; i < ND; ++i) acc[i] += xf[i];
+        }
+      }
       // inverse mass: x, y, z sweeps
 #pragma unroll
       for (int jz = 0; jz < N1; ++jz)

@@ -20,6 +20,7 @@
 
 #include "rkdg_common.h"
 #include "rkdg_hexsched.h"
+#include "rkdg_ncmesh.h"
 #include "rkdg_launch.h"
 #include "rkdg_refelem.h"
 
@@ -52,6 +53,16 @@ struct rkdg_ctx {
   size_t fslot_n = 0;
   HexTeamSched* d_hsched = nullptr;  // per-CTA schedules of the shared-face hexahedral kernel
   int hsched_rounds = 0;
+  // hanging faces of a nonconforming mesh (see rkdg_nc.cu)
+  int nnc = 0, nc_nel = 0;
+  int* d_nc_face = nullptr;
+  double* d_nc_bnc = nullptr;
+  double* d_nc_flux = nullptr;
+  int* d_nc_elem = nullptr;
+  int* d_nc_ptr = nullptr;
+  int* d_nc_ent = nullptr;
+  int* d_ncidx = nullptr;
+  double* d_xface = nullptr;
   int lim_block = 0;    // RKDG_TUNE_LIMITER_BLOCK
   int solver_quirks = 0;
   // mesh (host copies)
@@ -178,6 +189,15 @@ void free_mesh(rkdg_ctx* c) {
   c->fslot_n = 0;
   dfree(c->d_hsched);
   c->hsched_rounds = 0;
+  dfree(c->d_nc_face);
+  dfree(c->d_nc_bnc);
+  dfree(c->d_nc_flux);
+  dfree(c->d_nc_elem);
+  dfree(c->d_nc_ptr);
+  dfree(c->d_nc_ent);
+  dfree(c->d_ncidx);
+  dfree(c->d_xface);
+  c->nnc = c->nc_nel = 0;
   c->nprob = 0;
   c->has_mesh = false;
 }
@@ -268,6 +288,8 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   P.block = c->gen_block;
   P.fslot = c->d_fslot;
   P.hsched = c->d_hsched;
+  P.ncidx = c->nnc ? c->d_ncidx : nullptr;
+  P.xface = c->d_xface;
   if (c->geom == RKDG_GEOM_CUBE && c->p <= 2) {
     const int n1 = c->p + 1, nq1 = c->p + 2;
     const RefTables& T = c->tab;
@@ -289,6 +311,36 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
     fill(P.hops.d);
   }
   return P;
+}
+
+rkdg::NcParams nc_params(const rkdg_ctx* c) {
+  rkdg::NcParams N;
+  std::memset(&N, 0, sizeof N);
+  N.nnc = c->nnc;
+  N.nqf = c->tab.nqf;
+  N.nd = c->nd;
+  N.neq = c->neq;
+  N.nel = c->nc_nel;
+  N.face = c->d_nc_face;
+  N.bnc = c->d_nc_bnc;
+  N.flux = c->d_nc_flux;
+  N.elem = c->d_nc_elem;
+  N.ptr = c->d_nc_ptr;
+  N.ent = c->d_nc_ent;
+  N.xface = c->d_xface;
+  return N;
+}
+
+// One right-hand-side evaluation: on a nonconforming mesh first the hanging
+// faces (their wave speeds, and their face terms unless only the speed is
+// wanted), then the element kernel.
+cudaError_t launch_rhs_nc(rkdg_ctx* c, int prec, const RhsParams& P, const void* in, const void* ep) {
+  if (c->nnc) {
+    const cudaError_t e = rkdg::launch_nc(c->dim, prec, P, nc_params(c), in, !P.faces_only, c->stream);
+    if (e != cudaSuccess) return e;
+    c->launches += P.faces_only ? 1 : 2;
+  }
+  return rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p, prec, P, in, ep, c->stream);
 }
 
 // Kernels one right-hand-side launch issues (the split hexahedral variant
@@ -454,7 +506,7 @@ int enqueue_step64(rkdg_ctx* c, double* x, double dt, bool batch = false) {
     ep.means = lim ? c->d_means : nullptr;
     RhsParams P = rhs_params(c, 0, 0, i);
     if (batch) set_batch(c, P, i);
-    CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,0, P, in, &ep, c->stream));
+    CUDA_TRY(c, launch_rhs_nc(c, 0, P, in, &ep));
     c->launches += rhs_kernels(c, P);
     if (lim) {
       LimParams L = lim_params_for(c, batch);
@@ -528,7 +580,7 @@ int enqueue_step32(rkdg_ctx* c, double dt, bool batch = false) {
     ep.means = lim ? c->d_means : nullptr;
     RhsParams P = rhs_params(c, 1, 0, i);
     if (batch) set_batch(c, P, i);
-    CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,1, P, in, &ep, c->stream));
+    CUDA_TRY(c, launch_rhs_nc(c, 1, P, in, &ep));
     c->launches += rhs_kernels(c, P);
     if (lim) {
       LimParams L = lim_params_for(c, batch);
@@ -677,6 +729,8 @@ int rkdg_set_limiter(rkdg_ctx* c, int limiter, int indicator, int function, int 
     return fail(c, RKDG_ERR_UNSUPPORTED,
                 "Shu indicator with the Multi limiter: the reference multiplies by a cell "
                 "factor the Shu indicator never sets");
+  if (c->has_mesh && c->nnc && !(limiter == RKDG_LIM_FINDIFF && indicator == RKDG_IND_NOWHERE))
+    return fail(c, RKDG_ERR_UNSUPPORTED, "limiters on meshes with hanging faces are not supported");
   if ((quirk_flags & RKDG_LIMITER_LINEARIZE) && limiter == RKDG_LIM_MULTI && c->has_mesh &&
       c->geom != RKDG_GEOM_TRIANGLE && !c->tab.lin_ok)
     return fail(c, RKDG_ERR_UNSUPPORTED,
@@ -891,6 +945,7 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
       }
     }
   std::map<std::array<int, 4>, int> bkey;
+  std::vector<rkdg::NcFace> lone;
   for (int i = 0; i < m->num_bdr; ++i) bkey[face_key(m->bdr_vertices + (size_t)i * nvpf)] = m->bdr_attr[i];
   c->h_fnbr.assign((size_t)nfpe * ne, -1);
   c->h_fattr.assign((size_t)nfpe * ne, 0);
@@ -938,6 +993,7 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     if (f.s2.e < 0) {
       auto bit = bkey.find(kv.first);
       c->h_fattr[(size_t)lf1 * ne + e1] = bit == bkey.end() ? 0 : bit->second;
+      if (bit == bkey.end()) lone.push_back({e1, lf1});  // a hanging face (or a hole)
       c->h_fnbr[(size_t)lf1 * ne + e1] = -1;
       continue;
     }
@@ -993,6 +1049,55 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     c->h_fcode[(size_t)lf2 * ne + e2] = lf1 | (1 << 3) | (pid << 4);
   }
   T.nperm = (int)perm_ids.size();
+  // ---- hanging faces (nonconforming meshes) ----
+  std::vector<rkdg::NcSlave> slaves;
+  std::vector<int> nc_face, nc_elem, nc_ptr, nc_ent, ncidx;
+  std::vector<double> nc_bnc;
+  {
+    std::vector<double> fmeas((size_t)nfpe * ne);
+    for (int lf = 0; lf < nfpe; ++lf)
+      for (int e = 0; e < ne; ++e) fmeas[(size_t)lf * ne + e] = c->h_fgeo[(size_t)(lf * (dim + 1) + dim) * ne + e];
+    std::string why;
+    if (!rkdg::classify_nc_faces(geom, dim, nvpe, m->elem_coords, Jall, fmeas, ne, lone, slaves, why))
+      return fail(c, RKDG_ERR_INVALID, why.c_str());
+    if (!slaves.empty() && c->limiter_active())
+      return fail(c, RKDG_ERR_UNSUPPORTED, "limiters on meshes with hanging faces are not supported");
+    const int nns = (int)slaves.size();
+    if (nns) {
+      rkdg::Basis B(geom, p);
+      std::vector<std::vector<int>> ents(ne);
+      nc_bnc.resize((size_t)nns * T.nqf * nd);
+      std::vector<double> phi(nd);
+      for (int f = 0; f < nns; ++f) {
+        const rkdg::NcSlave& s = slaves[f];
+        nc_face.insert(nc_face.end(), {s.e1, s.lf1, s.e2});
+        ents[s.e1].push_back(2 * f);
+        ents[s.e2].push_back(2 * f + 1);
+        const double* X1 = m->elem_coords + (size_t)s.e1 * nvpe * dim;
+        const double* X2 = m->elem_coords + (size_t)s.e2 * nvpe * dim;
+        for (int q = 0; q < T.nqf; ++q) {
+          const rkdg::FacePoint& fp = fp_of(s.lf1, q);
+          double x[3] = {0, 0, 0}, xi2[3];
+          for (int i = 0; i < dim; ++i) {
+            x[i] = X1[i];
+            for (int r = 0; r < dim; ++r) x[i] += Jall[(size_t)s.e1 * 9 + i * dim + r] * fp.xi[r];
+          }
+          rkdg::affine_inverse(dim, X2, &Jall[(size_t)s.e2 * 9], x, xi2);
+          B.eval(xi2, phi.data(), nullptr);
+          for (int j = 0; j < nd; ++j) nc_bnc[((size_t)f * T.nqf + q) * nd + j] = phi[j];
+        }
+      }
+      ncidx.assign(ne, -1);
+      nc_ptr.push_back(0);
+      for (int e = 0; e < ne; ++e) {
+        if (ents[e].empty()) continue;
+        ncidx[e] = (int)nc_elem.size();
+        nc_elem.push_back(e);
+        nc_ent.insert(nc_ent.end(), ents[e].begin(), ents[e].end());
+        nc_ptr.push_back((int)nc_ent.size());
+      }
+    }
+  }
   // the hexahedral kernels keep one byte per point permutation of a square
   // face (at most its 8 orientations)
   if (c->geom == RKDG_GEOM_CUBE && T.nperm > RKDG_HEX_MAX_PERM)
@@ -1022,6 +1127,25 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
                          cudaMemcpyHostToDevice));
   CUDA_TRY(c, dalloc(c->d_means, (size_t)neq * ne));
   CUDA_TRY(c, dalloc(c->d_partial, (size_t)neq * 1024));
+  if (!slaves.empty()) {
+    const int nns = (int)slaves.size();
+    c->nnc = nns;
+    c->nc_nel = (int)nc_elem.size();
+    CUDA_TRY(c, dalloc(c->d_nc_face, nc_face.size()));
+    CUDA_TRY(c, dalloc(c->d_nc_bnc, nc_bnc.size()));
+    CUDA_TRY(c, dalloc(c->d_nc_flux, (size_t)nns * T.nqf * neq));
+    CUDA_TRY(c, dalloc(c->d_nc_elem, nc_elem.size()));
+    CUDA_TRY(c, dalloc(c->d_nc_ptr, nc_ptr.size()));
+    CUDA_TRY(c, dalloc(c->d_nc_ent, nc_ent.size()));
+    CUDA_TRY(c, dalloc(c->d_ncidx, ncidx.size()));
+    CUDA_TRY(c, dalloc(c->d_xface, (size_t)c->nc_nel * neq * nd));
+    CUDA_TRY(c, cudaMemcpy(c->d_nc_face, nc_face.data(), nc_face.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_nc_bnc, nc_bnc.data(), nc_bnc.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_nc_elem, nc_elem.data(), nc_elem.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_nc_ptr, nc_ptr.data(), nc_ptr.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_nc_ent, nc_ent.data(), nc_ent.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_ncidx, ncidx.data(), ncidx.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
   if (c->geom == RKDG_GEOM_CUBE && c->p <= 2) {
     std::vector<HexTeamSched> hs;
     if (rkdg::build_hex_sched(ne, nvpe, m->elem_coords, c->h_fnbr, c->h_fcode, hs, &c->hsched_rounds)) {
@@ -1078,7 +1202,7 @@ int rkdg_rhs(rkdg_ctx* c, const double* x, double* y, double* mcs_out) {
     ep.mode = 0;
     ep.out64 = y;
     RhsParams P = rhs_params(c, 0, 0, 0);
-    CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,0, P, x, &ep, c->stream));
+    CUDA_TRY(c, launch_rhs_nc(c, 0, P, x, &ep));
     c->launches += rhs_kernels(c, P);
   } else {
     CUDA_TRY(c, rkdg::launch_to_float(n, x, c->d_y32[0], c->stream));
@@ -1087,7 +1211,7 @@ int rkdg_rhs(rkdg_ctx* c, const double* x, double* y, double* mcs_out) {
     ep.mode = 0;
     ep.out64 = y;
     RhsParams P = rhs_params(c, 1, 0, 0);
-    CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,1, P, c->d_y32[0], &ep, c->stream));
+    CUDA_TRY(c, launch_rhs_nc(c, 1, P, c->d_y32[0], &ep));
     c->launches += 1 + rhs_kernels(c, P);
   }
   return read_mcs(c, 0, mcs_out);
@@ -1100,7 +1224,7 @@ int rkdg_face_speed(rkdg_ctx* c, const double* x, double* mcs_out) {
   EpiParams<double> ep;
   std::memset(&ep, 0, sizeof ep);
   RhsParams P = rhs_params(c, 0, 1, 0);
-  CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,0, P, x, &ep, c->stream));
+  CUDA_TRY(c, launch_rhs_nc(c, 0, P, x, &ep));
   c->launches++;
   return read_mcs(c, 0, mcs_out);
 }
@@ -1239,6 +1363,7 @@ int rkdg_batch_setup(rkdg_ctx* c, int nprob, const int* elem_offsets, const doub
     return fail(c, RKDG_ERR_INVALID, "invalid batch description");
   if (c->geom == RKDG_GEOM_CUBE)
     return fail(c, RKDG_ERR_UNSUPPORTED, "batched problems are supported on triangles and quads");
+  if (c->nnc) return fail(c, RKDG_ERR_UNSUPPORTED, "batched problems on meshes with hanging faces");
   if (elem_offsets[0] != 0 || elem_offsets[nprob] != c->ne)
     return fail(c, RKDG_ERR_INVALID, "element offsets must cover the mesh");
   std::vector<int> prob(c->ne);
@@ -1320,7 +1445,7 @@ int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0,
     std::memset(&ep, 0, sizeof ep);
     RhsParams P = rhs_params(c, 0, 1, 0);
     set_batch(c, P, c->s - 1);
-    CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p,0, P, x, &ep, c->stream));
+    CUDA_TRY(c, launch_rhs_nc(c, 0, P, x, &ep));
     CUDA_TRY(c, rkdg::launch_batch_init(bs, dt0, c->stream));
     c->launches += 2;
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -1447,7 +1572,7 @@ int plain_rhs(rkdg_ctx* c, const double* in, double* out) {
   ep.mode = 0;
   ep.out64 = out;
   RhsParams P = rhs_params(c, 0, 0, 7);
-  CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p, 0, P, in, &ep, c->stream));
+  CUDA_TRY(c, launch_rhs_nc(c, 0, P, in, &ep));
   c->launches += rhs_kernels(c, P);
   return RKDG_OK;
 }
@@ -1527,6 +1652,7 @@ int adjoint_ready(rkdg_ctx* c) {
   if (!rkdg::adjoint_supported(c->geom, c->p))
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint kernels for this element type / order");
   if (c->nprob > 0) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for batched problems");
+  if (c->nnc) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint on meshes with hanging faces");
   if ((c->quirks & RKDG_LIMITER_LINEARIZE) && c->limiter_active() && c->lim == RKDG_LIM_MULTI &&
       c->geom != RKDG_GEOM_TRIANGLE)
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for the linearize limiter option");
@@ -1679,7 +1805,7 @@ int rkdg_autotune(rkdg_ctx* c, const double* x, int* hex_kernel, int* generic_bl
     for (int r = 0; r < kWarm + kReps; ++r) {
       if (r == kWarm) CUDA_TRY(c, cudaEventRecord(ev[0], c->stream));
       CUDA_TRY(c, cudaMemsetAsync(c->d_mcs, 0, sizeof(unsigned long long), c->stream));
-      CUDA_TRY(c, rkdg::launch_rhs_v(c->hex_variant, c->geom, c->p, prec, P, in, ep, c->stream));
+      CUDA_TRY(c, launch_rhs_nc(c, prec, P, in, ep));
       c->launches += rhs_kernels(c, P);
     }
     CUDA_TRY(c, cudaEventRecord(ev[1], c->stream));

@@ -230,3 +230,97 @@ def read_gmsh22(path: str) -> Mesh:
              bv.reshape(-1, nvf).astype(np.int32), ba.astype(np.int32))
     m.validate()
     return m
+
+
+# MFEM reference vertices and local faces of the tensor elements
+_REF_VERT = {
+    GEOM_SQUARE: np.array([(0, 0), (1, 0), (1, 1), (0, 1)], float),
+    GEOM_CUBE: np.array([(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0),
+                         (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)], float),
+}
+_LOCAL_FACES = {
+    GEOM_SQUARE: [(0, 1), (1, 2), (2, 3), (3, 0)],
+    GEOM_CUBE: [(3, 2, 1, 0), (0, 1, 5, 4), (1, 2, 6, 5), (2, 3, 7, 6), (3, 0, 4, 7), (4, 5, 6, 7)],
+}
+
+
+def refine_nc(mesh: Mesh, elements) -> Mesh:
+    """Isotropic refinement of the listed quadrilaterals / hexahedra into
+    2^dim children each, leaving their neighbours as they are: the result is
+    a nonconforming mesh with hanging vertices, as MFEM's NC refinement
+    (``Mesh::GeneralRefinement`` on a mesh made nonconforming by
+    ``EnsureNCMesh``, ``case_manager.cpp:269``) produces.  New vertices are
+    identified by the parent vertices they split (edge midpoints by the
+    edge's two ids, face centres by the face's ids), so two refined
+    neighbours share them and periodic identifications carry over.  A
+    refined element is replaced by its first child; the others are
+    appended.  Boundary faces of refined elements are split likewise."""
+    geom = mesh.geom
+    if geom not in _REF_VERT:
+        raise ValueError("refine_nc supports quadrilaterals and hexahedra")
+    dim = mesh.dim
+    rv = _REF_VERT[geom]
+    nv = rv.shape[0]
+    ev = [list(r) for r in mesh.elem_vertices]
+    ec = [np.array(r) for r in mesh.elem_coords]
+    next_id = int(mesh.elem_vertices.max()) + 1
+    keys = {}
+    bdr = {tuple(sorted(r)): int(a) for r, a in zip(mesh.bdr_vertices.tolist(), mesh.bdr_attr.tolist())}
+    new_bdr = {}
+
+    def shape(r):  # multilinear shape functions at reference point r
+        return np.prod([np.where(rv[:, d] > 0.5, r[d], 1.0 - r[d]) for d in range(dim)], axis=0)
+
+    def vertex_id(pv, r):
+        nonlocal next_id
+        halves = [d for d in range(dim) if abs(r[d] - 0.5) < 1e-12]
+        if not halves:  # parent corner
+            k = int(np.argmin(np.abs(rv - r).sum(1)))
+            return pv[k]
+        # the parent vertices of the smallest entity (edge / face / cell) containing r
+        fixed = [d for d in range(dim) if d not in halves]
+        ids = [pv[k] for k in range(nv) if all(abs(rv[k, d] - r[d]) < 1e-12 for d in fixed)]
+        key = (len(halves), tuple(sorted(ids)))  # the cell centre: all of the parent's ids
+        if key not in keys:
+            keys[key] = next_id
+            next_id += 1
+        return keys[key]
+
+    children_of = {}
+    for e in sorted(set(int(i) for i in elements)):
+        pv, px = ev[e], ec[e]
+        kids = []
+        for c in range(2 ** dim):
+            off = np.array([(c >> d) & 1 for d in range(dim)], float)
+            rc = (rv + off) / 2.0  # child corners in the parent's reference space
+            ids = [vertex_id(pv, r) for r in rc]
+            xs = np.array([shape(r) @ px for r in rc])
+            kids.append((ids, xs))
+        children_of[e] = kids
+        # split the parent's boundary faces
+        for lf in _LOCAL_FACES[geom]:
+            fk = tuple(sorted(pv[k] for k in lf))
+            if fk not in bdr:
+                continue
+            attr = bdr.pop(fk)
+            corner = rv[list(lf)]
+            for c in range(2 ** (dim - 1)):
+                # sub-face of the face: corners in the parent's reference space
+                s_off = [(c >> d) & 1 for d in range(dim - 1)]
+                e0 = corner[1] - corner[0]
+                e1 = corner[-1] - corner[0] if dim == 3 else np.zeros(dim)
+                pts = []
+                for a, b in ([(0, 0), (1, 0), (1, 1), (0, 1)] if dim == 3 else [(0, 0), (1, 0)]):
+                    pts.append(corner[0] + e0 * (s_off[0] + a) / 2 + (e1 * (s_off[1] + b) / 2 if dim == 3 else 0))
+                new_bdr[tuple(sorted(vertex_id(pv, p) for p in pts))] = attr
+    for e, kids in children_of.items():
+        ev[e], ec[e] = kids[0]
+        for ids, xs in kids[1:]:
+            ev.append(ids)
+            ec.append(xs)
+    bdr.update(new_bdr)
+    bv = np.array(list(bdr.keys()), np.int32).reshape(-1, _NVF[geom])
+    ba = np.array(list(bdr.values()), np.int32)
+    m = Mesh(dim, geom, np.array(ev, np.int32), np.array(ec, np.float64), bv, ba)
+    m.validate()
+    return m

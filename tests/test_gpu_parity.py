@@ -426,3 +426,61 @@ def _face_neighbours(mesh):
         for a in els:
             rows[a].update(els)
     return rows
+
+
+# ---- nonconforming (adapted) meshes ----------------------------------------
+
+def _nc_case(kind, order, rs=RS_HLLC):
+    if kind == "hex":
+        m = M.refine_nc(M.hex_grid(4, 4, 4), [21, 22, 42])
+        return cases.Case("nc", m, order, rs, 0)
+    if kind == "hexwall":
+        m = M.refine_nc(M.hex_grid(4, 4, 4, periodic=(False,) * 3), [21, 5, 63])
+        return cases.Case("nc", m, order, rs, 0, bcs=[(a, BC_SLIP, None) for a in range(1, 7)])
+    m = M.refine_nc(M.quad_grid(8, 8, periodic=(True, True)), [9, 10, 18, 45])
+    return cases.Case("nc", m, order, rs, 0)
+
+
+@pytest.mark.parametrize("kind,order,prec,variant", [
+    ("hex", 2, 0, 0), ("hex", 2, 1, 0), ("hex", 1, 0, 0), ("hex", 1, 1, 0), ("hex", 2, 0, 1),
+    ("hex", 2, 0, 2), ("hex", 1, 0, 3), ("hex", 2, 1, 4), ("hexwall", 2, 0, 0), ("hexwall", 1, 1, 0),
+    ("quad", 2, 0, 0), ("quad", 3, 0, 0), ("quad", 1, 1, 0)])
+def test_rhs_nonconforming(cuda, kind, order, prec, variant):
+    """Meshes with hanging faces (isotropic refinement of a few elements, as
+    the reference's NC AMR leaves them): right-hand side, face-only speed and
+    one step against the oracle, on every kernel family."""
+    from rkdg3d_gb300.solver import TUNE_HEX_KERNEL
+    case = _nc_case(kind, order)
+    ctx, orc = pair(case)
+    if prec:
+        ctx.set_precision(1)
+    if variant:
+        ctx.set_tuning(TUNE_HEX_KERNEL, variant)
+    tol = RHS_TOL if prec == 0 else 1e-5
+    x = random_state(ctx.node_coords(), seed=11, amp=0.05, vel=0.1)
+    y_ref, m_ref = orc.rhs(x)
+    y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    m = ctx.rhs(dev(x), y)
+    assert rel_l1(y.cpu().numpy(), y_ref) < tol
+    assert abs(m - m_ref) <= (1e-13 if prec == 0 else 1e-6) * m_ref
+    assert abs(ctx.face_speed(dev(x)) - orc.face_speed(x)) <= (1e-13 if prec == 0 else 1e-6) * m_ref
+    xs_ref, _ = orc.step(x, 1e-3)
+    xd = dev(x)
+    ctx.step(xd, 1e-3)
+    assert rel_l1(xd.cpu().numpy(), xs_ref) < tol
+
+
+def test_nonconforming_mesh_errors(cuda):
+    """A hole (faces with neither a neighbour, a boundary element nor hanging
+    faces covering them) is an invalid mesh; limiters across hanging faces
+    are not supported and say so."""
+    from rkdg3d_gb300.solver import RkdgError
+    m = M.hex_grid(3, 3, 3, periodic=(False,) * 3)
+    keep = [e for e in range(m.num_elements) if e != 13]
+    holed = M.Mesh(3, M.GEOM_CUBE, m.elem_vertices[keep], m.elem_coords[keep], m.bdr_vertices, m.bdr_attr)
+    with pytest.raises(RkdgError):
+        Context(holed, 1, device=0)
+    case = _nc_case("quad", 1)
+    ctx = Context(case.mesh, case.order, device=0)
+    with pytest.raises(RkdgError):
+        ctx.set_limiter(LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 0)

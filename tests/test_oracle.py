@@ -291,3 +291,85 @@ def test_shu_indicator_known_answers(geom, order):
     y = orc.limit(jump)
     assert not np.allclose(y, jump)
     assert np.allclose(orc.means(y), orc.means(jump), rtol=0, atol=1e-13)
+
+
+# ---- nonconforming (AMR) meshes -------------------------------------------
+
+def _nc_meshes():
+    return [(M.hex_grid(3, 3, 3, periodic=(False,) * 3), [13, 4, 22]),
+            (M.quad_grid(4, 4), [5, 6, 0])]
+
+
+def _linear_state(X, dim):
+    """Constant velocity, linear density and pressure: every flux component is
+    linear in space, so each element's right-hand side depends on that
+    element alone and every face rule integrates it exactly."""
+    n = X.shape[1]
+    rho = 1.0 + 0.1 * X[0] + 0.05 * X[1]
+    vel = [np.full(n, 0.3), np.full(n, -0.2)] + ([np.full(n, 0.1)] if dim == 3 else [])
+    p = 1.0 + 0.1 * X[1] - 0.07 * X[0] + (0.05 * X[2] if dim == 3 else 0.0)
+    return cases.conservative([rho, *vel, p], 1.4, 0.0)
+
+
+def _open_case(mesh, order):
+    from rkdg3d_gb300.solver import BC_OPEN
+    attrs = sorted(set(mesh.bdr_attr.tolist()))
+    return cases.Case("nc", mesh, order, RS_HLLC, 0, bcs=[(a, BC_OPEN, None) for a in attrs])
+
+
+@pytest.mark.parametrize("k", [0, 1])
+@pytest.mark.parametrize("order", [1, 2])
+def test_nc_faces_match_conforming_meshes(k, order):
+    """Hanging faces (slave faces integrated from the fine side, the coarse
+    element evaluated at the mapped points, master faces skipped): for a
+    state whose fluxes are linear, an unrefined element's right-hand side on
+    the nonconforming mesh equals the coarse mesh's, and a child's equals the
+    fully refined mesh's."""
+    base, ref = _nc_meshes()[k]
+    nc = M.refine_nc(base, ref)
+    full = M.refine_nc(base, range(base.num_elements))
+    dim, neq = base.dim, base.dim + 2
+    nd = (order + 1) ** dim
+
+    def rhs(m):
+        o = _oracle(_open_case(m, order))
+        y, _ = o.rhs(_linear_state(o.node_coords(), dim))
+        return y.reshape(neq, m.num_elements, nd)
+
+    Yb, Yn, Yf = rhs(base), rhs(nc), rhs(full)
+    cf = full.elem_coords.mean(1)
+    refined = set(ref)
+    err = 0.0
+    for e in range(nc.num_elements):
+        if e < base.num_elements and e not in refined:
+            err = max(err, np.abs(Yn[:, e] - Yb[:, e]).max())
+        else:
+            j = int(np.argmin(np.abs(cf - nc.elem_coords[e].mean(0)).sum(1)))
+            err = max(err, np.abs(Yn[:, e] - Yf[:, j]).max())
+    assert err < 1e-11 * np.abs(Yb).max()
+
+
+@pytest.mark.parametrize("geom", [M.GEOM_CUBE, M.GEOM_SQUARE])
+def test_nc_free_stream_and_conservation(geom):
+    if geom == M.GEOM_CUBE:
+        m = M.refine_nc(M.hex_grid(4, 4, 4), [21, 22, 42])
+    else:
+        m = M.refine_nc(M.quad_grid(5, 5, periodic=(True, True)), [6, 7, 12, 18])
+    o = _oracle(cases.Case("nc", m, 2, RS_HLLC, 0))
+    X = o.node_coords()
+    one = np.ones(X.shape[1])
+    y, _ = o.rhs(cases.conservative([1.2 * one] + [0.3 * one] * m.dim + [one], 1.4, 0.0))
+    assert np.abs(y).max() < 1e-11
+    x = random_state(X, seed=4, amp=0.05, vel=0.1)
+    y, _ = o.rhs(x)
+    assert np.abs(o.totals(y)).max() < 1e-11 * np.abs(o.totals(x)).max()
+
+
+def test_nc_mesh_with_uncovered_face_is_rejected():
+    """A lone face that is neither inside another element's face nor covered
+    by slaves (a gap in the mesh) is an invalid mesh."""
+    m = M.hex_grid(3, 3, 3, periodic=(False,) * 3)
+    keep = [e for e in range(m.num_elements) if e != 13]  # a hole in the middle
+    holed = M.Mesh(3, M.GEOM_CUBE, m.elem_vertices[keep], m.elem_coords[keep], m.bdr_vertices, m.bdr_attr)
+    with pytest.raises(Exception):
+        Oracle(holed, 1)
