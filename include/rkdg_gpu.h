@@ -114,9 +114,10 @@ int rkdg_set_physics(rkdg_ctx* ctx, int rsolver, int averaging, double gamma,
  * the coarse element across, the master face not at all.  Such a face must
  * lie inside a face of the element across it, or be covered by such faces,
  * else RKDG_ERR_INVALID (a hole; also a hanging face across a periodic seam).
- * On a mesh with hanging faces the right-hand side, steps and runs are
- * available; an active limiter, batched problems and the adjoint return
- * RKDG_ERR_UNSUPPORTED. */
+ * Limiters see the elements across hanging faces as stencil cells and
+ * evaluate indicator points on the element's own slave and master faces
+ * (limiter.cpp:95-245).  Batched problems and the adjoint on such meshes
+ * return RKDG_ERR_UNSUPPORTED. */
 int rkdg_upload_mesh(rkdg_ctx* ctx, const rkdg_mesh_desc* mesh);
 /* Deviations from the shipped reference, off by default.
  * RKDG_QUIRK_HLLC_NEGATIVE_SPEED_OK: the reference treats any negative face

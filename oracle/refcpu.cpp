@@ -614,7 +614,7 @@ struct BC {
 struct Face {
   int e1 = -1, lf1 = -1, e2 = -1, lf2 = -1;
   int fv[4] = {-1, -1, -1, -1};  // face vertex ids in elem1's local order
-  double ref2[4][3];             // elem2 reference coords of fv[k]
+  double ref2[4][3] = {};        // elem2 reference coords of fv[k]
   bool master = false;           // coarse side of nonconforming faces (not integrated)
 };
 
@@ -1636,7 +1636,9 @@ int ref_limit(ref_ctx* c, double* x) {
       for (int lf = 0; lf < c->nfpe; ++lf) {
         int fid = c->elem_face[(size_t)e * c->nfpe + lf];
         const Face& f = c->faces[fid];
-        if (f.e2 < 0) continue;  // boundary faces are not in the stencil
+        // boundary faces are not in the stencil; a master face of hanging
+        // faces is (limiter.cpp:158-161, infoNC >= 0), at the cell's own points
+        if (f.e2 < 0 && !f.master) continue;
         // the cell's own local face: Loc1 if Elem1 == iCell, else Loc2
         for (int q = 0; q < rl.n; ++q) {
           double ip1[3], ip2[3], nor[3];

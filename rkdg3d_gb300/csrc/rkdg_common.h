@@ -178,7 +178,7 @@ struct RhsParams {
 // points mapped into it; master faces carry no integrator of their own.
 struct NcParams {
   int nnc, nqf, nd, neq, nel;
-  const int* face;      // [nnc][3]: fine element, its local face, coarse element
+  const int* face;      // [nnc][4]: fine element, its local face, coarse element, its face
   const double* bnc;    // [nnc][nqf][nd]: coarse element's basis at the mapped points
   void* flux;           // [nnc][nqf][neq]: w_q |J_f| Fhat (kernel precision)
   const int* elem;      // [nel] elements with hanging-face terms
@@ -235,6 +235,12 @@ struct LimParams {
   const double* pcov;
   const int* pactive;
   int block;            // threads per CTA (0: default)
+  // hanging faces (nonconforming meshes; null otherwise): element -> CSR row
+  // of its slave-face entries (2 * face + side) and the faces [nnc][4]
+  const int* ncidx;
+  const int* nc_ptr;
+  const int* nc_ent;
+  const int* nc_face;
 };
 
 // Device-side time control of batched problems (one entry per problem).

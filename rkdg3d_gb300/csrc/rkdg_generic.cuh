@@ -430,8 +430,20 @@ __device__ __forceinline__ void shu_indicator(const LimParams& prm, const R* __r
   }
   double wsum = 0.0;
   for (int q = 0; q < T->nqs; ++q) wsum += T->ws[q];
-  for (int s = -1; s < NFPE; ++s) {
-    const int kc = s < 0 ? e : prm.fnbr[s * ne + e];
+  // stencil: the cell, its face neighbours, then the elements across its
+  // hanging faces (ElementToElementTable, limiter.cpp:118-123)
+  const int ncrow = prm.ncidx ? prm.ncidx[e] : -1;
+  const int nnc = ncrow >= 0 ? prm.nc_ptr[ncrow + 1] - prm.nc_ptr[ncrow] : 0;
+  for (int s = -1; s < NFPE + nnc; ++s) {
+    int kc;
+    if (s < 0) {
+      kc = e;
+    } else if (s < NFPE) {
+      kc = prm.fnbr[s * ne + e];
+    } else {
+      const int ent = prm.nc_ent[prm.nc_ptr[ncrow] + s - NFPE];
+      kc = prm.nc_face[(ent >> 1) * 4 + ((ent & 1) ? 0 : 2)];
+    }
     if (kc < 0) continue;  // boundary faces are not in the stencil
     // e's reference point xi -> k's reference point A xi + b
     double A[DIM][DIM], b[DIM];
@@ -608,9 +620,27 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
         MI[k] = v > MI[k] ? v : MI[k];
       }
     }
+    // hanging faces: the elements across them are stencil cells
+    // (ElementToElementTable, limiter.cpp:118-123) and the element's own
+    // slave or master faces carry indicator points (limiter.cpp:125-161)
+    unsigned ncfaces = 0;
+    if (prm.ncidx && prm.ncidx[e] >= 0) {
+      const int row = prm.ncidx[e];
+      for (int c = prm.nc_ptr[row]; c < prm.nc_ptr[row + 1]; ++c) {
+        const int f = prm.nc_ent[c] >> 1, side = prm.nc_ent[c] & 1;
+        const int nb = prm.nc_face[f * 4 + (side ? 0 : 2)];
+        ncfaces |= 1u << prm.nc_face[f * 4 + (side ? 3 : 1)];
+#pragma unroll
+        for (int k = 0; k < NEQ; ++k) {
+          const R v = (R)prm.means[(long long)k * ne + nb];
+          mI[k] = v < mI[k] ? v : mI[k];
+          MI[k] = v > MI[k] ? v : MI[k];
+        }
+      }
+    }
     for (int lf = 0; lf < NFPE; ++lf) {
       const int nb = prm.fnbr[lf * ne + e];
-      if (nb < 0) continue;  // only interior faces carry indicator points
+      if (nb < 0 && !((ncfaces >> lf) & 1u)) continue;  // only interior faces carry indicator points
 #pragma unroll
       for (int q = 0; q < NQL; ++q) {
 #pragma unroll

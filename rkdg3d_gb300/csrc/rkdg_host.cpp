@@ -390,6 +390,12 @@ LimParams lim_params(rkdg_ctx* c) {
   L.last_hope = c->last_hope;
   L.quirks = c->quirks;
   L.block = c->lim_block;
+  if (c->nnc) {
+    L.ncidx = c->d_ncidx;
+    L.nc_ptr = c->d_nc_ptr;
+    L.nc_ent = c->d_nc_ent;
+    L.nc_face = c->d_nc_face;
+  }
   return L;
 }
 
@@ -729,8 +735,6 @@ int rkdg_set_limiter(rkdg_ctx* c, int limiter, int indicator, int function, int 
     return fail(c, RKDG_ERR_UNSUPPORTED,
                 "Shu indicator with the Multi limiter: the reference multiplies by a cell "
                 "factor the Shu indicator never sets");
-  if (c->has_mesh && c->nnc && !(limiter == RKDG_LIM_FINDIFF && indicator == RKDG_IND_NOWHERE))
-    return fail(c, RKDG_ERR_UNSUPPORTED, "limiters on meshes with hanging faces are not supported");
   if ((quirk_flags & RKDG_LIMITER_LINEARIZE) && limiter == RKDG_LIM_MULTI && c->has_mesh &&
       c->geom != RKDG_GEOM_TRIANGLE && !c->tab.lin_ok)
     return fail(c, RKDG_ERR_UNSUPPORTED,
@@ -1060,8 +1064,6 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     std::string why;
     if (!rkdg::classify_nc_faces(geom, dim, nvpe, m->elem_coords, Jall, fmeas, ne, lone, slaves, why))
       return fail(c, RKDG_ERR_INVALID, why.c_str());
-    if (!slaves.empty() && c->limiter_active())
-      return fail(c, RKDG_ERR_UNSUPPORTED, "limiters on meshes with hanging faces are not supported");
     const int nns = (int)slaves.size();
     if (nns) {
       rkdg::Basis B(geom, p);
@@ -1070,7 +1072,7 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
       std::vector<double> phi(nd);
       for (int f = 0; f < nns; ++f) {
         const rkdg::NcSlave& s = slaves[f];
-        nc_face.insert(nc_face.end(), {s.e1, s.lf1, s.e2});
+        nc_face.insert(nc_face.end(), {s.e1, s.lf1, s.e2, s.lf2});
         ents[s.e1].push_back(2 * f);
         ents[s.e2].push_back(2 * f + 1);
         const double* X1 = m->elem_coords + (size_t)s.e1 * nvpe * dim;

@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(128) k_nc_flux(const __grid_constant__ RhsPara
   R lmax = R(0);
   if (t < nc.nnc * nc.nqf) {
     const int f = t / nc.nqf, q = t - f * nc.nqf;
-    const int e1 = nc.face[f * 3], lf1 = nc.face[f * 3 + 1], e2 = nc.face[f * 3 + 2];
+    const int e1 = nc.face[f * 4], lf1 = nc.face[f * 4 + 1], e2 = nc.face[f * 4 + 2];
     const int ne = prm.ne, nd = nc.nd;
     const long long NDa = prm.ndofs;
     const R* fg = (const R*)prm.fgeo;
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(128) k_nc_gather(const __grid_constant__ RhsPa
   R s = R(0);
   for (int c = nc.ptr[i]; c < nc.ptr[i + 1]; ++c) {
     const int f = nc.ent[c] >> 1, side = nc.ent[c] & 1;
-    const int lf1 = nc.face[f * 3 + 1];
+    const int lf1 = nc.face[f * 4 + 1];
     const R sg = side ? R(1) : R(-1);
     for (int q = 0; q < nqf; ++q) {
       const R phi = side ? (R)nc.bnc[((long long)f * nqf + q) * nd + j] : (R)T->B[lf1][q][j];

@@ -244,7 +244,7 @@ _LOCAL_FACES = {
 }
 
 
-def refine_nc(mesh: Mesh, elements) -> Mesh:
+def refine_nc(mesh: Mesh, elements, return_children: bool = False):
     """Isotropic refinement of the listed quadrilaterals / hexahedra into
     2^dim children each, leaving their neighbours as they are: the result is
     a nonconforming mesh with hanging vertices, as MFEM's NC refinement
@@ -254,7 +254,9 @@ def refine_nc(mesh: Mesh, elements) -> Mesh:
     edge's two ids, face centres by the face's ids), so two refined
     neighbours share them and periodic identifications carry over.  A
     refined element is replaced by its first child; the others are
-    appended.  Boundary faces of refined elements are split likewise."""
+    appended.  Boundary faces of refined elements are split likewise.  With
+    return_children, also {parent: [element of child c]} where child c sits
+    at offset ((c >> d) & 1) / 2 along reference axis d of its parent."""
     geom = mesh.geom
     if geom not in _REF_VERT:
         raise ValueError("refine_nc supports quadrilaterals and hexahedra")
@@ -313,9 +315,12 @@ def refine_nc(mesh: Mesh, elements) -> Mesh:
                 for a, b in ([(0, 0), (1, 0), (1, 1), (0, 1)] if dim == 3 else [(0, 0), (1, 0)]):
                     pts.append(corner[0] + e0 * (s_off[0] + a) / 2 + (e1 * (s_off[1] + b) / 2 if dim == 3 else 0))
                 new_bdr[tuple(sorted(vertex_id(pv, p) for p in pts))] = attr
+    child_elems = {}
     for e, kids in children_of.items():
         ev[e], ec[e] = kids[0]
+        child_elems[e] = [e]
         for ids, xs in kids[1:]:
+            child_elems[e].append(len(ev))
             ev.append(ids)
             ec.append(xs)
     bdr.update(new_bdr)
@@ -323,4 +328,39 @@ def refine_nc(mesh: Mesh, elements) -> Mesh:
     ba = np.array(list(bdr.values()), np.int32)
     m = Mesh(dim, geom, np.array(ev, np.int32), np.array(ec, np.float64), bv, ba)
     m.validate()
-    return m
+    return (m, child_elems) if return_children else m
+
+
+def prolong_refined(x: np.ndarray, dim: int, order: int, ne_old: int, ne_new: int,
+                    children: dict) -> np.ndarray:
+    """Nodal DG state (byNODES, neq = dim + 2 variables) on the mesh before
+    refine_nc -> the refined mesh: each child's nodal values are its
+    parent's polynomial at the child's Gauss-Legendre nodes, the
+    interpolation MFEM's GridFunction::Update applies to an L2 space after
+    refinement (amr.cpp:45-46); exact, so cell integrals are conserved."""
+    n1 = order + 1
+    nd, neq = n1 ** dim, dim + 2
+    t, _ = np.polynomial.legendre.leggauss(n1)
+    x1 = (t + 1.0) / 2.0  # 1D GL nodes on [0, 1]
+
+    def lagrange(s):  # l_i(s) for all i, s an array of points
+        L = np.ones((len(s), n1))
+        for i in range(n1):
+            for m in range(n1):
+                if m != i:
+                    L[:, i] *= (s - x1[m]) / (x1[i] - x1[m])
+        return L
+
+    idx = np.stack(np.unravel_index(np.arange(nd), (n1,) * dim)[::-1], 1)  # node j -> (jx, jy, jz)
+    xo = x.reshape(neq, ne_old, nd)
+    xn = np.zeros((neq, ne_new, nd))
+    xn[:, :ne_old] = xo
+    for e, kids in children.items():
+        for c, ce in enumerate(kids):
+            off = np.array([(c >> d) & 1 for d in range(dim)], float)
+            P = np.ones((nd, nd))
+            for d in range(dim):
+                Ld = lagrange((off[d] + x1[idx[:, d]]) / 2.0)  # child node -> parent basis along d
+                P *= Ld[:, idx[:, d]]
+            xn[:, ce] = xo[:, e] @ P.T
+    return xn.reshape(-1)

@@ -143,6 +143,18 @@ class Context:
         d.bdr_attr = m.bdr_attr.ctypes.data_as(_capi._ip)
         self._chk(self._L.rkdg_upload_mesh(self.h, C.byref(d)))
 
+    def update_mesh(self, mesh: Mesh):
+        """After an adapt (UpdateAndRebalance, amr.cpp:3-133): rebuild every
+        device table for the new (possibly nonconforming) mesh, as
+        UpdateAfluxPointer / UpdateInverseMassMatrix do (main.cpp:610-611).
+        Physics, boundary conditions, limiter and tableau are kept."""
+        self.mesh = mesh.contiguous()
+        self._upload()
+        ndofs = C.c_longlong()
+        self._chk(self._L.rkdg_sizes(self.h, C.byref(ndofs), None, None))
+        self.ndofs = ndofs.value
+        self.ne = self.mesh.num_elements
+
     def __del__(self):
         if getattr(self, "h", None) is not None and self.h.value:
             self._L.rkdg_destroy(self.h)

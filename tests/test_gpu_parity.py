@@ -18,7 +18,7 @@ from rkdg3d_gb300.solver import (AVG_EINFELDT, AVG_TRRS, BC_FIXED_PRESSURE_OUTLE
                                  BC_TOTAL_PRESSURE_OUTLET, FUN_BJ, FUN_MICHALAK, FUN_VENKATAKRISHNAN,
                                  IND_BJ, IND_EVERYWHERE, IND_NOWHERE, LIM_FINDIFF, LIM_MULTI,
                                  RS_HLL, RS_HLLC, RS_LLF, RS_RUSANOV, TABLEAU_REFERENCE_RK3,
-                                 TABLEAU_SSPRK3, Context)
+                                 TABLEAU_SSPRK3, Context, IND_SHU)
 from tests.helpers import periodic_case, random_state, rel_l1, walled_case
 
 pytestmark = pytest.mark.gpu
@@ -470,10 +470,33 @@ def test_rhs_nonconforming(cuda, kind, order, prec, variant):
     assert rel_l1(xd.cpu().numpy(), xs_ref) < tol
 
 
+@pytest.mark.parametrize("kind,order,lim,ind,fun", [
+    ("quad", 1, LIM_MULTI, IND_BJ, FUN_MICHALAK), ("quad", 2, LIM_FINDIFF, IND_BJ, FUN_MICHALAK),
+    ("hex", 1, LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN), ("hex", 2, LIM_MULTI, IND_BJ, FUN_BJ),
+    ("hexwall", 1, LIM_MULTI, IND_BJ, FUN_MICHALAK), ("quad", 1, LIM_FINDIFF, IND_SHU, FUN_MICHALAK),
+    ("hex", 1, LIM_FINDIFF, IND_SHU, FUN_MICHALAK)])
+def test_limiter_nonconforming(cuda, kind, order, lim, ind, fun):
+    """Limiters on meshes with hanging faces: the elements across them join
+    the stencil (ElementToElementTable) and the element's own slave or master
+    faces carry indicator points, as in limiter.cpp:95-245; limit and one
+    limited step against the oracle."""
+    case = _nc_case(kind, order)
+    case.limiter = (lim, ind, fun, 1, 0)
+    ctx, orc = pair(case)
+    x = random_state(ctx.node_coords(), seed=13, amp=0.1, vel=0.2)
+    xd = dev(x)
+    ctx.limit(xd)
+    assert rel_l1(xd.cpu().numpy(), orc.limit(x)) < 1e-12
+    xs_ref, _ = orc.step(x, 2e-4)
+    xd = dev(x)
+    ctx.step(xd, 2e-4)
+    assert rel_l1(xd.cpu().numpy(), xs_ref) < 1e-10
+
+
 def test_nonconforming_mesh_errors(cuda):
     """A hole (faces with neither a neighbour, a boundary element nor hanging
-    faces covering them) is an invalid mesh; limiters across hanging faces
-    are not supported and say so."""
+    faces covering them) is an invalid mesh; the adjoint across hanging faces
+    is not supported and says so."""
     from rkdg3d_gb300.solver import RkdgError
     m = M.hex_grid(3, 3, 3, periodic=(False,) * 3)
     keep = [e for e in range(m.num_elements) if e != 13]
@@ -481,6 +504,43 @@ def test_nonconforming_mesh_errors(cuda):
     with pytest.raises(RkdgError):
         Context(holed, 1, device=0)
     case = _nc_case("quad", 1)
-    ctx = Context(case.mesh, case.order, device=0)
+    ctx, _ = pair(case)
+    x = dev(random_state(ctx.node_coords(), seed=2, amp=0.05, vel=0.1))
     with pytest.raises(RkdgError):
-        ctx.set_limiter(LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 0)
+        ctx.rhs_vjp(x, torch.ones_like(x), torch.empty_like(x))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_adapt_and_continue(cuda, prec):
+    """The AMR cycle of main.cpp:564-696 on one context: steps on the coarse
+    mesh, refinement of a few elements with the state interpolated onto the
+    children (GridFunction::Update), rkdg_upload_mesh of the nonconforming
+    mesh into the same context (UpdateAfluxPointer / UpdateInverseMassMatrix),
+    further limited steps -- against the oracle doing the same."""
+    base = M.hex_grid(4, 4, 4)
+    case = cases.Case("adapt", base, 2, RS_HLLC, 0)
+    case.limiter = (LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 0)
+    ctx, orc = pair(case)
+    if prec:
+        ctx.set_precision(1)
+    x = random_state(ctx.node_coords(), seed=17, amp=0.05, vel=0.1)
+    xd = dev(x)
+    for _ in range(3):
+        ctx.step(xd, 1e-3)
+        x, _ = orc.step(x, 1e-3)
+    tol = 1e-10 if prec == 0 else 1e-5
+    assert rel_l1(xd.cpu().numpy(), x) < tol
+    new, kids = M.refine_nc(base, [21, 22, 42], return_children=True)
+    before = orc.totals(x)
+    xg = M.prolong_refined(xd.cpu().numpy(), 3, 2, base.num_elements, new.num_elements, kids)
+    x = M.prolong_refined(x, 3, 2, base.num_elements, new.num_elements, kids)
+    ctx.update_mesh(new)
+    orc2 = Oracle(new, 2)
+    cases.configure_oracle(cases.Case("adapt", new, 2, RS_HLLC, 0,
+                                      limiter=(LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 0)), orc2)
+    assert np.abs(orc2.totals(x) - before).max() <= 1e-13 * np.abs(before).max()  # conservative transfer
+    xd = dev(xg)
+    for _ in range(3):
+        ctx.step(xd, 5e-4)
+        x, _ = orc2.step(x, 5e-4)
+    assert rel_l1(xd.cpu().numpy(), x) < tol
