@@ -38,6 +38,7 @@ class Case:
     max_steps: int = 0
     ic: object = None         # callable(coords[dim, NDofs]) -> primitive (rho, u, v, [w], p)
     solver_quirks: int = 0    # RKDG_QUIRK_* of rkdg_set_solver_quirks
+    gas_constant: float = 1.0  # R of the pressure / temperature boundary conditions
 
     @property
     def dim(self) -> int:
@@ -265,7 +266,7 @@ def configure_batch(bc: BatchCase, ctx) -> None:
 
 
 def configure_oracle(case: Case, oracle) -> None:
-    oracle.set_physics(case.rsolver, case.averaging, case.gamma, case.covolume, 1.0)
+    oracle.set_physics(case.rsolver, case.averaging, case.gamma, case.covolume, case.gas_constant)
     for attr, t, st in case.bcs:
         oracle.set_bc(attr, t, st)
     oracle.set_limiter(*case.limiter)
@@ -277,7 +278,7 @@ def configure_context(case: Case, ctx) -> None:
     from .solver import Physics, RiemannSolver
     rs = RiemannSolver(case.averaging)
     rs.code = case.rsolver
-    ctx.set_physics(rs, Physics(case.gamma, case.covolume, 1.0))
+    ctx.set_physics(rs, Physics(case.gamma, case.covolume, case.gas_constant))
     ctx.set_solver_quirks(case.solver_quirks)
     for attr, t, st in case.bcs:
         ctx.set_bc(attr, t, st)

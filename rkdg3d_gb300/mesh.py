@@ -232,6 +232,23 @@ def read_gmsh22(path: str) -> Mesh:
     return m
 
 
+def read_gmsh22_physical_names(path: str) -> dict:
+    """$PhysicalNames of a Gmsh v2.2 ASCII file: {name: (dimension, tag)}.  The
+    reference maps each boundaryField patch name to its tag through this
+    section (case_manager.cpp:299-448, 614-660)."""
+    out = {}
+    with open(path) as fh:
+        lines = [ln.strip() for ln in fh]
+    for k, ln in enumerate(lines):
+        if ln == "$PhysicalNames":
+            n = int(lines[k + 1])
+            for r in range(n):
+                parts = lines[k + 2 + r].split(maxsplit=2)
+                out[parts[2].strip().strip('"')] = (int(parts[0]), int(parts[1]))
+            break
+    return out
+
+
 # MFEM reference vertices and local faces of the tensor elements
 _REF_VERT = {
     GEOM_SQUARE: np.array([(0, 0), (1, 0), (1, 1), (0, 1)], float),
