@@ -275,8 +275,10 @@ def refine_nc(mesh: Mesh, elements, return_children: bool = False):
     return_children, also {parent: [element of child c]} where child c sits
     at offset ((c >> d) & 1) / 2 along reference axis d of its parent."""
     geom = mesh.geom
+    if geom == GEOM_TRIANGLE:
+        return _refine_tri(mesh, elements, return_children)
     if geom not in _REF_VERT:
-        raise ValueError("refine_nc supports quadrilaterals and hexahedra")
+        raise ValueError("refine_nc supports triangles, quadrilaterals and hexahedra")
     dim = mesh.dim
     rv = _REF_VERT[geom]
     nv = rv.shape[0]
@@ -344,6 +346,49 @@ def refine_nc(mesh: Mesh, elements, return_children: bool = False):
     bv = np.array(list(bdr.keys()), np.int32).reshape(-1, _NVF[geom])
     ba = np.array(list(bdr.values()), np.int32)
     m = Mesh(dim, geom, np.array(ev, np.int32), np.array(ec, np.float64), bv, ba)
+    m.validate()
+    return (m, child_elems) if return_children else m
+
+
+def _refine_tri(mesh: Mesh, elements, return_children: bool):
+    """refine_nc for triangles: each listed triangle (v0, v1, v2) splits at
+    its edge midpoints m01, m12, m20 into (v0, m01, m20), (m01, v1, m12),
+    (m20, m12, v2) and the centre (m12, m20, m01), all counter-clockwise."""
+    ev = [list(r) for r in mesh.elem_vertices]
+    ec = [np.array(r) for r in mesh.elem_coords]
+    next_id = int(mesh.elem_vertices.max()) + 1
+    mids = {}
+    bdr = {tuple(sorted(r)): int(a) for r, a in zip(mesh.bdr_vertices.tolist(), mesh.bdr_attr.tolist())}
+
+    def mid(a, b):
+        nonlocal next_id
+        k = (min(a, b), max(a, b))
+        if k not in mids:
+            mids[k] = next_id
+            next_id += 1
+        return mids[k]
+
+    child_elems = {}
+    for e in sorted(set(int(i) for i in elements)):
+        (a, b, c), (xa, xb, xc) = ev[e], ec[e]
+        mab, mbc, mca = mid(a, b), mid(b, c), mid(c, a)
+        pab, pbc, pca = (xa + xb) / 2, (xb + xc) / 2, (xc + xa) / 2
+        kids = [([a, mab, mca], [xa, pab, pca]), ([mab, b, mbc], [pab, xb, pbc]),
+                ([mca, mbc, c], [pca, pbc, xc]), ([mbc, mca, mab], [pbc, pca, pab])]
+        for u, v, m in ((a, b, mab), (b, c, mbc), (c, a, mca)):
+            attr = bdr.pop(tuple(sorted((u, v))), None)
+            if attr is not None:
+                bdr[tuple(sorted((u, m)))] = attr
+                bdr[tuple(sorted((m, v)))] = attr
+        ev[e], ec[e] = kids[0][0], np.array(kids[0][1])
+        child_elems[e] = [e]
+        for ids, xs in kids[1:]:
+            child_elems[e].append(len(ev))
+            ev.append(ids)
+            ec.append(np.array(xs))
+    bv = np.array(list(bdr.keys()), np.int32).reshape(-1, 2)
+    ba = np.array(list(bdr.values()), np.int32)
+    m = Mesh(2, GEOM_TRIANGLE, np.array(ev, np.int32), np.array(ec, np.float64), bv, ba)
     m.validate()
     return (m, child_elems) if return_children else m
 

@@ -437,6 +437,9 @@ def _nc_case(kind, order, rs=RS_HLLC):
     if kind == "hexwall":
         m = M.refine_nc(M.hex_grid(4, 4, 4, periodic=(False,) * 3), [21, 5, 63])
         return cases.Case("nc", m, order, rs, 0, bcs=[(a, BC_SLIP, None) for a in range(1, 7)])
+    if kind == "tri":
+        m = M.refine_nc(M.tri_grid(6, 6, 0, 1, 0, 1, jitter=0.2, seed=3), [14, 15, 30])
+        return cases.Case("nc", m, order, rs, 0, bcs=[(a, BC_SLIP, None) for a in range(1, 5)])
     m = M.refine_nc(M.quad_grid(8, 8, periodic=(True, True)), [9, 10, 18, 45])
     return cases.Case("nc", m, order, rs, 0)
 
@@ -444,7 +447,8 @@ def _nc_case(kind, order, rs=RS_HLLC):
 @pytest.mark.parametrize("kind,order,prec,variant", [
     ("hex", 2, 0, 0), ("hex", 2, 1, 0), ("hex", 1, 0, 0), ("hex", 1, 1, 0), ("hex", 2, 0, 1),
     ("hex", 2, 0, 2), ("hex", 1, 0, 3), ("hex", 2, 1, 4), ("hexwall", 2, 0, 0), ("hexwall", 1, 1, 0),
-    ("quad", 2, 0, 0), ("quad", 3, 0, 0), ("quad", 1, 1, 0)])
+    ("quad", 2, 0, 0), ("quad", 3, 0, 0), ("quad", 1, 1, 0), ("tri", 1, 0, 0), ("tri", 2, 0, 0),
+    ("tri", 2, 1, 0)])
 def test_rhs_nonconforming(cuda, kind, order, prec, variant):
     """Meshes with hanging faces (isotropic refinement of a few elements, as
     the reference's NC AMR leaves them): right-hand side, face-only speed and
@@ -474,7 +478,8 @@ def test_rhs_nonconforming(cuda, kind, order, prec, variant):
     ("quad", 1, LIM_MULTI, IND_BJ, FUN_MICHALAK), ("quad", 2, LIM_FINDIFF, IND_BJ, FUN_MICHALAK),
     ("hex", 1, LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN), ("hex", 2, LIM_MULTI, IND_BJ, FUN_BJ),
     ("hexwall", 1, LIM_MULTI, IND_BJ, FUN_MICHALAK), ("quad", 1, LIM_FINDIFF, IND_SHU, FUN_MICHALAK),
-    ("hex", 1, LIM_FINDIFF, IND_SHU, FUN_MICHALAK)])
+    ("hex", 1, LIM_FINDIFF, IND_SHU, FUN_MICHALAK), ("tri", 1, LIM_MULTI, IND_BJ, FUN_MICHALAK),
+    ("tri", 2, LIM_FINDIFF, IND_SHU, FUN_MICHALAK)])
 def test_limiter_nonconforming(cuda, kind, order, lim, ind, fun):
     """Limiters on meshes with hanging faces: the elements across them join
     the stencil (ElementToElementTable) and the element's own slave or master

@@ -297,7 +297,8 @@ def test_shu_indicator_known_answers(geom, order):
 
 def _nc_meshes():
     return [(M.hex_grid(3, 3, 3, periodic=(False,) * 3), [13, 4, 22]),
-            (M.quad_grid(4, 4), [5, 6, 0])]
+            (M.quad_grid(4, 4), [5, 6, 0]),
+            (M.tri_grid(4, 4, 0, 1, 0, 1, jitter=0.2, seed=3), [9, 10, 0])]
 
 
 def _linear_state(X, dim):
@@ -317,7 +318,7 @@ def _open_case(mesh, order):
     return cases.Case("nc", mesh, order, RS_HLLC, 0, bcs=[(a, BC_OPEN, None) for a in attrs])
 
 
-@pytest.mark.parametrize("k", [0, 1])
+@pytest.mark.parametrize("k", [0, 1, 2])
 @pytest.mark.parametrize("order", [1, 2])
 def test_nc_faces_match_conforming_meshes(k, order):
     """Hanging faces (slave faces integrated from the fine side, the coarse
@@ -329,7 +330,7 @@ def test_nc_faces_match_conforming_meshes(k, order):
     nc = M.refine_nc(base, ref)
     full = M.refine_nc(base, range(base.num_elements))
     dim, neq = base.dim, base.dim + 2
-    nd = (order + 1) ** dim
+    nd = (order + 1) * (order + 2) // 2 if base.geom == M.GEOM_TRIANGLE else (order + 1) ** dim
 
     def rhs(m):
         o = _oracle(_open_case(m, order))
