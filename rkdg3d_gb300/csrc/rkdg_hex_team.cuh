@@ -354,6 +354,36 @@ __device__ __forceinline__ void team_gather_any(int lfo, const R* src,
   }
 }
 
+// Dispatch on a face's normal axis only (three code copies instead of six;
+// the side enters at run time).
+template <int P, bool GLOBAL, typename R>
+__device__ __forceinline__ void team_gather_axis(int lfo, const R* src,
+                                                 R (&nbv)[(P + 1) * (P + 1) * (P + 1)]) {
+  switch (hex_face_axis(lfo)) {  // the gather order depends on the axis only
+    case 0: team_gather<P, 2, GLOBAL>(src, nbv); break;
+    case 1: team_gather<P, 1, GLOBAL>(src, nbv); break;
+    default: team_gather<P, 0, GLOBAL>(src, nbv); break;
+  }
+}
+template <int P, typename R>
+__device__ __forceinline__ void team_contract_s_axis(int lf, const R* su, const R* lend,
+                                                     R (&v)[(P + 1) * (P + 1)]) {
+  switch (hex_face_axis(lf)) {
+    case 0: team_contract_s_ax<P, 0>(hex_face_side(lf), su, lend, v); break;
+    case 1: team_contract_s_ax<P, 1>(hex_face_side(lf), su, lend, v); break;
+    default: team_contract_s_ax<P, 2>(hex_face_side(lf), su, lend, v); break;
+  }
+}
+template <int P, int ST, typename R>
+__device__ __forceinline__ void team_lift_axis(int lf, const R* f, const R* l1d, const R* lend,
+                                               R (&acc)[(P + 1) * (P + 1) * (P + 1)]) {
+  switch (hex_face_axis(lf)) {
+    case 0: team_lift_ax<P, 0, ST>(hex_face_side(lf), f, l1d, lend, acc); break;
+    case 1: team_lift_ax<P, 1, ST>(hex_face_side(lf), f, l1d, lend, acc); break;
+    default: team_lift_ax<P, 2, ST>(hex_face_side(lf), f, l1d, lend, acc); break;
+  }
+}
+
 // Phase 1 of one face (runtime index LF) for the team's variable k: the own
 // trace and, across an interior face, the neighbour's trace at the face
 // points, stored point-major (To[q*NEQ + k], Tn[q*NEQ + k]).  The own values
@@ -374,13 +404,13 @@ __device__ __forceinline__ void team_traces(const int LF, const R* __restrict__ 
   R nbv[ND];
   if (nb >= 0) {
     if (nb >= e0 && nb < e0 + nel)  // neighbour staged in this tile
-      team_gather_any<P, false>(lfo, sU + ((nb - e0) * NEQ + k) * ND, nbv);
+      team_gather_axis<P, false>(lfo, sU + ((nb - e0) * NEQ + k) * ND, nbv);
     else
-      team_gather_any<P, true>(lfo, ug + k * NDa + (long long)nb * ND, nbv);
+      team_gather_axis<P, true>(lfo, ug + k * NDa + (long long)nb * ND, nbv);
   }
   {
     R v[N1 * N1];
-    team_contract_s_any<P>(LF, su, lend, v);
+    team_contract_s_axis<P>(LF, su, lend, v);
     team_interp<P, NEQ>(v, l1d, To + k);
   }
   if (nb >= 0) {
@@ -718,7 +748,7 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
                               cov, lmax);
       __syncwarp();
       if (MODE == 0 && nb != -1 && !prm.faces_only)
-        team_lift_any<P, NEQ>(lf, xch + 2 * NEQ * NQF + k, tL1, tLend, acc);
+        team_lift_axis<P, NEQ>(lf, xch + 2 * NEQ * NQF + k, tL1, tLend, acc);
     }
     if constexpr (MODE == 1) {
       block_max_commit<R>(lmax, prm.mcs);

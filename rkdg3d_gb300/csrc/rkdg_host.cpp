@@ -336,7 +336,7 @@ rkdg::NcParams nc_params(const rkdg_ctx* c) {
 // wanted), then the element kernel.
 cudaError_t launch_rhs_nc(rkdg_ctx* c, int prec, const RhsParams& P, const void* in, const void* ep) {
   if (c->nnc) {
-    const cudaError_t e = rkdg::launch_nc(c->dim, prec, P, nc_params(c), in, !P.faces_only, c->stream);
+    const cudaError_t e = rkdg::launch_nc(c->geom, c->p, prec, P, nc_params(c), in, !P.faces_only, c->stream);
     if (e != cudaSuccess) return e;
     c->launches += P.faces_only ? 1 : 2;
   }

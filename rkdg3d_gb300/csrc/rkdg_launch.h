@@ -27,8 +27,8 @@ cudaError_t launch_means(int geom, int p, int mode, int ne, long long ndofs,
 // Hanging faces of a nonconforming mesh (rkdg_nc.cu): fluxes at the slave
 // points (and the wave speed), then, with gather, the per-element face terms
 // prm.xface that the element kernels add.  u: FP64 (prec 0) or FP32 state.
-cudaError_t launch_nc(int dim, int prec, const RhsParams& prm, const NcParams& nc, const void* u,
-                      bool gather, cudaStream_t st);
+cudaError_t launch_nc(int geom, int p, int prec, const RhsParams& prm, const NcParams& nc,
+                      const void* u, bool gather, cudaStream_t st);
 
 cudaError_t launch_riemann_batch(int dim, int prec, int n, const double* u1, const double* u2,
                                  const double* nor, double* flux, double* speed, double gamma,

@@ -20,7 +20,9 @@
 
 namespace rkdg {
 
-template <int DIM, typename R>
+// Compile-time node and face-point counts (ND, NQF) unroll the trace and
+// gather loops, so each thread's table and state loads issue together.
+template <int DIM, int ND, int NQF, typename R>
 __global__ void __launch_bounds__(128) k_nc_flux(const __grid_constant__ RhsParams prm,
                                                  const __grid_constant__ NcParams nc,
                                                  const R* __restrict__ u) {
@@ -28,10 +30,10 @@ __global__ void __launch_bounds__(128) k_nc_flux(const __grid_constant__ RhsPara
   const RefTables* T = prm.tab;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   R lmax = R(0);
-  if (t < nc.nnc * nc.nqf) {
-    const int f = t / nc.nqf, q = t - f * nc.nqf;
+  if (t < nc.nnc * NQF) {
+    const int f = t / NQF, q = t - f * NQF;
     const int e1 = nc.face[f * 4], lf1 = nc.face[f * 4 + 1], e2 = nc.face[f * 4 + 2];
-    const int ne = prm.ne, nd = nc.nd;
+    const int ne = prm.ne;
     const long long NDa = prm.ndofs;
     const R* fg = (const R*)prm.fgeo;
     R n[DIM];
@@ -39,16 +41,23 @@ __global__ void __launch_bounds__(128) k_nc_flux(const __grid_constant__ RhsPara
     for (int c = 0; c < DIM; ++c) n[c] = fg[(long long)(lf1 * (DIM + 1) + c) * ne + e1];
     const R jac = fg[(long long)(lf1 * (DIM + 1) + DIM) * ne + e1];
     const double* B1 = T->B[lf1][q];
-    const double* B2 = nc.bnc + ((long long)f * nc.nqf + q) * nd;
+    const double* B2 = nc.bnc + ((long long)f * NQF + q) * ND;
+    R b1[ND], b2[ND];
+#pragma unroll
+    for (int s = 0; s < ND; ++s) {
+      b1[s] = (R)B1[s];
+      b2[s] = (R)B2[s];
+    }
     R s1[NEQ], s2[NEQ];
 #pragma unroll
     for (int k = 0; k < NEQ; ++k) {
-      const R* u1 = u + k * NDa + (long long)e1 * nd;
-      const R* u2 = u + k * NDa + (long long)e2 * nd;
+      const R* u1 = u + k * NDa + (long long)e1 * ND;
+      const R* u2 = u + k * NDa + (long long)e2 * ND;
       R a = R(0), b = R(0);
-      for (int s = 0; s < nd; ++s) {
-        a += u1[s] * (R)B1[s];
-        b += u2[s] * (R)B2[s];
+#pragma unroll
+      for (int s = 0; s < ND; ++s) {
+        a += u1[s] * b1[s];
+        b += u2[s] * b2[s];
       }
       s1[k] = a;
       s2[k] = b;
@@ -57,56 +66,75 @@ __global__ void __launch_bounds__(128) k_nc_flux(const __grid_constant__ RhsPara
     R F[NEQ];
     lmax = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e1);
     const R wq = (R)T->wf[q];
-    R* out = (R*)nc.flux + ((long long)f * nc.nqf + q) * NEQ;
+    R* out = (R*)nc.flux + ((long long)f * NQF + q) * NEQ;
 #pragma unroll
     for (int k = 0; k < NEQ; ++k) out[k] = (F[k] * wq) * jac;
   }
   block_max_commit<R>(lmax, prm.mcs);
 }
 
-template <int DIM, typename R>
+template <int DIM, int ND, int NQF, typename R>
 __global__ void __launch_bounds__(128) k_nc_gather(const __grid_constant__ RhsParams prm,
                                                    const __grid_constant__ NcParams nc) {
   constexpr int NEQ = DIM + 2;
   const RefTables* T = prm.tab;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nd = nc.nd, nqf = nc.nqf;
-  if (t >= nc.nel * NEQ * nd) return;
-  const int i = t / (NEQ * nd), rem = t - i * NEQ * nd;
-  const int k = rem / nd, j = rem - k * nd;
+  if (t >= nc.nel * NEQ * ND) return;
+  const int i = t / (NEQ * ND), rem = t - i * NEQ * ND;
+  const int k = rem / ND, j = rem - k * ND;
   const R* fl = (const R*)nc.flux;
   R s = R(0);
   for (int c = nc.ptr[i]; c < nc.ptr[i + 1]; ++c) {
     const int f = nc.ent[c] >> 1, side = nc.ent[c] & 1;
-    const int lf1 = nc.face[f * 4 + 1];
     const R sg = side ? R(1) : R(-1);
-    for (int q = 0; q < nqf; ++q) {
-      const R phi = side ? (R)nc.bnc[((long long)f * nqf + q) * nd + j] : (R)T->B[lf1][q][j];
-      s += sg * fl[((long long)f * nqf + q) * NEQ + k] * phi;
+    // the element's basis function j at the slave points: its own face
+    // points (fine side) or the mapped points (coarse side)
+    const double* ph = side ? nc.bnc + (long long)f * NQF * ND + j : &T->B[nc.face[f * 4 + 1]][0][j];
+    const int pst = side ? ND : RKDG_MAX_ND;
+    const R* ff = fl + (long long)f * NQF * NEQ + k;
+    R fv[NQF], pv[NQF];
+#pragma unroll
+    for (int q = 0; q < NQF; ++q) {
+      fv[q] = ff[q * NEQ];
+      pv[q] = (R)ph[q * pst];
     }
+#pragma unroll
+    for (int q = 0; q < NQF; ++q) s += sg * fv[q] * pv[q];
   }
-  ((R*)nc.xface)[((long long)i * NEQ + k) * nd + j] = s;
+  ((R*)nc.xface)[((long long)i * NEQ + k) * ND + j] = s;
+}
+
+template <int G, int P>
+static void nc_launch_gp(int prec, const RhsParams& prm, const NcParams& nc, const void* u,
+                         bool gather, cudaStream_t st) {
+  using E = El<G, P>;
+  const int bs = 128;
+  const int g1 = (nc.nnc * E::NQF + bs - 1) / bs;
+  const int g2 = (nc.nel * E::NEQ * E::ND + bs - 1) / bs;
+  if (prec == 0) {
+    k_nc_flux<E::DIM, E::ND, E::NQF, double><<<g1, bs, 0, st>>>(prm, nc, (const double*)u);
+    if (gather && g2 > 0) k_nc_gather<E::DIM, E::ND, E::NQF, double><<<g2, bs, 0, st>>>(prm, nc);
+  } else {
+    k_nc_flux<E::DIM, E::ND, E::NQF, float><<<g1, bs, 0, st>>>(prm, nc, (const float*)u);
+    if (gather && g2 > 0) k_nc_gather<E::DIM, E::ND, E::NQF, float><<<g2, bs, 0, st>>>(prm, nc);
+  }
 }
 
 // Both kernels for one right-hand-side evaluation (prec 0: FP64 state,
 // 1: FP32 stage input); the gather is skipped for the face-only speed.
-cudaError_t launch_nc(int dim, int prec, const RhsParams& prm, const NcParams& nc, const void* u,
-                      bool gather, cudaStream_t st) {
+cudaError_t launch_nc(int geom, int p, int prec, const RhsParams& prm, const NcParams& nc,
+                      const void* u, bool gather, cudaStream_t st) {
   if (nc.nnc <= 0) return cudaSuccess;
-  const int bs = 128;
-  const int g1 = (nc.nnc * nc.nqf + bs - 1) / bs;
-  const int g2 = (nc.nel * (dim + 2) * nc.nd + bs - 1) / bs;
-#define RKDG_NC_LAUNCH(D, R)                                                        \
-  do {                                                                              \
-    k_nc_flux<D, R><<<g1, bs, 0, st>>>(prm, nc, (const R*)u);                       \
-    if (gather && g2 > 0) k_nc_gather<D, R><<<g2, bs, 0, st>>>(prm, nc);            \
-  } while (0)
-  if (dim == 2) {
-    if (prec == 0) RKDG_NC_LAUNCH(2, double); else RKDG_NC_LAUNCH(2, float);
-  } else {
-    if (prec == 0) RKDG_NC_LAUNCH(3, double); else RKDG_NC_LAUNCH(3, float);
+  switch (geom * 10 + p) {
+    case 21: nc_launch_gp<2, 1>(prec, prm, nc, u, gather, st); break;
+    case 22: nc_launch_gp<2, 2>(prec, prm, nc, u, gather, st); break;
+    case 31: nc_launch_gp<3, 1>(prec, prm, nc, u, gather, st); break;
+    case 32: nc_launch_gp<3, 2>(prec, prm, nc, u, gather, st); break;
+    case 33: nc_launch_gp<3, 3>(prec, prm, nc, u, gather, st); break;
+    case 51: nc_launch_gp<5, 1>(prec, prm, nc, u, gather, st); break;
+    case 52: nc_launch_gp<5, 2>(prec, prm, nc, u, gather, st); break;
+    default: return cudaErrorInvalidValue;
   }
-#undef RKDG_NC_LAUNCH
   return cudaGetLastError();
 }
 
