@@ -763,7 +763,7 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
       R fv[NQF];
 #pragma unroll
       for (int q = 0; q < NQF; ++q) fv[q] = __ldg(fs + lf * (NEQ * NQF) + q);
-      team_lift_any<P, 1>(lf, fv, tL1, tLend, acc);
+      team_lift_axis<P, 1>(lf, fv, tL1, tLend, acc);
     }
   }
   // neighbours inside the tile were read from the staged DOFs, which the

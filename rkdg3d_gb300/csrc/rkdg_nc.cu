@@ -11,8 +11,8 @@
 // kernels supply their terms:
 //   k_nc_flux    one thread per slave-face point: both traces, the numerical
 //                flux (Elem1, Elem2 order), the wave speed, w_q |J_f| Fhat;
-//   k_nc_gather  one thread per (element, variable, node) of an element
-//                touched by hanging faces: its face term, summed over its
+//   k_nc_gather  one thread per (element, node) of an element touched by
+//                hanging faces: its face terms, summed over its
 //                slave faces and points in a fixed order (no atomics), added
 //                by the element kernels before the inverse mass.
 #include "rkdg_generic.cuh"
@@ -78,12 +78,13 @@ __global__ void __launch_bounds__(128) k_nc_gather(const __grid_constant__ RhsPa
                                                    const __grid_constant__ NcParams nc) {
   constexpr int NEQ = DIM + 2;
   const RefTables* T = prm.tab;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nc.nel * NEQ * ND) return;
-  const int i = t / (NEQ * ND), rem = t - i * NEQ * ND;
-  const int k = rem / ND, j = rem - k * ND;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (element, node j), all variables
+  if (t >= nc.nel * ND) return;
+  const int i = t / ND, j = t - i * ND;
   const R* fl = (const R*)nc.flux;
-  R s = R(0);
+  R s[NEQ];
+#pragma unroll
+  for (int k = 0; k < NEQ; ++k) s[k] = R(0);
   for (int c = nc.ptr[i]; c < nc.ptr[i + 1]; ++c) {
     const int f = nc.ent[c] >> 1, side = nc.ent[c] & 1;
     const R sg = side ? R(1) : R(-1);
@@ -91,17 +92,16 @@ __global__ void __launch_bounds__(128) k_nc_gather(const __grid_constant__ RhsPa
     // points (fine side) or the mapped points (coarse side)
     const double* ph = side ? nc.bnc + (long long)f * NQF * ND + j : &T->B[nc.face[f * 4 + 1]][0][j];
     const int pst = side ? ND : RKDG_MAX_ND;
-    const R* ff = fl + (long long)f * NQF * NEQ + k;
-    R fv[NQF], pv[NQF];
+    const R* ff = fl + (long long)f * NQF * NEQ;
 #pragma unroll
     for (int q = 0; q < NQF; ++q) {
-      fv[q] = ff[q * NEQ];
-      pv[q] = (R)ph[q * pst];
-    }
+      const R w = sg * (R)ph[q * pst];
 #pragma unroll
-    for (int q = 0; q < NQF; ++q) s += sg * fv[q] * pv[q];
+      for (int k = 0; k < NEQ; ++k) s[k] += ff[q * NEQ + k] * w;
+    }
   }
-  ((R*)nc.xface)[((long long)i * NEQ + k) * ND + j] = s;
+#pragma unroll
+  for (int k = 0; k < NEQ; ++k) ((R*)nc.xface)[((long long)i * NEQ + k) * ND + j] = s[k];
 }
 
 template <int G, int P>
@@ -110,7 +110,7 @@ static void nc_launch_gp(int prec, const RhsParams& prm, const NcParams& nc, con
   using E = El<G, P>;
   const int bs = 128;
   const int g1 = (nc.nnc * E::NQF + bs - 1) / bs;
-  const int g2 = (nc.nel * E::NEQ * E::ND + bs - 1) / bs;
+  const int g2 = (nc.nel * E::ND + bs - 1) / bs;
   if (prec == 0) {
     k_nc_flux<E::DIM, E::ND, E::NQF, double><<<g1, bs, 0, st>>>(prm, nc, (const double*)u);
     if (gather && g2 > 0) k_nc_gather<E::DIM, E::ND, E::NQF, double><<<g2, bs, 0, st>>>(prm, nc);
