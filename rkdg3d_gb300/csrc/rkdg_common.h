@@ -180,7 +180,7 @@ struct NcParams {
   int nnc, nqf, nd, neq, nel;
   const int* face;      // [nnc][4]: fine element, its local face, coarse element, its face
   const double* bnc;    // [nnc][nqf][nd]: coarse element's basis at the mapped points
-  void* flux;           // [nnc][nqf][neq]: w_q |J_f| Fhat (kernel precision)
+  void* flux;           // [nnc][2][neq][nd]: each face's term for its fine and coarse element
   const int* elem;      // [nel] elements with hanging-face terms
   const int* ptr;       // [nel + 1] CSR rows of ent
   const int* ent;       // 2 * slave face + side (0: fine, 1: coarse)

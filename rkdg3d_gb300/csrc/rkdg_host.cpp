@@ -1135,7 +1135,7 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     c->nc_nel = (int)nc_elem.size();
     CUDA_TRY(c, dalloc(c->d_nc_face, nc_face.size()));
     CUDA_TRY(c, dalloc(c->d_nc_bnc, nc_bnc.size()));
-    CUDA_TRY(c, dalloc(c->d_nc_flux, (size_t)nns * T.nqf * neq));
+    CUDA_TRY(c, dalloc(c->d_nc_flux, (size_t)nns * 2 * neq * nd));  // per face: both elements' terms
     CUDA_TRY(c, dalloc(c->d_nc_elem, nc_elem.size()));
     CUDA_TRY(c, dalloc(c->d_nc_ptr, nc_ptr.size()));
     CUDA_TRY(c, dalloc(c->d_nc_ent, nc_ent.size()));

@@ -9,29 +9,39 @@
 // points mapped into it -- and skips the master face.  The element kernels
 // treat both kinds of face as faces without an integrator; these two
 // kernels supply their terms:
-//   k_nc_flux    one thread per slave-face point: both traces, the numerical
-//                flux (Elem1, Elem2 order), the wave speed, w_q |J_f| Fhat;
+//   k_nc_face    64 / NQF slave faces per CTA: both traces at each point, the
+//                numerical flux (Elem1, Elem2 order), the wave speed, then the
+//                face's term for each of its two elements;
 //   k_nc_gather  one thread per (element, node) of an element touched by
-//                hanging faces: its face terms, summed over its
-//                slave faces and points in a fixed order (no atomics), added
-//                by the element kernels before the inverse mass.
+//                hanging faces: the sum of its faces' terms in a fixed order
+//                (no atomics), which the element kernels add before the
+//                inverse mass.
 #include "rkdg_generic.cuh"
 #include "rkdg_launch.h"
 
 namespace rkdg {
 
-// Compile-time node and face-point counts (ND, NQF) unroll the trace and
-// gather loops, so each thread's table and state loads issue together.
+// Compile-time node and face-point counts (ND, NQF) unroll the loops.
+// k_nc_face: FPC = 64 / NQF slave faces per CTA.  Each thread evaluates one
+// point flux into shared memory; then the CTA forms each face's term for
+// both its elements, term[side][k][j] = sign * sum_q w_q |J_f| Fhat_k(q)
+// phi_j(q) (phi of the fine element's own face points, or of the coarse
+// element at the mapped points), sign -1 on the fine (Elem1) side.
+constexpr int kNcFaceThreads = 64;
+
 template <int DIM, int ND, int NQF, typename R>
-__global__ void __launch_bounds__(128) k_nc_flux(const __grid_constant__ RhsParams prm,
-                                                 const __grid_constant__ NcParams nc,
-                                                 const R* __restrict__ u) {
-  constexpr int NEQ = DIM + 2;
+__global__ void __launch_bounds__(kNcFaceThreads) k_nc_face(const __grid_constant__ RhsParams prm,
+                                                            const __grid_constant__ NcParams nc,
+                                                            const R* __restrict__ u,
+                                                            int with_terms) {
+  constexpr int NEQ = DIM + 2, FPC = kNcFaceThreads / NQF;
+  static_assert(FPC >= 1, "one thread per face point");
+  __shared__ R sF[FPC][NQF][NEQ];
   const RefTables* T = prm.tab;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lf = threadIdx.x / NQF, q = threadIdx.x - lf * NQF;
+  const int f = blockIdx.x * FPC + lf;
   R lmax = R(0);
-  if (t < nc.nnc * NQF) {
-    const int f = t / NQF, q = t - f * NQF;
+  if (lf < FPC && f < nc.nnc) {
     const int e1 = nc.face[f * 4], lf1 = nc.face[f * 4 + 1], e2 = nc.face[f * 4 + 2];
     const int ne = prm.ne;
     const long long NDa = prm.ndofs;
@@ -66,39 +76,50 @@ __global__ void __launch_bounds__(128) k_nc_flux(const __grid_constant__ RhsPara
     R F[NEQ];
     lmax = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e1);
     const R wq = (R)T->wf[q];
-    R* out = (R*)nc.flux + ((long long)f * NQF + q) * NEQ;
 #pragma unroll
-    for (int k = 0; k < NEQ; ++k) out[k] = (F[k] * wq) * jac;
+    for (int k = 0; k < NEQ; ++k) sF[lf][q][k] = (F[k] * wq) * jac;
   }
-  block_max_commit<R>(lmax, prm.mcs);
+  block_max_commit<R>(lmax, prm.mcs);  // contains a CTA barrier: sF is complete after it
+  if (!with_terms) return;
+  for (int o = threadIdx.x; o < FPC * 2 * ND; o += blockDim.x) {
+    const int c = o / (2 * ND), r = o - c * 2 * ND;
+    const int side = r / ND, j = r - side * ND;
+    const int fc = blockIdx.x * FPC + c;
+    if (fc >= nc.nnc) break;
+    const int lf1 = nc.face[fc * 4 + 1];
+    const R sg = side ? R(1) : R(-1);
+    R acc[NEQ];
+#pragma unroll
+    for (int k = 0; k < NEQ; ++k) acc[k] = R(0);
+#pragma unroll
+    for (int qq = 0; qq < NQF; ++qq) {
+      const R w = sg * (R)(side ? nc.bnc[((long long)fc * NQF + qq) * ND + j] : T->B[lf1][qq][j]);
+#pragma unroll
+      for (int k = 0; k < NEQ; ++k) acc[k] += sF[c][qq][k] * w;
+    }
+    R* term = (R*)nc.flux + (long long)fc * 2 * NEQ * ND;
+#pragma unroll
+    for (int k = 0; k < NEQ; ++k) term[(side * NEQ + k) * ND + j] = acc[k];
+  }
 }
 
-template <int DIM, int ND, int NQF, typename R>
-__global__ void __launch_bounds__(128) k_nc_gather(const __grid_constant__ RhsParams prm,
-                                                   const __grid_constant__ NcParams nc) {
+// k_nc_gather: one thread per (element, node) of an element touched by
+// hanging faces, adding its faces' terms in list order.
+template <int DIM, int ND, typename R>
+__global__ void __launch_bounds__(128) k_nc_gather(const __grid_constant__ NcParams nc) {
   constexpr int NEQ = DIM + 2;
-  const RefTables* T = prm.tab;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (element, node j), all variables
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc.nel * ND) return;
   const int i = t / ND, j = t - i * ND;
-  const R* fl = (const R*)nc.flux;
+  const R* terms = (const R*)nc.flux;
   R s[NEQ];
 #pragma unroll
   for (int k = 0; k < NEQ; ++k) s[k] = R(0);
   for (int c = nc.ptr[i]; c < nc.ptr[i + 1]; ++c) {
     const int f = nc.ent[c] >> 1, side = nc.ent[c] & 1;
-    const R sg = side ? R(1) : R(-1);
-    // the element's basis function j at the slave points: its own face
-    // points (fine side) or the mapped points (coarse side)
-    const double* ph = side ? nc.bnc + (long long)f * NQF * ND + j : &T->B[nc.face[f * 4 + 1]][0][j];
-    const int pst = side ? ND : RKDG_MAX_ND;
-    const R* ff = fl + (long long)f * NQF * NEQ;
+    const R* tv = terms + ((long long)f * 2 + side) * NEQ * ND + j;
 #pragma unroll
-    for (int q = 0; q < NQF; ++q) {
-      const R w = sg * (R)ph[q * pst];
-#pragma unroll
-      for (int k = 0; k < NEQ; ++k) s[k] += ff[q * NEQ + k] * w;
-    }
+    for (int k = 0; k < NEQ; ++k) s[k] += tv[k * ND];
   }
 #pragma unroll
   for (int k = 0; k < NEQ; ++k) ((R*)nc.xface)[((long long)i * NEQ + k) * ND + j] = s[k];
@@ -108,15 +129,15 @@ template <int G, int P>
 static void nc_launch_gp(int prec, const RhsParams& prm, const NcParams& nc, const void* u,
                          bool gather, cudaStream_t st) {
   using E = El<G, P>;
-  const int bs = 128;
-  const int g1 = (nc.nnc * E::NQF + bs - 1) / bs;
-  const int g2 = (nc.nel * E::ND + bs - 1) / bs;
+  const int fpc = kNcFaceThreads / E::NQF;
+  const int g1 = (nc.nnc + fpc - 1) / fpc;
+  const int g2 = (nc.nel * E::ND + 127) / 128;
   if (prec == 0) {
-    k_nc_flux<E::DIM, E::ND, E::NQF, double><<<g1, bs, 0, st>>>(prm, nc, (const double*)u);
-    if (gather && g2 > 0) k_nc_gather<E::DIM, E::ND, E::NQF, double><<<g2, bs, 0, st>>>(prm, nc);
+    k_nc_face<E::DIM, E::ND, E::NQF, double><<<g1, kNcFaceThreads, 0, st>>>(prm, nc, (const double*)u, gather);
+    if (gather && g2 > 0) k_nc_gather<E::DIM, E::ND, double><<<g2, 128, 0, st>>>(nc);
   } else {
-    k_nc_flux<E::DIM, E::ND, E::NQF, float><<<g1, bs, 0, st>>>(prm, nc, (const float*)u);
-    if (gather && g2 > 0) k_nc_gather<E::DIM, E::ND, E::NQF, float><<<g2, bs, 0, st>>>(prm, nc);
+    k_nc_face<E::DIM, E::ND, E::NQF, float><<<g1, kNcFaceThreads, 0, st>>>(prm, nc, (const float*)u, gather);
+    if (gather && g2 > 0) k_nc_gather<E::DIM, E::ND, float><<<g2, 128, 0, st>>>(nc);
   }
 }
 
