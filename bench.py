@@ -52,9 +52,9 @@ def workload_config(case, n_elem_side):
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element per
 # stage launch of k_rhs_hex_team<2,float>: mean of the three stage launches of
-# one RK step captured with ncu on the 48^3 pulse (329.4 MB / 110,592
+# one RK step captured with ncu on the 48^3 pulse (329.5 MB / 110,592
 # elements); traffic scales with the element count.
-TRAFFIC_BYTES_PER_ELEMENT_LAUNCH = 2978.0
+TRAFFIC_BYTES_PER_ELEMENT_LAUNCH = 2979.5
 
 
 def algorithmic_bytes_per_step(N, ne, precision):
@@ -361,6 +361,9 @@ def run_config(args, local):
       c4  256 batched Riemann problems on N x 4 strips, one graph launch, to t = 0.15
       c5  adjoint: 32^3 Q1 Gaussian pulses, HLLC + Venkatakrishnan, 200 fixed-dt
           steps forward, then the checkpointed adjoint run (every 20 steps)
+      c6  adapted mesh: the C2 pulse on a 48^3 Q2 mesh whose elements within
+          0.15 of the pulse centre are refined once (hanging faces), against
+          the same pulse on the conforming 48^3 mesh, 100 fixed-dt steps
     FP64 and FP32-bulk runs of the same workload with the density / energy error
     of the latter against the former, and the FP64 oracle on a bounded sample."""
     import torch
@@ -471,6 +474,42 @@ def run_config(args, local):
                                               "elements) run alone, FP64 oracle"}
         except refcpu.OracleError as ex:
             line["cpu_baseline"] = {"unavailable": str(ex)[:80]}
+    elif w == "c6":
+        from rkdg3d_gb300 import mesh as M
+        base = cases.pulse3d(n=48)
+        cen = base.mesh.elem_coords.mean(1)
+        ref = np.flatnonzero(np.linalg.norm(cen - 0.5, axis=1) < 0.15)
+        nc = cases.pulse3d(n=48)
+        nc.mesh = M.refine_nc(base.mesh, ref)
+        steps = args.config_steps // 2
+        out = {}
+        for label, case in (("conforming", base), ("adapted", nc)):
+            for name, prec in (("fp64", FP64), ("fp32_bulk", FP32_BULK)):
+                ctx = context(case, prec)
+                x0 = torch.tensor(cases.project(case, ctx.node_coords()), dtype=torch.float64,
+                                  device=dev)
+                dt = case.cfl * ctx.hmin() / ctx.face_speed(x0) / (2 * case.order + 1)
+                x = x0.clone()
+                ctx.run(x, 1e30, dt0=dt, dt_mode=2, max_steps=2)  # warm-up
+                x = x0.clone()
+                info, sec = timed(lambda: ctx.run(x, 1e30, dt0=dt, dt_mode=2, max_steps=steps))
+                out[(label, name)] = x.cpu().numpy()
+                line.setdefault(label, {})[name] = {"value": ctx.n * STAGES * steps / sec,
+                                                    "ms_per_step": 1e3 * sec / steps}
+                line[label]["unknowns"] = ctx.n
+                line[label]["elements"] = ctx.ne
+            line[label]["error_fp32_bulk_vs_fp64"] = errors(out[(label, "fp32_bulk")],
+                                                           out[(label, "fp64")], ctx.ndofs)
+        line["adapted"]["refined_elements"] = int(len(ref))
+        orc = refcpu.Oracle(nc.mesh, nc.order)
+        cases.configure_oracle(nc, orc)
+        refcpu.set_threads(threads)
+        xo = cases.project(nc, orc.node_coords())
+        t0 = time.perf_counter()
+        orc.run(xo, 1e30, dt0=dt, dt_mode=2, max_steps=2)
+        sec = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": orc.n * STAGES * 2 / sec, "cores": threads,
+                                "kind": "port", "sample": "2 RK steps on the adapted mesh, FP64 oracle"}
     elif w == "c5":
         case = cases.gaussian_pulses(n=32, seed=0)
         ctx = context(case, FP64)
@@ -511,8 +550,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--hex-kernel", type=int, default=0,
                     help="RKDG_TUNE_HEX_KERNEL of the FP32-bulk context (0: library default)")
-    ap.add_argument("--config", default="c2", choices=["c2", "c1", "c3", "c4", "c5"],
-                    help="c2: the headline pulse (default); c1/c3/c4/c5: the other "
+    ap.add_argument("--config", default="c2", choices=["c2", "c1", "c3", "c4", "c5", "c6"],
+                    help="c2: the headline pulse (default); c1/c3/c4/c5/c6: the other "
                          "configurations, one JSON line each")
     ap.add_argument("--config-steps", type=int, default=200,
                     help="RK steps of the c3 runs (first steps of the t = 0.2 run)")
