@@ -114,6 +114,10 @@ int rkdg_set_physics(rkdg_ctx* ctx, int rsolver, int averaging, double gamma,
  * the coarse element across, the master face not at all.  Such a face must
  * lie inside a face of the element across it, or be covered by such faces,
  * else RKDG_ERR_INVALID (a hole; also a hanging face across a periodic seam).
+ * Elements: affine triangles, parallelograms and parallelepipeds, and
+ * general (bilinear) quadrilaterals; non-affine hexahedra return
+ * RKDG_ERR_UNSUPPORTED, as do the Shu indicator and the adjoint on
+ * non-parallelogram quadrilaterals.
  * Limiters see the elements across hanging faces as stencil cells and
  * evaluate indicator points on the element's own slave and master faces
  * (limiter.cpp:95-245).  Batched problems and the adjoint on such meshes

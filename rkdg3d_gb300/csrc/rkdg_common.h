@@ -76,6 +76,10 @@ struct RefTables {
   // arbitrary reference points needs: the 1D GL nodes (tensor elements) or
   // the monomial expansion phi_j = sum_m tcoef[m][j] x^tmono[m][0] y^tmono[m][1]
   // (triangles)
+  // non-parallelogram quadrilateral meshes: cell-mean weights of each
+  // element [ne][nd] on the device (null when every element is affine and
+  // wmean serves all)
+  const double* wmn_e;
   int nqs;
   double xs[RKDG_MAX_NQS][3];
   double ws[RKDG_MAX_NQS];
@@ -169,6 +173,9 @@ struct RhsParams {
   // added to the element's face + volume terms before the inverse mass
   const int* ncidx;
   const void* xface;
+  // non-parallelogram quadrilaterals: adj(J) and 1/det J at every node,
+  // [dim*dim + 1][nd][ne] in the kernel's precision (null: egeo per element)
+  const void* ngeo;
   HexOpsPair hops;      // hexahedra (order <= 2): 1D operators
 };
 

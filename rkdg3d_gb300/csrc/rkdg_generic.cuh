@@ -297,6 +297,7 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
     }
     if (!prm.faces_only) {
       const R* eg = (const R*)prm.egeo;
+      const R* ng = (const R*)prm.ngeo;  // per-node geometry (bilinear quads) or null
       R adj[DIM][DIM];
 #pragma unroll
       for (int r = 0; r < DIM; ++r)
@@ -305,6 +306,12 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
       const R idet = eg[(long long)(DIM * DIM) * ne + e];
 #pragma unroll
       for (int m = 0; m < ND; ++m) {
+        if (ng) {
+#pragma unroll
+          for (int r = 0; r < DIM; ++r)
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) adj[r][d] = ng[((long long)(r * DIM + d) * ND + m) * ne + e];
+        }
         R st[NEQ];
 #pragma unroll
         for (int k = 0; k < NEQ; ++k) st[k] = u[k * NDa + (long long)e * ND + m];
@@ -340,9 +347,18 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
           R v = R(0);
 #pragma unroll
           for (int j = 0; j < ND; ++j) v += sMinv[i][j] * acc[k][j];
-          y[i] = v * idet;
+          // the collocated mass of a quad is diagonal, so a per-node 1/det J
+          // (bilinear quads) applies row by row
+          y[i] = v * (ng ? ng[((long long)(DIM * DIM) * ND + i) * ne + e] : idet);
         }
-        epilogue<ND, R>(ep, k * NDa + (long long)e * ND, y, sWm, ne, e, k, dts);
+        if (T->wmn_e) {  // this element's own cell-mean weights
+          R wl[ND];
+#pragma unroll
+          for (int i = 0; i < ND; ++i) wl[i] = (R)T->wmn_e[(long long)e * ND + i];
+          epilogue<ND, R>(ep, k * NDa + (long long)e * ND, y, wl, ne, e, k, dts);
+        } else {
+          epilogue<ND, R>(ep, k * NDa + (long long)e * ND, y, sWm, ne, e, k, dts);
+        }
       }
     }
   }
@@ -797,7 +813,7 @@ __global__ void k_means_generic(int ne, long long ndofs, const RefTables* tab,
     for (int j = 0; j < ND; ++j) {
       double v = (double)u[k * ndofs + (long long)e * ND + j];
       if (ulo) v += (double)ulo[k * ndofs + (long long)e * ND + j];
-      m += tab->wmean[j] * v;
+      m += (tab->wmn_e ? tab->wmn_e[(long long)e * ND + j] : tab->wmean[j]) * v;
     }
     means[(long long)k * ne + e] = m;
   }

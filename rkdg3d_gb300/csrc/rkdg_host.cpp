@@ -55,6 +55,13 @@ struct rkdg_ctx {
   int hsched_rounds = 0;
   // hanging faces of a nonconforming mesh (see rkdg_nc.cu)
   int nnc = 0, nc_nel = 0;
+  // non-parallelogram quadrilaterals: per-node adj(J) and 1/det J
+  // [dim*dim + 1][nd][ne] and per-element cell-mean weights [ne][nd]
+  int nonaffine = 0;
+  double* d_ngeo64 = nullptr;
+  float* d_ngeo32 = nullptr;
+  double* d_wmn64 = nullptr;
+  float* d_wmn32 = nullptr;
   int* d_nc_face = nullptr;
   double* d_nc_bnc = nullptr;
   double* d_nc_flux = nullptr;
@@ -198,6 +205,11 @@ void free_mesh(rkdg_ctx* c) {
   dfree(c->d_ncidx);
   dfree(c->d_xface);
   c->nnc = c->nc_nel = 0;
+  dfree(c->d_ngeo64);
+  dfree(c->d_ngeo32);
+  dfree(c->d_wmn64);
+  dfree(c->d_wmn32);
+  c->nonaffine = 0;
   c->nprob = 0;
   c->has_mesh = false;
 }
@@ -290,6 +302,7 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   P.hsched = c->d_hsched;
   P.ncidx = c->nnc ? c->d_ncidx : nullptr;
   P.xface = c->d_xface;
+  P.ngeo = c->nonaffine ? (prec == 0 ? (const void*)c->d_ngeo64 : (const void*)c->d_ngeo32) : nullptr;
   if (c->geom == RKDG_GEOM_CUBE && c->p <= 2) {
     const int n1 = c->p + 1, nq1 = c->p + 2;
     const RefTables& T = c->tab;
@@ -731,6 +744,9 @@ int rkdg_set_limiter(rkdg_ctx* c, int limiter, int indicator, int function, int 
   if (!c) return RKDG_ERR_INVALID;
   if (limiter < 0 || limiter > 1 || indicator < 0 || indicator > 3 || function < 0 || function > 2)
     return fail(c, RKDG_ERR_INVALID, "invalid limiter configuration");
+  if (indicator == RKDG_IND_SHU && c->has_mesh && c->nonaffine)
+    return fail(c, RKDG_ERR_UNSUPPORTED,
+                "the Shu indicator maps between elements affinely: not on non-parallelogram quads");
   if (indicator == RKDG_IND_SHU && limiter == RKDG_LIM_MULTI)
     return fail(c, RKDG_ERR_UNSUPPORTED,
                 "Shu indicator with the Multi limiter: the reference multiplies by a cell "
@@ -852,14 +868,25 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     double scale = 0;
     for (int r = 0; r < dim; ++r)
       for (int i = 0; i < dim; ++i) scale = std::max(scale, std::fabs(col[r][i]));
+    bool affine = true;
     for (int v = 0; v < nvpe; ++v) {
       const double* rv = rkdg::kRefVert[gs][v];
       for (int i = 0; i < dim; ++i) {
         double pred = X[i];
         for (int r = 0; r < dim; ++r) pred += rv[r] * col[r][i];
-        if (std::fabs(pred - X[v * dim + i]) > 1e-9 * scale)
-          return fail(c, RKDG_ERR_UNSUPPORTED, "non-affine element (only affine elements are supported)", e);
+        if (std::fabs(pred - X[v * dim + i]) > 1e-9 * scale) affine = false;
       }
+    }
+    if (!affine) {
+      if (geom != RKDG_GEOM_SQUARE)
+        return fail(c, RKDG_ERR_UNSUPPORTED,
+                    "non-affine hexahedron (bilinear quadrilaterals and affine elements are supported)", e);
+      // bilinear quadrilateral: J at the element centre (Mesh::GetElementSize)
+      for (int i = 0; i < 2; ++i) {
+        col[0][i] = 0.5 * ((X[2 + i] - X[i]) + (X[4 + i] - X[6 + i]));
+        col[1][i] = 0.5 * ((X[6 + i] - X[i]) + (X[4 + i] - X[2 + i]));
+      }
+      c->nonaffine++;
     }
     double J[9] = {0};
     for (int i = 0; i < dim; ++i)
@@ -901,6 +928,47 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     std::memcpy(&Jall[(size_t)e * 9], J, sizeof J);
   }
   c->hmin = hmin;
+  // ---- non-parallelogram (bilinear) quadrilaterals ----
+  // The volume and mass rules of quads are the Gauss-Legendre nodes (orders
+  // 2p and 2p + 1), so the element operator only needs adj(J) and det J at
+  // the nodes; cell means use the averages rule (order p + 1) with det J.
+  std::vector<double> h_ngeo, h_wmn;
+  if (c->nonaffine) {
+    rkdg::Basis B(geom, p);
+    std::vector<double> rx, rw, phi(nd);
+    rkdg::mean_rule(geom, p, rx, rw);
+    h_ngeo.assign((size_t)5 * nd * ne, 0.0);
+    h_wmn.assign((size_t)ne * nd, 0.0);
+    for (int e = 0; e < ne; ++e) {
+      const double* X = m->elem_coords + (size_t)e * 8;
+      auto jac = [&](const double* xi, double* J) {  // J[i*2 + r] = dx_i / dxi_r
+        const double s = xi[0], t = xi[1];
+        for (int i = 0; i < 2; ++i) {
+          J[i * 2] = (1 - t) * (X[2 + i] - X[i]) + t * (X[4 + i] - X[6 + i]);
+          J[i * 2 + 1] = (1 - s) * (X[6 + i] - X[i]) + s * (X[4 + i] - X[2 + i]);
+        }
+        return J[0] * J[3] - J[1] * J[2];
+      };
+      for (int j = 0; j < nd; ++j) {
+        double J[4];
+        const double det = jac(&B.nodes[j * 2], J);
+        if (!(det > 0.0)) return fail(c, RKDG_ERR_INVALID, "inverted or degenerate element", e);
+        const double adj[4] = {J[3], -J[1], -J[2], J[0]};
+        for (int rd = 0; rd < 4; ++rd) h_ngeo[((size_t)rd * nd + j) * ne + e] = adj[rd];
+        h_ngeo[((size_t)4 * nd + j) * ne + e] = 1.0 / det;
+      }
+      double area = 0.0;
+      for (size_t q = 0; q < rw.size(); ++q) {
+        double J[4];
+        const double w = rw[q] * jac(&rx[q * 2], J);
+        B.eval(&rx[q * 2], phi.data(), nullptr);
+        for (int j = 0; j < nd; ++j) h_wmn[(size_t)e * nd + j] += w * phi[j];
+        area += w;
+      }
+      for (int j = 0; j < nd; ++j) h_wmn[(size_t)e * nd + j] /= area;
+      c->h_wdet[e] = area;
+    }
+  }
   {
     rkdg::Basis B(geom, p);
     for (int e = 0; e < ne; ++e) {
@@ -909,7 +977,12 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
       for (int j = 0; j < nd; ++j)
         for (int i = 0; i < dim; ++i) {
           double v = X[i];
-          for (int r = 0; r < dim; ++r) v += J[i * dim + r] * B.nodes[j * dim + r];
+          if (c->nonaffine && geom == RKDG_GEOM_SQUARE) {  // bilinear map
+            const double s = B.nodes[j * 2], t = B.nodes[j * 2 + 1];
+            v = (1 - s) * (1 - t) * X[i] + s * (1 - t) * X[2 + i] + s * t * X[4 + i] + (1 - s) * t * X[6 + i];
+          } else {
+            for (int r = 0; r < dim; ++r) v += J[i * dim + r] * B.nodes[j * dim + r];
+          }
           c->h_nodes[(size_t)i * c->ndofs + (long long)e * nd + j] = v;
         }
     }
@@ -1062,6 +1135,8 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     for (int lf = 0; lf < nfpe; ++lf)
       for (int e = 0; e < ne; ++e) fmeas[(size_t)lf * ne + e] = c->h_fgeo[(size_t)(lf * (dim + 1) + dim) * ne + e];
     std::string why;
+    if (c->nonaffine && !lone.empty())
+      return fail(c, RKDG_ERR_UNSUPPORTED, "hanging faces on non-parallelogram quadrilaterals");
     if (!rkdg::classify_nc_faces(geom, dim, nvpe, m->elem_coords, Jall, fmeas, ne, lone, slaves, why))
       return fail(c, RKDG_ERR_INVALID, why.c_str());
     const int nns = (int)slaves.size();
@@ -1107,6 +1182,16 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
   c->tab = T;
   // ---- upload ----
   const size_t nf = (size_t)nfpe * ne;
+  if (c->nonaffine) {
+    CUDA_TRY(c, dalloc(c->d_wmn64, h_wmn.size()));
+    CUDA_TRY(c, cudaMemcpy(c->d_wmn64, h_wmn.data(), h_wmn.size() * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<float> n32(h_ngeo.begin(), h_ngeo.end());
+    CUDA_TRY(c, dalloc(c->d_ngeo64, h_ngeo.size()));
+    CUDA_TRY(c, dalloc(c->d_ngeo32, n32.size()));
+    CUDA_TRY(c, cudaMemcpy(c->d_ngeo64, h_ngeo.data(), h_ngeo.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_ngeo32, n32.data(), n32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  c->tab.wmn_e = c->d_wmn64;
   CUDA_TRY(c, dalloc(c->d_tab, 1));
   CUDA_TRY(c, cudaMemcpy(c->d_tab, &c->tab, sizeof(RefTables), cudaMemcpyHostToDevice));
   CUDA_TRY(c, dalloc(c->d_fnbr, nf));
@@ -1167,6 +1252,9 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
       c->geom != RKDG_GEOM_TRIANGLE && !c->tab.lin_ok)
     return fail(c, RKDG_ERR_UNSUPPORTED,
                 "linearize needs order 1 (its rule of order p+1 has fewer points than nodes)");
+  if (c->nonaffine && c->ind == RKDG_IND_SHU && c->limiter_active())
+    return fail(c, RKDG_ERR_UNSUPPORTED,
+                "the Shu indicator maps between elements affinely: not on non-parallelogram quads");
   return ensure_scratch(c);
 }
 
@@ -1655,6 +1743,7 @@ int adjoint_ready(rkdg_ctx* c) {
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint kernels for this element type / order");
   if (c->nprob > 0) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for batched problems");
   if (c->nnc) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint on meshes with hanging faces");
+  if (c->nonaffine) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint on non-parallelogram quadrilaterals");
   if ((c->quirks & RKDG_LIMITER_LINEARIZE) && c->limiter_active() && c->lim == RKDG_LIM_MULTI &&
       c->geom != RKDG_GEOM_TRIANGLE)
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for the linearize limiter option");

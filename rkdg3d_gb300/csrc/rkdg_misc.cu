@@ -155,7 +155,9 @@ __global__ void k_totals(int nd, int neq, int ne, long long ndofs, const RefTabl
     double s = 0.0;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
       double v = 0.0;
-      for (int j = 0; j < nd; ++j) v += tab->wmean[j] * u[k * ndofs + (long long)e * nd + j];
+      for (int j = 0; j < nd; ++j)
+        v += (tab->wmn_e ? tab->wmn_e[(long long)e * nd + j] : tab->wmean[j]) *
+             u[k * ndofs + (long long)e * nd + j];
       s += wdet[e] * v;
     }
     red[threadIdx.x] = s;

@@ -260,6 +260,13 @@ void Basis::eval(const double* xi, double* phi, double* dphi) const {
 }
 
 // Element-reference coordinates of face parameter s on local face lf.
+void mean_rule(int geom, int p, std::vector<double>& x, std::vector<double>& w) {
+  const int orderW = geom == 2 ? 0 : (geom == 3 ? 1 : 2);
+  Pts r = elem_rule(geom, p + orderW);
+  x = r.x;
+  w = r.w;
+}
+
 void face_to_elem(int geom, int lf, const double* s, double* xi) {
   const int g = geom_slot(geom);
   const int dim = geom == 5 ? 3 : 2;

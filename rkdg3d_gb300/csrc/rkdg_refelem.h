@@ -29,6 +29,9 @@ struct FacePoint {
 };
 
 void face_to_elem(int geom, int lf, const double* s, double* xi);
+// The cell-mean rule (order p + OrderW, averager.cpp:104): reference points
+// x[n*dim] and weights w[n].
+void mean_rule(int geom, int p, std::vector<double>& x, std::vector<double>& w);
 bool build_ref_tables(int geom, int p, RefTables& T, std::vector<FacePoint>* fpts);
 
 }  // namespace rkdg

@@ -135,6 +135,32 @@ def hex_grid(nx: int, ny: int, nz: int, box=((0.0, 1.0), (0.0, 1.0), (0.0, 1.0))
     return m
 
 
+def perturb(mesh: Mesh, amount: float, seed: int = 0) -> Mesh:
+    """The mesh with every vertex that lies on no boundary face moved by
+    U(-amount, amount) per coordinate (the same move for every element
+    sharing the vertex): on a quad grid this gives general, non-parallelogram
+    quadrilaterals.  Periodic seams keep their coordinates."""
+    rng = np.random.default_rng(seed)
+    nv = int(mesh.elem_vertices.max()) + 1
+    shift = rng.uniform(-amount, amount, (nv, mesh.dim))
+    fixed = np.zeros(nv, bool)
+    fixed[mesh.bdr_vertices.ravel()] = True
+    # vertices whose elements disagree on their position lie on a periodic seam
+    first = {}
+    for e in range(mesh.num_elements):
+        for k, v in enumerate(mesh.elem_vertices[e]):
+            x = mesh.elem_coords[e, k]
+            if v in first and np.abs(first[v] - x).max() > 1e-12:
+                fixed[v] = True
+            first.setdefault(v, x)
+    shift[fixed] = 0.0
+    ec = mesh.elem_coords + shift[mesh.elem_vertices]
+    m = Mesh(mesh.dim, mesh.geom, mesh.elem_vertices.copy(), ec, mesh.bdr_vertices.copy(),
+             mesh.bdr_attr.copy())
+    m.validate()
+    return m
+
+
 def tri_grid(nx: int, ny: int, x0=0.0, x1=1.0, y0=0.0, y1=1.0, jitter=0.0, seed=0) -> Mesh:
     """Structured grid with every quad split along its (i,j)-(i+1,j+1) diagonal
     into two counter-clockwise triangles (elements 2q, 2q+1 for quad q =

@@ -549,3 +549,69 @@ def test_adapt_and_continue(cuda, prec):
         ctx.step(xd, 5e-4)
         x, _ = orc2.step(x, 5e-4)
     assert rel_l1(xd.cpu().numpy(), x) < tol
+
+
+# ---- non-parallelogram (bilinear) quadrilaterals --------------------------------
+
+def _bilinear_case(order, periodic, rs=RS_HLLC):
+    if periodic:
+        m = M.perturb(M.quad_grid(8, 8, periodic=(True, True)), 0.03, seed=4)
+        return cases.Case("bq", m, order, rs, 0)
+    m = M.perturb(M.quad_grid(8, 6, 0, 1, 0, 0.75), 0.02, seed=1)
+    return cases.Case("bq", m, order, rs, 0, bcs=[(a, BC_SLIP, None) for a in range(1, 5)])
+
+
+@pytest.mark.parametrize("order,periodic,prec", [(1, True, 0), (2, True, 0), (3, False, 0),
+                                                 (2, False, 1), (1, True, 1)])
+def test_rhs_bilinear_quads(cuda, order, periodic, prec):
+    """Non-parallelogram quadrilaterals (per-node adj(J) and det J in the
+    collocated volume term and lumped mass, per-element cell-mean weights):
+    right-hand side, face-only speed, cell means, totals and one step
+    against the oracle."""
+    case = _bilinear_case(order, periodic)
+    ctx, orc = pair(case)
+    if prec:
+        ctx.set_precision(1)
+    tol = RHS_TOL if prec == 0 else 1e-5
+    x = random_state(ctx.node_coords(), seed=19, amp=0.05, vel=0.1)
+    assert np.allclose(ctx.node_coords(), orc.node_coords(), rtol=0, atol=1e-14)
+    y_ref, m_ref = orc.rhs(x)
+    y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    m = ctx.rhs(dev(x), y)
+    assert rel_l1(y.cpu().numpy(), y_ref) < tol
+    assert abs(m - m_ref) <= (1e-13 if prec == 0 else 1e-6) * m_ref
+    assert abs(ctx.face_speed(dev(x)) - orc.face_speed(x)) <= (1e-13 if prec == 0 else 1e-6) * m_ref
+    md = torch.empty(ctx.neq * ctx.ne, dtype=torch.float64, device="cuda")
+    ctx.cell_means(dev(x), md)
+    assert np.allclose(md.cpu().numpy(), orc.means(x), rtol=1e-13, atol=1e-14)
+    assert np.allclose(ctx.totals(dev(x)), orc.totals(x), rtol=1e-13)
+    xs_ref, _ = orc.step(x, 1e-3)
+    xd = dev(x)
+    ctx.step(xd, 1e-3)
+    assert rel_l1(xd.cpu().numpy(), xs_ref) < tol
+
+
+@pytest.mark.parametrize("order,lim", [(1, LIM_MULTI), (2, LIM_FINDIFF)])
+def test_limiter_bilinear_quads(cuda, order, lim):
+    case = _bilinear_case(order, False)
+    case.limiter = (lim, IND_BJ, FUN_MICHALAK, 1, 0)
+    ctx, orc = pair(case)
+    x = random_state(ctx.node_coords(), seed=13, amp=0.1, vel=0.2)
+    xd = dev(x)
+    ctx.limit(xd)
+    assert rel_l1(xd.cpu().numpy(), orc.limit(x)) < 1e-12
+    xs_ref, _ = orc.step(x, 2e-4)
+    xd = dev(x)
+    ctx.step(xd, 2e-4)
+    assert rel_l1(xd.cpu().numpy(), xs_ref) < 1e-10
+
+
+def test_bilinear_quads_refusals(cuda):
+    """The Shu indicator and the adjoint assume affine elements."""
+    from rkdg3d_gb300.solver import RkdgError
+    ctx, _ = pair(_bilinear_case(1, True))
+    with pytest.raises(RkdgError):
+        ctx.set_limiter(LIM_FINDIFF, IND_SHU, FUN_MICHALAK, 1, 0)
+    x = dev(random_state(ctx.node_coords(), seed=2, amp=0.05, vel=0.1))
+    with pytest.raises(RkdgError):
+        ctx.rhs_vjp(x, torch.ones_like(x), torch.empty_like(x))

@@ -374,3 +374,23 @@ def test_nc_mesh_with_uncovered_face_is_rejected():
     holed = M.Mesh(3, M.GEOM_CUBE, m.elem_vertices[keep], m.elem_coords[keep], m.bdr_vertices, m.bdr_attr)
     with pytest.raises(Exception):
         Oracle(holed, 1)
+
+
+# ---- non-parallelogram (bilinear) quadrilaterals --------------------------------
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_bilinear_quads_free_stream_and_conservation(order):
+    """General quadrilaterals (interior vertices moved): a uniform flow stays
+    uniform on a periodic mesh (the collocated metric terms of a bilinear map
+    are exact), and the discrete totals are conserved."""
+    m = M.perturb(M.quad_grid(6, 6, periodic=(True, True)), 0.03, seed=2)
+    X = m.elem_coords
+    assert (np.abs(X[:, 0] + X[:, 2] - X[:, 1] - X[:, 3]).max(1) > 1e-6).sum() > 10
+    o = _oracle(cases.Case("q", m, order, RS_HLLC, 0))
+    Xn = o.node_coords()
+    one = np.ones(Xn.shape[1])
+    y, _ = o.rhs(cases.conservative([1.1 * one, 0.3 * one, -0.2 * one, one], 1.4, 0.0))
+    assert np.abs(y).max() < 1e-11
+    x = random_state(Xn, seed=6, amp=0.05, vel=0.1)
+    y, _ = o.rhs(x)
+    assert np.abs(o.totals(y)).max() < 1e-12 * np.abs(o.totals(x)).max()
