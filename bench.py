@@ -544,7 +544,8 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=64, help="elements per side")
+    ap.add_argument("--n", "--elements-per-side", dest="n", type=int, default=64,
+                    help="elements per side (the long form passes through torchrun)")
     ap.add_argument("--fp64-steps", type=int, default=500,
                     help="steps of the plain FP64 run (timed, and the accuracy reference)")
     ap.add_argument("--no-cpu", action="store_true")

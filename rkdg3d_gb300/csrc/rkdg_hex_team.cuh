@@ -169,27 +169,27 @@ __device__ __forceinline__ void team_interp(const R (&v)[(P + 1) * (P + 1)], con
         dst[(2 * pa + NQ1 * b) * ST] = s.x;
         dst[(2 * pa + 1 + NQ1 * b) * ST] = s.y;
       }
-    return;
+  } else {
+    R w[NQ1][N1];
+#pragma unroll
+    for (int a = 0; a < NQ1; ++a)
+#pragma unroll
+      for (int i1 = 0; i1 < N1; ++i1) {
+        R s = R(0);
+#pragma unroll
+        for (int i0 = 0; i0 < N1; ++i0) s += l1d[a * N1 + i0] * v[i0 * N1 + i1];
+        w[a][i1] = s;
+      }
+#pragma unroll
+    for (int b = 0; b < NQ1; ++b)
+#pragma unroll
+      for (int a = 0; a < NQ1; ++a) {
+        R s = R(0);
+#pragma unroll
+        for (int i1 = 0; i1 < N1; ++i1) s += l1d[b * N1 + i1] * w[a][i1];
+        dst[(a + NQ1 * b) * ST] = s;
+      }
   }
-  R w[NQ1][N1];
-#pragma unroll
-  for (int a = 0; a < NQ1; ++a)
-#pragma unroll
-    for (int i1 = 0; i1 < N1; ++i1) {
-      R s = R(0);
-#pragma unroll
-      for (int i0 = 0; i0 < N1; ++i0) s += l1d[a * N1 + i0] * v[i0 * N1 + i1];
-      w[a][i1] = s;
-    }
-#pragma unroll
-  for (int b = 0; b < NQ1; ++b)
-#pragma unroll
-    for (int a = 0; a < NQ1; ++a) {
-      R s = R(0);
-#pragma unroll
-      for (int i1 = 0; i1 < N1; ++i1) s += l1d[b * N1 + i1] * w[a][i1];
-      dst[(a + NQ1 * b) * ST] = s;
-    }
 }
 
 // Lift face values f[(a + NQ1*b) * ST] of face LF into the accumulators.
@@ -529,12 +529,11 @@ __device__ __forceinline__ void shared_rounds(const RhsParams& prm, const R* __r
                                               R gamma, R cov, R& lmax,
                                               R (&acc)[(P + 1) * (P + 1) * (P + 1)]) {
   using T = TeamSize<P>;
-  constexpr int N1 = T::N1, ND = T::ND, NQF = T::NQF, NEQ = T::NEQ, NF2 = T::NF2, TPW = T::TPW;
+  constexpr int N1 = T::N1, ND = T::ND, NQF = T::NQF, NEQ = T::NEQ, NF2 = T::NF2;
   constexpr int XG = T::XG;
   auto row = [&](int sl) { return sX + rowoff[sl]; };
   const int tid = threadIdx.x;
   const int jb = tid / NEQ, jk = tid - NEQ * jb;  // this thread's job: (listed slot, variable)
-  const int ne = prm.ne;
 #pragma unroll 1
   for (int r = 0; r < S.nr; ++r) {
     const int lf = act ? S.rlf[el][r] : 0xFF;
