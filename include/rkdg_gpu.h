@@ -116,7 +116,7 @@ int rkdg_set_physics(rkdg_ctx* ctx, int rsolver, int averaging, double gamma,
  * else RKDG_ERR_INVALID (a hole; also a hanging face across a periodic seam).
  * Elements: affine triangles, parallelograms and parallelepipeds, and
  * general (bilinear) quadrilaterals; non-affine hexahedra return
- * RKDG_ERR_UNSUPPORTED, as do the Shu indicator and the adjoint on
+ * RKDG_ERR_UNSUPPORTED, as do the Shu indicator and hanging faces on
  * non-parallelogram quadrilaterals.
  * Limiters see the elements across hanging faces as stencil cells and
  * evaluate indicator points on the element's own slave and master faces

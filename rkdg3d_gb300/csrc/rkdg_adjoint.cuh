@@ -37,6 +37,7 @@ __global__ void k_minv_apply(int ne, long long ndofs, const RefTables* tab, cons
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   const double idet = egeo[(long long)(DIM * DIM) * ne + e];
+  const double* ng = tab->ngeo_e;  // per-node geometry (bilinear quads): diagonal mass, per-node 1/det J
   for (int k = 0; k < NEQ; ++k) {
     double in[ND];
 #pragma unroll
@@ -46,7 +47,7 @@ __global__ void k_minv_apply(int ne, long long ndofs, const RefTables* tab, cons
       double v = 0.0;
 #pragma unroll
       for (int j = 0; j < ND; ++j) v += tab->Minv[j][i] * in[j];
-      r[k * ndofs + (long long)e * ND + i] = v * idet;
+      r[k * ndofs + (long long)e * ND + i] = v * (ng ? ng[((long long)(DIM * DIM) * ND + i) * ne + e] : idet);
     }
   }
 }
@@ -126,6 +127,9 @@ __global__ void __launch_bounds__(64)
   for (int rr = 0; rr < DIM; ++rr)
     for (int d = 0; d < DIM; ++d) adj[rr][d] = ((const double*)prm.egeo)[(long long)(rr * DIM + d) * ne + e];
   for (int m = 0; m < ND; ++m) {
+    if (T->ngeo_e)  // bilinear quads: adj(J) at the node
+      for (int rr = 0; rr < DIM; ++rr)
+        for (int d = 0; d < DIM; ++d) adj[rr][d] = T->ngeo_e[((long long)(rr * DIM + d) * ND + m) * ne + e];
     D st[NEQ];
     for (int k = 0; k < NEQ; ++k) st[k] = D::var(u[k * NDa + (long long)e * ND + m], k);
     D F[NEQ][DIM];
@@ -258,7 +262,7 @@ __global__ void __launch_bounds__(64)
       elind_last = yl;
     }
   }
-  const double* w = T->wmean;
+  const double* w = T->wmn_e ? T->wmn_e + (long long)e * ND : T->wmean;
   if (prm.limiter == 1) {
     const int reps = (prm.quirks & 1) ? 1 : ND;
     const double mv = m.v;
@@ -334,7 +338,9 @@ __global__ void k_limit_vjp_gather(const RhsParams prm, const double* __restrict
     s += cross[(long long)lfo * ne + e];
   }
   if (s != 0.0)
-    for (int j = 0; j < ND; ++j) zbar[(long long)c * ND + j] += prm.tab->wmean[j] * s;
+    for (int j = 0; j < ND; ++j)
+      zbar[(long long)c * ND + j] +=
+          (prm.tab->wmn_e ? prm.tab->wmn_e[(long long)c * ND + j] : prm.tab->wmean[j]) * s;
 }
 
 }  // namespace rkdg

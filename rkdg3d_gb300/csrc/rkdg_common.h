@@ -80,6 +80,8 @@ struct RefTables {
   // element [ne][nd] on the device (null when every element is affine and
   // wmean serves all)
   const double* wmn_e;
+  // and their FP64 adj(J), 1/det J at every node, [dim*dim + 1][nd][ne]
+  const double* ngeo_e;
   int nqs;
   double xs[RKDG_MAX_NQS][3];
   double ws[RKDG_MAX_NQS];

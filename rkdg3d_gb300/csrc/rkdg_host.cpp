@@ -1192,6 +1192,7 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     CUDA_TRY(c, cudaMemcpy(c->d_ngeo32, n32.data(), n32.size() * sizeof(float), cudaMemcpyHostToDevice));
   }
   c->tab.wmn_e = c->d_wmn64;
+  c->tab.ngeo_e = c->d_ngeo64;
   CUDA_TRY(c, dalloc(c->d_tab, 1));
   CUDA_TRY(c, cudaMemcpy(c->d_tab, &c->tab, sizeof(RefTables), cudaMemcpyHostToDevice));
   CUDA_TRY(c, dalloc(c->d_fnbr, nf));
@@ -1743,7 +1744,6 @@ int adjoint_ready(rkdg_ctx* c) {
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint kernels for this element type / order");
   if (c->nprob > 0) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for batched problems");
   if (c->nnc) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint on meshes with hanging faces");
-  if (c->nonaffine) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint on non-parallelogram quadrilaterals");
   if ((c->quirks & RKDG_LIMITER_LINEARIZE) && c->limiter_active() && c->lim == RKDG_LIM_MULTI &&
       c->geom != RKDG_GEOM_TRIANGLE)
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for the linearize limiter option");

@@ -227,3 +227,56 @@ def test_adjoint_gradient_full_size(cuda):
         worst = max(worst, abs(ad - fd[1]) / abs(fd[1]))
     assert judged >= ndir // 3, (judged, ndir)
     assert worst <= 1e-5, worst
+
+
+def _bilinear(order, limiter=None):
+    case = cases.Case("bq", M.perturb(M.quad_grid(5, 5, periodic=(True, True)), 0.03, seed=4),
+                      order, RS_HLLC, AVG_TRRS)
+    if limiter:
+        case.limiter = limiter
+    return case
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_vjp_bilinear_quads_fd(cuda, order):
+    """Non-parallelogram quadrilaterals: the right-hand side, limiter and
+    step VJPs use adj(J) and det J per node and per-element mean weights."""
+    ctx = ctx_for(_bilinear(order, (LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN, 1, 0)))
+    x = random_state(ctx.node_coords(), seed=6, amp=0.1, vel=0.2)
+
+    def rhs(xx):
+        y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.rhs(dev(xx), y)
+        return y.cpu().numpy()
+
+    def rhs_vjp(w):
+        out = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.rhs_vjp(dev(x), dev(w), out)
+        return out.cpu().numpy()
+
+    fd_check(rhs, rhs_vjp, x, seed=1)
+
+    def lim(xx):
+        y = dev(xx)
+        ctx.limit(y)
+        return y.cpu().numpy()
+
+    def lim_vjp(w):
+        out = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.limit_vjp(dev(x), dev(w), out)
+        return out.cpu().numpy()
+
+    fd_check(lim, lim_vjp, x, seed=2, eps=1e-7)
+    xs = smooth_state(ctx.node_coords(), 2)
+
+    def step(xx):
+        y = dev(xx)
+        ctx.step(y, 1e-3)
+        return y.cpu().numpy()
+
+    def step_vjp(w):
+        xb = dev(w)
+        ctx.step_vjp(dev(xs), 1e-3, xb)
+        return xb.cpu().numpy()
+
+    fd_check(step, step_vjp, xs, seed=4, eps=1e-7)
