@@ -44,6 +44,23 @@ cudaError_t launch_rhs_vjp(int geom, int p, const RhsParams& prm, const double* 
 }
 
 template <int G, int P>
+static cudaError_t nc_vjp_t(const RhsParams& prm, const NcParams& nc, const double* u,
+                            const double* r, double* ub, cudaStream_t st) {
+  using E = El<G, P>;
+  k_nc_vjp_point<G, P><<<(nc.nnc * E::NQF + 63) / 64, 64, 0, st>>>(prm, nc, u, r);
+  if (nc.nel > 0)
+    k_nc_vjp_gather<G, P><<<(nc.nel * E::ND + 127) / 128, 128, 0, st>>>(nc, prm.tab, prm.ndofs, ub);
+  return cudaGetLastError();
+}
+cudaError_t launch_nc_vjp(int geom, int p, const RhsParams& prm, const NcParams& nc, const double* u,
+                          const double* r, double* ub, cudaStream_t st) {
+  if (nc.nnc <= 0) return cudaSuccess;
+#define CALL_NV(G, P) nc_vjp_t<G, P>(prm, nc, u, r, ub, st)
+  RKDG_ADJ_DISPATCH(CALL_NV)
+#undef CALL_NV
+}
+
+template <int G, int P>
 static cudaError_t lim_vjp_t(const LimParams& prm, const double* z, const double* yb, double* zb,
                              double* cross, cudaStream_t st) {
   k_limit_vjp<G, P><<<(prm.ne + 63) / 64, 64, 0, st>>>(prm, z, yb, zb, cross);

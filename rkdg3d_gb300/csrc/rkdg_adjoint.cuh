@@ -152,6 +152,88 @@ __global__ void __launch_bounds__(64)
     for (int s = 0; s < ND; ++s) ubar[k * NDa + (long long)e * ND + s] = acc[k][s];
 }
 
+// Hanging faces of a nonconforming mesh (see rkdg_nc.cu).  The element VJP
+// above skips them (they carry no integrator of their own); here, per slave
+// point q, Fhat_bar = w_q |J_f| (-B1 r_fine + Bc r_coarse) and, with the
+// flux differentiated once per side, g_side = (dFhat/du_side)^T Fhat_bar
+// (k_nc_vjp_point, stored [face][q][side][k]); k_nc_vjp_gather then adds
+// phi_j(q) g_side over each touched element's slave faces to u_bar.
+template <int G, int P>
+__global__ void __launch_bounds__(64)
+    k_nc_vjp_point(const RhsParams prm, const NcParams nc, const double* __restrict__ u,
+                   const double* __restrict__ r) {
+  using E = El<G, P>;
+  constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NQF = E::NQF;
+  using D = Dual<NEQ>;
+  const RefTables* T = prm.tab;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nc.nnc * NQF) return;
+  const int f = t / NQF, q = t - f * NQF;
+  const int e1 = nc.face[f * 4], lf1 = nc.face[f * 4 + 1], e2 = nc.face[f * 4 + 2];
+  const int ne = prm.ne;
+  const long long NDa = prm.ndofs;
+  const double* fg = (const double*)prm.fgeo;
+  D n[DIM];
+  for (int c = 0; c < DIM; ++c) n[c] = D(fg[(long long)(lf1 * (DIM + 1) + c) * ne + e1]);
+  const double jac = fg[(long long)(lf1 * (DIM + 1) + DIM) * ne + e1];
+  const double* B1 = T->B[lf1][q];
+  const double* B2 = nc.bnc + ((long long)f * NQF + q) * ND;
+  double v1[NEQ], v2[NEQ], fbar[NEQ];
+  for (int k = 0; k < NEQ; ++k) {
+    double a = 0.0, b = 0.0, ra = 0.0, rb = 0.0;
+    for (int s = 0; s < ND; ++s) {
+      a += u[k * NDa + (long long)e1 * ND + s] * B1[s];
+      ra += r[k * NDa + (long long)e1 * ND + s] * B1[s];
+      b += u[k * NDa + (long long)e2 * ND + s] * B2[s];
+      rb += r[k * NDa + (long long)e2 * ND + s] * B2[s];
+    }
+    v1[k] = a;
+    v2[k] = b;
+    fbar[k] = T->wf[q] * jac * (-ra + rb);
+  }
+  const D gamma = D(prm.gamma), cov = D(prm.covolume);
+  double* g = (double*)nc.flux + ((long long)f * NQF + q) * 2 * NEQ;
+  for (int side = 0; side < 2; ++side) {
+    D s1[NEQ], s2[NEQ];
+    for (int k = 0; k < NEQ; ++k) {
+      s1[k] = side == 0 ? D::var(v1[k], k) : D(v1[k]);
+      s2[k] = side == 1 ? D::var(v2[k], k) : D(v2[k]);
+    }
+    D F[NEQ];
+    riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg);
+    for (int kk = 0; kk < NEQ; ++kk) {
+      double s = 0.0;
+      for (int k = 0; k < NEQ; ++k) s += fbar[k] * F[k].d[kk];
+      g[side * NEQ + kk] = s;
+    }
+  }
+}
+
+template <int G, int P>
+__global__ void __launch_bounds__(128)
+    k_nc_vjp_gather(const NcParams nc, const RefTables* __restrict__ T, long long NDa,
+                    double* __restrict__ ubar) {
+  using E = El<G, P>;
+  constexpr int ND = E::ND, NEQ = E::NEQ, NQF = E::NQF;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nc.nel * ND) return;
+  const int i = t / ND, j = t - i * ND;
+  double s[NEQ];
+  for (int k = 0; k < NEQ; ++k) s[k] = 0.0;
+  const double* gb = (const double*)nc.flux;
+  for (int c = nc.ptr[i]; c < nc.ptr[i + 1]; ++c) {
+    const int f = nc.ent[c] >> 1, side = nc.ent[c] & 1;
+    const int lf1 = nc.face[f * 4 + 1];
+    for (int q = 0; q < NQF; ++q) {
+      const double phi = side ? nc.bnc[((long long)f * NQF + q) * ND + j] : T->B[lf1][q][j];
+      const double* g = gb + (((long long)f * NQF + q) * 2 + side) * NEQ;
+      for (int k = 0; k < NEQ; ++k) s[k] += phi * g[k];
+    }
+  }
+  const int e = nc.elem[i];
+  for (int k = 0; k < NEQ; ++k) ubar[k * NDa + (long long)e * ND + j] += s[k];
+}
+
 // Limiter VJP, own part; cross[lf][e] receives the derivative with respect to
 // the density mean of the neighbour through face lf.
 template <int G, int P>

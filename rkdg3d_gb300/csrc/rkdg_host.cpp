@@ -1221,7 +1221,9 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
     c->nc_nel = (int)nc_elem.size();
     CUDA_TRY(c, dalloc(c->d_nc_face, nc_face.size()));
     CUDA_TRY(c, dalloc(c->d_nc_bnc, nc_bnc.size()));
-    CUDA_TRY(c, dalloc(c->d_nc_flux, (size_t)nns * 2 * neq * nd));  // per face: both elements' terms
+    // per face: both elements' terms (forward), or per point both sides'
+    // flux derivatives (adjoint)
+    CUDA_TRY(c, dalloc(c->d_nc_flux, (size_t)nns * 2 * neq * std::max(nd, T.nqf)));
     CUDA_TRY(c, dalloc(c->d_nc_elem, nc_elem.size()));
     CUDA_TRY(c, dalloc(c->d_nc_ptr, nc_ptr.size()));
     CUDA_TRY(c, dalloc(c->d_nc_ent, nc_ent.size()));
@@ -1682,6 +1684,10 @@ int rhs_t(rkdg_ctx* c, Adj& A, const double* y, const double* kbar, double* out)
   CUDA_TRY(c, rkdg::launch_minv_apply(c->geom, c->p, c->ne, c->ndofs, c->d_tab, c->d_egeo64, kbar, A.r, c->stream));
   RhsParams P = rhs_params(c, 0, 0, 7);
   CUDA_TRY(c, rkdg::launch_rhs_vjp(c->geom, c->p, P, y, A.r, out, c->stream));
+  if (c->nnc) {  // the hanging faces' share, added to u_bar
+    CUDA_TRY(c, rkdg::launch_nc_vjp(c->geom, c->p, P, nc_params(c), y, A.r, out, c->stream));
+    c->launches += 2;
+  }
   c->launches += 2;
   return RKDG_OK;
 }
@@ -1743,7 +1749,8 @@ int adjoint_ready(rkdg_ctx* c) {
   if (!rkdg::adjoint_supported(c->geom, c->p))
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint kernels for this element type / order");
   if (c->nprob > 0) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for batched problems");
-  if (c->nnc) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint on meshes with hanging faces");
+  if (c->nnc && c->limiter_active())
+    return fail(c, RKDG_ERR_UNSUPPORTED, "no limiter adjoint on meshes with hanging faces");
   if ((c->quirks & RKDG_LIMITER_LINEARIZE) && c->limiter_active() && c->lim == RKDG_LIM_MULTI &&
       c->geom != RKDG_GEOM_TRIANGLE)
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for the linearize limiter option");

@@ -53,6 +53,9 @@ cudaError_t launch_minv_apply(int geom, int p, int ne, long long ndofs, const Re
                               const double* egeo, const double* kb, double* r, cudaStream_t st);
 cudaError_t launch_rhs_vjp(int geom, int p, const RhsParams& prm, const double* u, const double* r,
                            double* ub, cudaStream_t st);
+// u_bar += the hanging faces' part of (dz/du)^T r (nonconforming meshes).
+cudaError_t launch_nc_vjp(int geom, int p, const RhsParams& prm, const NcParams& nc, const double* u,
+                          const double* r, double* ub, cudaStream_t st);
 cudaError_t launch_limit_vjp(int geom, int p, const LimParams& prm, const double* z,
                              const double* yb, double* zb, double* cross, cudaStream_t st);
 cudaError_t launch_limit_vjp_gather(int geom, int p, const RhsParams& prm, const double* cross,

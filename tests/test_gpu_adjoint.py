@@ -280,3 +280,62 @@ def test_vjp_bilinear_quads_fd(cuda, order):
         return xb.cpu().numpy()
 
     fd_check(step, step_vjp, xs, seed=4, eps=1e-7)
+
+
+def _nc(kind, order):
+    if kind == "hex":
+        m = M.refine_nc(M.hex_grid(4, 4, 4), [21, 22, 42])
+        return cases.Case("nc", m, order, RS_HLLC, 0)
+    if kind == "tri":
+        m = M.refine_nc(M.tri_grid(6, 6, 0, 1, 0, 1, jitter=0.2, seed=3), [14, 15, 30])
+        return cases.Case("nc", m, order, RS_HLL, 0, bcs=[(a, BC_SLIP, None) for a in range(1, 5)])
+    m = M.refine_nc(M.quad_grid(8, 8, periodic=(True, True)), [9, 10, 18, 45])
+    return cases.Case("nc", m, order, RS_RUSANOV, AVG_TRRS)
+
+
+@pytest.mark.parametrize("kind,order", [("quad", 2), ("quad", 1), ("hex", 1), ("tri", 1)])
+def test_rhs_vjp_nonconforming_fd(cuda, kind, order):
+    """Hanging faces: the slave-face terms (fine element at its own points,
+    coarse element at the mapped points) enter u_bar through both sides'
+    flux derivatives."""
+    ctx = ctx_for(_nc(kind, order))
+    x = random_state(ctx.node_coords(), seed=5, amp=0.1, vel=0.2)
+
+    def apply(xx):
+        y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.rhs(dev(xx), y)
+        return y.cpu().numpy()
+
+    def vjp(w):
+        out = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.rhs_vjp(dev(x), dev(w), out)
+        return out.cpu().numpy()
+
+    fd_check(apply, vjp, x, seed=1)
+
+
+def test_step_vjp_nonconforming_fd(cuda):
+    """An unlimited SSP-RK3 step on a mesh with hanging faces; with a limiter
+    the adjoint on such a mesh is refused."""
+    from rkdg3d_gb300.solver import RkdgError
+    case = _nc("hex", 1)
+    case.tableau = TABLEAU_SSPRK3
+    ctx = ctx_for(case)
+    x = smooth_state(ctx.node_coords(), 3)
+    dt = 2e-3
+
+    def apply(xx):
+        y = dev(xx)
+        ctx.step(y, dt)
+        return y.cpu().numpy()
+
+    def vjp(w):
+        xb = dev(w)
+        ctx.step_vjp(dev(x), dt, xb)
+        return xb.cpu().numpy()
+
+    fd_check(apply, vjp, x, seed=4, eps=1e-7)
+    case.limiter = (LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN, 1, 0)
+    ctx = ctx_for(case)
+    with pytest.raises(RkdgError, match="hanging"):
+        ctx.step_vjp(dev(x), dt, dev(x))
