@@ -120,8 +120,8 @@ int rkdg_set_physics(rkdg_ctx* ctx, int rsolver, int averaging, double gamma,
  * non-parallelogram quadrilaterals.
  * Limiters see the elements across hanging faces as stencil cells and
  * evaluate indicator points on the element's own slave and master faces
- * (limiter.cpp:95-245).  Batched problems on such meshes, and the adjoint
- * there while a limiter is active, return RKDG_ERR_UNSUPPORTED. */
+ * (limiter.cpp:95-245); the adjoint covers them too.  Batched problems on
+ * such meshes return RKDG_ERR_UNSUPPORTED. */
 int rkdg_upload_mesh(rkdg_ctx* ctx, const rkdg_mesh_desc* mesh);
 /* Deviations from the shipped reference, off by default.
  * RKDG_QUIRK_HLLC_NEGATIVE_SPEED_OK: the reference treats any negative face

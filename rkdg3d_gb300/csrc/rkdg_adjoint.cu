@@ -74,11 +74,11 @@ cudaError_t launch_limit_vjp(int geom, int p, const LimParams& prm, const double
 }
 
 template <int G, int P>
-static cudaError_t gather_t(const RhsParams& prm, const double* cross, double* zb, cudaStream_t st) {
+static cudaError_t gather_t(const LimParams& prm, const double* cross, double* zb, cudaStream_t st) {
   k_limit_vjp_gather<G, P><<<(prm.ne + 127) / 128, 128, 0, st>>>(prm, cross, zb);
   return cudaGetLastError();
 }
-cudaError_t launch_limit_vjp_gather(int geom, int p, const RhsParams& prm, const double* cross,
+cudaError_t launch_limit_vjp_gather(int geom, int p, const LimParams& prm, const double* cross,
                                     double* zb, cudaStream_t st) {
 #define CALL_G(G, P) gather_t<G, P>(prm, cross, zb, st)
   RKDG_ADJ_DISPATCH(CALL_G)

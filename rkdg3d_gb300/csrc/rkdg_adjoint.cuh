@@ -234,15 +234,45 @@ __global__ void __launch_bounds__(128)
   for (int k = 0; k < NEQ; ++k) ubar[k * NDa + (long long)e * ND + j] += s[k];
 }
 
-// Limiter VJP, own part; cross[lf][e] receives the derivative with respect to
-// the density mean of the neighbour through face lf.
+// The limiter's stencil of element e (limiter.cpp:95-123): its face
+// neighbours, then the elements across its hanging faces (nonconforming
+// meshes).  stencil_size / stencil_at enumerate it; an entry is -1 where a
+// face has no neighbour.
+__device__ __forceinline__ int lim_ncrow(const LimParams& prm, int e) {
+  return prm.ncidx ? prm.ncidx[e] : -1;
+}
+__device__ __forceinline__ int stencil_size(const LimParams& prm, int row, int nfpe) {
+  return nfpe + (row >= 0 ? prm.nc_ptr[row + 1] - prm.nc_ptr[row] : 0);
+}
+__device__ __forceinline__ int stencil_at(const LimParams& prm, int e, int row, int nfpe, int i) {
+  if (i < nfpe) return prm.fnbr[i * prm.ne + e];
+  const int ent = prm.nc_ent[prm.nc_ptr[row] + i - nfpe];
+  return prm.nc_face[(ent >> 1) * 4 + ((ent & 1) ? 0 : 2)];
+}
+// Local faces of e that are slave or master faces: they carry indicator
+// points although no conforming neighbour lies across them.
+__device__ __forceinline__ unsigned hanging_faces(const LimParams& prm, int row) {
+  unsigned m = 0;
+  if (row >= 0)
+    for (int c = prm.nc_ptr[row]; c < prm.nc_ptr[row + 1]; ++c) {
+      const int f = prm.nc_ent[c] >> 1, side = prm.nc_ent[c] & 1;
+      m |= 1u << prm.nc_face[f * 4 + (side ? 3 : 1)];
+    }
+  return m;
+}
+
+// Limiter VJP, own part.  The stencil's density minimum and maximum are
+// each one element's mean (the first one in stencil order on ties, as the
+// forward min/max keeps it); the derivative with respect to them goes to
+// cross[0..3][e] = (argmin element or -1 for e itself, d/dmin, argmax
+// element or -1, d/dmax), which k_limit_vjp_gather hands to those elements.
 template <int G, int P>
 __global__ void __launch_bounds__(64)
     k_limit_vjp(const LimParams prm, const double* __restrict__ z, const double* __restrict__ ybar,
                 double* __restrict__ zbar, double* __restrict__ cross) {
   using E = El<G, P>;
   constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NFPE = E::NFPE, NQL = E::NQL, NV = E::NV;
-  constexpr int NVAR = ND + 1 + NFPE;
+  constexpr int NVAR = ND + 3;  // nodal densities, own mean, stencil min, stencil max
   using D = Dual<NVAR>;
   const RefTables* T = prm.tab;
   const int ne = prm.ne;
@@ -257,12 +287,16 @@ __global__ void __launch_bounds__(64)
       yb[k][j] = ybar[k * NDa + (long long)e * ND + j];
     }
   }
-  for (int lf = 0; lf < NFPE; ++lf) cross[(long long)lf * ne + e] = 0.0;
+  for (int i = 0; i < 4; ++i) cross[(long long)i * ne + e] = i == 0 || i == 2 ? -1.0 : 0.0;
+  const int row = lim_ncrow(prm, e);
+  const int nst = stencil_size(prm, row, NFPE);
+  const unsigned ncfaces = hanging_faces(prm, row);
   double zb[NEQ][ND];
   for (int k = 0; k < NEQ; ++k)
     for (int j = 0; j < ND; ++j) zb[k][j] = 0.0;
   // density indicator with derivatives
   D m;
+  int amin = -1, amax = -1;
   double elind_last = 1.0;
   if (prm.indicator == 0) {
     m = D(1.0);
@@ -273,18 +307,25 @@ __global__ void __launch_bounds__(64)
     D rho[ND];
     for (int j = 0; j < ND; ++j) rho[j] = D::var(el[0][j], j);
     const D mself = D::var(um[0], ND);
-    D mI = mself < D(1e9) ? mself : D(1e9);
-    D MI = mself > D(-1e9) ? mself : D(-1e9);
-    for (int lf = 0; lf < NFPE; ++lf) {
-      const int nb = prm.fnbr[lf * ne + e];
+    double mIv = um[0] < 1e9 ? um[0] : 1e9, MIv = um[0] > -1e9 ? um[0] : -1e9;
+    for (int i = 0; i < nst; ++i) {
+      const int nb = stencil_at(prm, e, row, NFPE, i);
       if (nb < 0) continue;
-      const D v = D::var(prm.means[nb], ND + 1 + lf);
-      mI = v < mI ? v : mI;
-      MI = v > MI ? v : MI;
+      const double v = prm.means[nb];
+      if (v < mIv) {
+        mIv = v;
+        amin = nb;
+      }
+      if (v > MIv) {
+        MIv = v;
+        amax = nb;
+      }
     }
+    const D mI = amin >= 0 ? D::var(mIv, ND + 1) : (mself < D(1e9) ? mself : D(1e9));
+    const D MI = amax >= 0 ? D::var(MIv, ND + 2) : (mself > D(-1e9) ? mself : D(-1e9));
     D yMin = D(1e9);
     for (int lf = 0; lf < NFPE; ++lf) {
-      if (prm.fnbr[lf * ne + e] < 0) continue;
+      if (prm.fnbr[lf * ne + e] < 0 && !((ncfaces >> lf) & 1u)) continue;
       for (int q = 0; q < NQL; ++q) {
         D v = D(0.0);
         for (int j = 0; j < ND; ++j) v += rho[j] * T->Bl[lf][q][j];
@@ -315,15 +356,15 @@ __global__ void __launch_bounds__(64)
     if (prm.limiter == 0) {
       const int kl = NEQ - 1;
       double mIl = um[kl], MIl = um[kl], yl = 1e9;
-      for (int lf = 0; lf < NFPE; ++lf) {
-        const int nb = prm.fnbr[lf * ne + e];
+      for (int i = 0; i < nst; ++i) {
+        const int nb = stencil_at(prm, e, row, NFPE, i);
         if (nb < 0) continue;
         const double v = prm.means[(long long)kl * ne + nb];
         mIl = v < mIl ? v : mIl;
         MIl = v > MIl ? v : MIl;
       }
       for (int lf = 0; lf < NFPE; ++lf) {
-        if (prm.fnbr[lf * ne + e] < 0) continue;
+        if (prm.fnbr[lf * ne + e] < 0 && !((ncfaces >> lf) & 1u)) continue;
         for (int q = 0; q < NQL; ++q) {
           double v = 0.0;
           for (int j = 0; j < ND; ++j) v += el[kl][j] * T->Bl[lf][q][j];
@@ -383,7 +424,10 @@ __global__ void __launch_bounds__(64)
       }
       if (prm.indicator == 2) {
         for (int j = 0; j < ND; ++j) zb[0][j] += mbar * (m.d[j] + m.d[ND] * w[j]);
-        for (int lf = 0; lf < NFPE; ++lf) cross[(long long)lf * ne + e] = mbar * m.d[ND + 1 + lf];
+        cross[(long long)0 * ne + e] = amin;
+        cross[(long long)1 * ne + e] = mbar * m.d[ND + 1];
+        cross[(long long)2 * ne + e] = amax;
+        cross[(long long)3 * ne + e] = mbar * m.d[ND + 2];
       }
     }
   } else {
@@ -402,22 +446,28 @@ __global__ void __launch_bounds__(64)
     for (int j = 0; j < ND; ++j) zbar[k * NDa + (long long)e * ND + j] = zb[k][j];
 }
 
-// Gather the neighbours' derivatives with respect to this element's density
-// mean (mean = sum_j wmean_j rho_j).
+// Gather, for element c, the derivatives that the elements of its stencil
+// (which hold c in theirs) took with respect to c's density mean (mean =
+// sum_j w_j rho_j), each stencil element once.
 template <int G, int P>
-__global__ void k_limit_vjp_gather(const RhsParams prm, const double* __restrict__ cross,
+__global__ void k_limit_vjp_gather(const LimParams prm, const double* __restrict__ cross,
                                    double* __restrict__ zbar) {
   using E = El<G, P>;
   constexpr int ND = E::ND, NFPE = E::NFPE;
   const int ne = prm.ne;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ne) return;
+  const int row = lim_ncrow(prm, c);
+  const int nst = stencil_size(prm, row, NFPE);
   double s = 0.0;
-  for (int lf = 0; lf < NFPE; ++lf) {
-    const int e = prm.fnbr[lf * ne + c];
-    if (e < 0) continue;
-    const int lfo = prm.fcode[lf * ne + c] & 7;
-    s += cross[(long long)lfo * ne + e];
+  for (int i = 0; i < nst; ++i) {
+    const int e = stencil_at(prm, c, row, NFPE, i);
+    if (e < 0 || e == c) continue;
+    bool seen = false;
+    for (int i2 = 0; i2 < i && !seen; ++i2) seen = stencil_at(prm, c, row, NFPE, i2) == e;
+    if (seen) continue;
+    if (cross[e] == (double)c) s += cross[(long long)ne + e];
+    if (cross[(long long)2 * ne + e] == (double)c) s += cross[(long long)3 * ne + e];
   }
   if (s != 0.0)
     for (int j = 0; j < ND; ++j)

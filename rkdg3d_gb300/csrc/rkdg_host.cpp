@@ -1640,7 +1640,7 @@ struct Adj {
 int adj_bufs(rkdg_ctx* c, Adj& A) {
   const size_t n = (size_t)c->ndofs * c->neq;
   const size_t nvec = 5 + 16;
-  const size_t need = nvec * n + (size_t)c->nfpe * c->ne;
+  const size_t need = nvec * n + (size_t)4 * c->ne;  // + the limiter's min/max derivatives
   if (c->adj_n < need) {
     CUDA_TRY(c, dalloc(c->d_adj, need));
     c->adj_n = need;
@@ -1702,8 +1702,7 @@ int lim_t(rkdg_ctx* c, Adj& A, const double* z, const double* ybar, double* out)
   CUDA_TRY(c, rkdg::launch_means(c->geom, c->p, 0, c->ne, c->ndofs, c->d_tab, z, nullptr, c->d_means, c->stream));
   LimParams L = lim_params(c);
   CUDA_TRY(c, rkdg::launch_limit_vjp(c->geom, c->p, L, z, ybar, out, A.cross, c->stream));
-  RhsParams P = rhs_params(c, 0, 0, 7);
-  CUDA_TRY(c, rkdg::launch_limit_vjp_gather(c->geom, c->p, P, A.cross, out, c->stream));
+  CUDA_TRY(c, rkdg::launch_limit_vjp_gather(c->geom, c->p, L, A.cross, out, c->stream));
   c->launches += 3;
   return RKDG_OK;
 }
@@ -1749,8 +1748,6 @@ int adjoint_ready(rkdg_ctx* c) {
   if (!rkdg::adjoint_supported(c->geom, c->p))
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint kernels for this element type / order");
   if (c->nprob > 0) return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for batched problems");
-  if (c->nnc && c->limiter_active())
-    return fail(c, RKDG_ERR_UNSUPPORTED, "no limiter adjoint on meshes with hanging faces");
   if ((c->quirks & RKDG_LIMITER_LINEARIZE) && c->limiter_active() && c->lim == RKDG_LIM_MULTI &&
       c->geom != RKDG_GEOM_TRIANGLE)
     return fail(c, RKDG_ERR_UNSUPPORTED, "no adjoint for the linearize limiter option");

@@ -58,7 +58,7 @@ cudaError_t launch_nc_vjp(int geom, int p, const RhsParams& prm, const NcParams&
                           const double* r, double* ub, cudaStream_t st);
 cudaError_t launch_limit_vjp(int geom, int p, const LimParams& prm, const double* z,
                              const double* yb, double* zb, double* cross, cudaStream_t st);
-cudaError_t launch_limit_vjp_gather(int geom, int p, const RhsParams& prm, const double* cross,
+cudaError_t launch_limit_vjp_gather(int geom, int p, const LimParams& prm, const double* cross,
                                     double* zb, cudaStream_t st);
 cudaError_t launch_axpy(long long n, double a, const double* x, double* y, cudaStream_t st);
 cudaError_t launch_scale_copy(long long n, double a, const double* x, double* y, cudaStream_t st);

@@ -315,27 +315,49 @@ def test_rhs_vjp_nonconforming_fd(cuda, kind, order):
 
 
 def test_step_vjp_nonconforming_fd(cuda):
-    """An unlimited SSP-RK3 step on a mesh with hanging faces; with a limiter
-    the adjoint on such a mesh is refused."""
-    from rkdg3d_gb300.solver import RkdgError
+    """An SSP-RK3 step on a mesh with hanging faces, unlimited and limited."""
     case = _nc("hex", 1)
     case.tableau = TABLEAU_SSPRK3
+    x = None
+    for limiter in (case.limiter, (LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN, 1, 0)):
+        case.limiter = limiter
+        ctx = ctx_for(case)
+        if x is None:
+            x = smooth_state(ctx.node_coords(), 3)
+        dt = 2e-3
+
+        def apply(xx):
+            y = dev(xx)
+            ctx.step(y, dt)
+            return y.cpu().numpy()
+
+        def vjp(w):
+            xb = dev(w)
+            ctx.step_vjp(dev(x), dt, xb)
+            return xb.cpu().numpy()
+
+        fd_check(apply, vjp, x, seed=4, eps=1e-7)
+
+
+@pytest.mark.parametrize("kind,order,fun", [("quad", 1, FUN_VENKATAKRISHNAN), ("quad", 2, FUN_MICHALAK),
+                                            ("hex", 1, FUN_VENKATAKRISHNAN), ("tri", 1, FUN_MICHALAK)])
+def test_limit_vjp_nonconforming_fd(cuda, kind, order, fun):
+    """The limiter across hanging faces: the elements across them are stencil
+    cells (a coarse element sees each fine neighbour) and the element's slave
+    and master faces carry indicator points."""
+    case = _nc(kind, order)
+    case.limiter = (LIM_MULTI, IND_BJ, fun, 1, 0)
     ctx = ctx_for(case)
-    x = smooth_state(ctx.node_coords(), 3)
-    dt = 2e-3
+    x = random_state(ctx.node_coords(), seed=5, amp=0.1, vel=0.2)
 
     def apply(xx):
         y = dev(xx)
-        ctx.step(y, dt)
+        ctx.limit(y)
         return y.cpu().numpy()
 
     def vjp(w):
-        xb = dev(w)
-        ctx.step_vjp(dev(x), dt, xb)
-        return xb.cpu().numpy()
+        out = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+        ctx.limit_vjp(dev(x), dev(w), out)
+        return out.cpu().numpy()
 
-    fd_check(apply, vjp, x, seed=4, eps=1e-7)
-    case.limiter = (LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN, 1, 0)
-    ctx = ctx_for(case)
-    with pytest.raises(RkdgError, match="hanging"):
-        ctx.step_vjp(dev(x), dt, dev(x))
+    fd_check(apply, vjp, x, seed=2, eps=1e-7)

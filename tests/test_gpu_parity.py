@@ -500,8 +500,8 @@ def test_limiter_nonconforming(cuda, kind, order, lim, ind, fun):
 
 def test_nonconforming_mesh_errors(cuda):
     """A hole (faces with neither a neighbour, a boundary element nor hanging
-    faces covering them) is an invalid mesh; the limiter adjoint across
-    hanging faces is not supported and says so."""
+    faces covering them) is an invalid mesh; batched problems on meshes with
+    hanging faces are not supported and say so."""
     from rkdg3d_gb300.solver import RkdgError
     m = M.hex_grid(3, 3, 3, periodic=(False,) * 3)
     keep = [e for e in range(m.num_elements) if e != 13]
@@ -509,11 +509,9 @@ def test_nonconforming_mesh_errors(cuda):
     with pytest.raises(RkdgError):
         Context(holed, 1, device=0)
     case = _nc_case("quad", 1)
-    case.limiter = (LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 0)
     ctx, _ = pair(case)
-    x = dev(random_state(ctx.node_coords(), seed=2, amp=0.05, vel=0.1))
     with pytest.raises(RkdgError, match="hanging"):
-        ctx.limit_vjp(x, torch.ones_like(x), torch.empty_like(x))
+        ctx.batch_setup([0, ctx.ne], [1.4], [0.0])
 
 
 @pytest.mark.parametrize("prec", [0, 1])
