@@ -5,7 +5,7 @@
 namespace rkdg {
 
 bool adjoint_supported(int geom, int p) {
-  return (geom == 2 && p == 1) || (geom == 3 && (p == 1 || p == 2)) || (geom == 5 && p == 1);
+  return (geom == 2 && p == 1) || (geom == 3 && (p == 1 || p == 2)) || (geom == 5 && (p == 1 || p == 2));
 }
 
 #define RKDG_ADJ_DISPATCH(CALL)       \
@@ -14,6 +14,7 @@ bool adjoint_supported(int geom, int p) {
     case 31: return CALL(3, 1);       \
     case 32: return CALL(3, 2);       \
     case 51: return CALL(5, 1);       \
+    case 52: return CALL(5, 2);       \
     default: return cudaErrorInvalidValue; \
   }
 

@@ -47,6 +47,7 @@ def fd_check(apply, vjp, x, seed, eps=1e-6, tol=1e-5):
 
 
 @pytest.mark.parametrize("geom,order,rs,walled", [(M.GEOM_CUBE, 1, RS_HLLC, False),
+                                                  (M.GEOM_CUBE, 2, RS_HLLC, True),
                                                   (M.GEOM_SQUARE, 1, RS_HLL, True),
                                                   (M.GEOM_SQUARE, 2, RS_RUSANOV, False),
                                                   (M.GEOM_TRIANGLE, 1, RS_HLLC, True)])
@@ -93,9 +94,9 @@ def test_rhs_vjp_pressure_bcs_fd(cuda, bc, params, geom):
 
 
 @pytest.mark.parametrize("fun", [FUN_VENKATAKRISHNAN, FUN_MICHALAK])
-@pytest.mark.parametrize("geom", [M.GEOM_SQUARE, M.GEOM_CUBE])
-def test_limit_vjp_fd(cuda, fun, geom):
-    case = periodic_case(geom, 4, 1, RS_HLLC)
+@pytest.mark.parametrize("geom,order", [(M.GEOM_SQUARE, 1), (M.GEOM_CUBE, 1), (M.GEOM_CUBE, 2)])
+def test_limit_vjp_fd(cuda, fun, geom, order):
+    case = periodic_case(geom, 4, order, RS_HLLC)
     case.limiter = (LIM_MULTI, IND_BJ, fun, 1, 0)
     ctx = ctx_for(case)
     x = random_state(ctx.node_coords(), seed=5, amp=0.1, vel=0.2)
@@ -113,8 +114,9 @@ def test_limit_vjp_fd(cuda, fun, geom):
     fd_check(apply, vjp, x, seed=2, eps=1e-7)
 
 
-def test_step_vjp_fd(cuda):
-    case = periodic_case(M.GEOM_CUBE, 3, 1, RS_HLLC)
+@pytest.mark.parametrize("order", [1, 2])
+def test_step_vjp_fd(cuda, order):
+    case = periodic_case(M.GEOM_CUBE, 3, order, RS_HLLC)
     case.limiter = (LIM_MULTI, IND_BJ, FUN_VENKATAKRISHNAN, 1, 0)
     case.tableau = TABLEAU_SSPRK3
     ctx = ctx_for(case)
@@ -293,7 +295,7 @@ def _nc(kind, order):
     return cases.Case("nc", m, order, RS_RUSANOV, AVG_TRRS)
 
 
-@pytest.mark.parametrize("kind,order", [("quad", 2), ("quad", 1), ("hex", 1), ("tri", 1)])
+@pytest.mark.parametrize("kind,order", [("quad", 2), ("quad", 1), ("hex", 1), ("hex", 2), ("tri", 1)])
 def test_rhs_vjp_nonconforming_fd(cuda, kind, order):
     """Hanging faces: the slave-face terms (fine element at its own points,
     coarse element at the mapped points) enter u_bar through both sides'
