@@ -234,7 +234,8 @@ int rkdg_batch_run(rkdg_ctx* ctx, double* x_dev, double t_end, double cfl, doubl
                    double* t_out, double* sum_dt_out);
 /* ---- discrete adjoint (FP64 path) ------------------------------------------
  * Vector-Jacobian products of the hot path (no counterpart in the reference,
- * which has no adjoint).  Supported: triangles P1, quads Q1/Q2, hexes Q1/Q2.
+ * which has no adjoint).  Supported: every element type and order of the forward path (triangles
+ * P1/P2, quads Q1-Q3, hexes Q1/Q2).
  * xbar = (d FE_Evolution::Mult / dx)^T kbar: */
 int rkdg_rhs_vjp(rkdg_ctx* ctx, const double* x_dev, const double* kbar_dev, double* xbar_dev);
 /* zbar = (d Limiter::update / dz)^T ybar (active branch of min/max and of the

@@ -5,14 +5,17 @@
 namespace rkdg {
 
 bool adjoint_supported(int geom, int p) {
-  return (geom == 2 && p == 1) || (geom == 3 && (p == 1 || p == 2)) || (geom == 5 && (p == 1 || p == 2));
+  return (geom == 2 && (p == 1 || p == 2)) || (geom == 3 && p >= 1 && p <= 3) ||
+         (geom == 5 && (p == 1 || p == 2));
 }
 
 #define RKDG_ADJ_DISPATCH(CALL)       \
   switch (geom * 10 + p) {            \
     case 21: return CALL(2, 1);       \
+    case 22: return CALL(2, 2);       \
     case 31: return CALL(3, 1);       \
     case 32: return CALL(3, 2);       \
+    case 33: return CALL(3, 3);       \
     case 51: return CALL(5, 1);       \
     case 52: return CALL(5, 2);       \
     default: return cudaErrorInvalidValue; \

@@ -50,6 +50,8 @@ def fd_check(apply, vjp, x, seed, eps=1e-6, tol=1e-5):
                                                   (M.GEOM_CUBE, 2, RS_HLLC, True),
                                                   (M.GEOM_SQUARE, 1, RS_HLL, True),
                                                   (M.GEOM_SQUARE, 2, RS_RUSANOV, False),
+                                                  (M.GEOM_SQUARE, 3, RS_HLLC, True),
+                                                  (M.GEOM_TRIANGLE, 2, RS_HLL, True),
                                                   (M.GEOM_TRIANGLE, 1, RS_HLLC, True)])
 def test_rhs_vjp_fd(cuda, geom, order, rs, walled):
     case = walled_case(geom, 3, order, rs, bc=BC_SLIP) if walled else periodic_case(geom, 3, order, rs)
@@ -94,9 +96,11 @@ def test_rhs_vjp_pressure_bcs_fd(cuda, bc, params, geom):
 
 
 @pytest.mark.parametrize("fun", [FUN_VENKATAKRISHNAN, FUN_MICHALAK])
-@pytest.mark.parametrize("geom,order", [(M.GEOM_SQUARE, 1), (M.GEOM_CUBE, 1), (M.GEOM_CUBE, 2)])
+@pytest.mark.parametrize("geom,order", [(M.GEOM_SQUARE, 1), (M.GEOM_SQUARE, 3), (M.GEOM_CUBE, 1),
+                                        (M.GEOM_CUBE, 2), (M.GEOM_TRIANGLE, 2)])
 def test_limit_vjp_fd(cuda, fun, geom, order):
-    case = periodic_case(geom, 4, order, RS_HLLC)
+    case = (walled_case(geom, 4, order, RS_HLLC, bc=BC_SLIP) if geom == M.GEOM_TRIANGLE
+            else periodic_case(geom, 4, order, RS_HLLC))
     case.limiter = (LIM_MULTI, IND_BJ, fun, 1, 0)
     ctx = ctx_for(case)
     x = random_state(ctx.node_coords(), seed=5, amp=0.1, vel=0.2)
