@@ -218,7 +218,11 @@ int rkdg_riemann_batch(rkdg_ctx* ctx, int n, const double* u1, const double* u2,
  * conditions are shared; gamma and covolume are per problem.  There is no
  * counterpart in the reference, which runs one problem per process; each
  * problem follows the reference's single-problem semantics (main.cpp:467-733)
- * with its own h_min, CFL dt and time. */
+ * with its own h_min, CFL dt and time.  Adapted (nonconforming) problems are
+ * allowed; since rkdg_upload_mesh pairs hanging faces by position, such
+ * problems must occupy disjoint regions of space, and offsets that put the
+ * two sides of a face or hanging face into different problems return
+ * RKDG_ERR_INVALID.  Quadrilaterals and triangles. */
 int rkdg_batch_setup(rkdg_ctx* ctx, int nprob, const int* elem_offsets,
                      const double* gamma, const double* covolume);
 /* Advance every problem to t_end (dt_mode as rkdg_run, per problem).  With

@@ -78,6 +78,7 @@ struct rkdg_ctx {
   long long ndofs = 0;
   RefTables tab;
   std::vector<int> h_fnbr, h_fattr, h_fcode;
+  std::vector<int> h_nc_face;  // hanging faces [nnc][4] (fine element, its face, coarse element, its face)
   std::vector<double> h_fgeo, h_egeo, h_wdet, h_nodes;
   double hmin = 0.0;
   // device tables
@@ -205,6 +206,7 @@ void free_mesh(rkdg_ctx* c) {
   dfree(c->d_ncidx);
   dfree(c->d_xface);
   c->nnc = c->nc_nel = 0;
+  c->h_nc_face.clear();
   dfree(c->d_ngeo64);
   dfree(c->d_ngeo32);
   dfree(c->d_wmn64);
@@ -1218,6 +1220,7 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
   if (!slaves.empty()) {
     const int nns = (int)slaves.size();
     c->nnc = nns;
+    c->h_nc_face = nc_face;
     c->nc_nel = (int)nc_elem.size();
     CUDA_TRY(c, dalloc(c->d_nc_face, nc_face.size()));
     CUDA_TRY(c, dalloc(c->d_nc_bnc, nc_bnc.size()));
@@ -1456,7 +1459,6 @@ int rkdg_batch_setup(rkdg_ctx* c, int nprob, const int* elem_offsets, const doub
     return fail(c, RKDG_ERR_INVALID, "invalid batch description");
   if (c->geom == RKDG_GEOM_CUBE)
     return fail(c, RKDG_ERR_UNSUPPORTED, "batched problems are supported on triangles and quads");
-  if (c->nnc) return fail(c, RKDG_ERR_UNSUPPORTED, "batched problems on meshes with hanging faces");
   if (elem_offsets[0] != 0 || elem_offsets[nprob] != c->ne)
     return fail(c, RKDG_ERR_INVALID, "element offsets must cover the mesh");
   std::vector<int> prob(c->ne);
@@ -1476,6 +1478,11 @@ int rkdg_batch_setup(rkdg_ctx* c, int nprob, const int* elem_offsets, const doub
       if (nb >= 0 && prob[nb] != prob[e])
         return fail(c, RKDG_ERR_INVALID, "problems are connected through a face", e);
     }
+  for (int f = 0; f < c->nnc; ++f) {
+    const int e1 = c->h_nc_face[(size_t)f * 4], e2 = c->h_nc_face[(size_t)f * 4 + 2];
+    if (prob[e1] != prob[e2])
+      return fail(c, RKDG_ERR_INVALID, "problems are connected through a hanging face", e1);
+  }
   c->nprob = nprob;
   c->h_poff.assign(elem_offsets, elem_offsets + nprob + 1);
   CUDA_TRY(c, dalloc(c->d_prob, (size_t)c->ne));

@@ -41,7 +41,13 @@ __global__ void __launch_bounds__(kNcFaceThreads) k_nc_face(const __grid_constan
   const int lf = threadIdx.x / NQF, q = threadIdx.x - lf * NQF;
   const int f = blockIdx.x * FPC + lf;
   R lmax = R(0);
-  if (lf < FPC && f < nc.nnc) {
+  int pb = -1;  // batched problems: the face's problem (both elements share it)
+  bool live = lf < FPC && f < nc.nnc;
+  if (live && prm.prob) {
+    pb = prm.prob[nc.face[f * 4]];
+    live = prm.pactive[pb] != 0;
+  }
+  if (live) {
     const int e1 = nc.face[f * 4], lf1 = nc.face[f * 4 + 1], e2 = nc.face[f * 4 + 2];
     const int ne = prm.ne;
     const long long NDa = prm.ndofs;
@@ -72,20 +78,27 @@ __global__ void __launch_bounds__(kNcFaceThreads) k_nc_face(const __grid_constan
       s1[k] = a;
       s2[k] = b;
     }
-    const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+    const R gamma = (R)(pb >= 0 ? prm.pgamma[pb] : prm.gamma);
+    const R cov = (R)(pb >= 0 ? prm.pcov[pb] : prm.covolume);
     R F[NEQ];
-    lmax = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e1);
+    lmax = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e1, pb);
     const R wq = (R)T->wf[q];
 #pragma unroll
     for (int k = 0; k < NEQ; ++k) sF[lf][q][k] = (F[k] * wq) * jac;
   }
-  block_max_commit<R>(lmax, prm.mcs);  // contains a CTA barrier: sF is complete after it
+  if (prm.prob) {  // per-problem maximum; a face point of an idle problem commits nothing
+    if (pb >= 0) atomic_max_nonneg(prm.pmcs + pb, (double)lmax);
+    __syncthreads();  // sF is complete after it
+  } else {
+    block_max_commit<R>(lmax, prm.mcs);  // contains a CTA barrier: sF is complete after it
+  }
   if (!with_terms) return;
   for (int o = threadIdx.x; o < FPC * 2 * ND; o += blockDim.x) {
     const int c = o / (2 * ND), r = o - c * 2 * ND;
     const int side = r / ND, j = r - side * ND;
     const int fc = blockIdx.x * FPC + c;
     if (fc >= nc.nnc) break;
+    if (prm.prob && !prm.pactive[prm.prob[nc.face[fc * 4]]]) continue;  // idle problem
     const int lf1 = nc.face[fc * 4 + 1];
     const R sg = side ? R(1) : R(-1);
     R acc[NEQ];

@@ -129,3 +129,59 @@ def test_batch_full_size(cuda):
             xr, ir = orc.run(cases.project(c, orc.node_coords()), c.t_end, c.cfl)
             assert info["steps"][p] == ir["steps"], p
             assert rel_l1(xb[0], xr[:orc.ndofs]) < 1e-8, p
+
+
+def test_batch_nonconforming(cuda):
+    """A batch whose problems are adapted meshes (a few elements at the
+    interface refined, leaving hanging faces): each problem bit-identical to
+    the same problem alone, and close to its own oracle run.  Hanging faces
+    are paired by position when the mesh is uploaded, so the problems sit in
+    disjoint regions (problem p shifted by 2p in y; the initial states depend
+    on x only)."""
+    from rkdg3d_gb300 import mesh as M
+    bc = _batch(nprob=4, nmin=16, nmax=30)
+    for p, c in enumerate(bc.cases):
+        nx = c.mesh.num_elements // 4
+        m = M.refine_nc(c.mesh, [nx // 2 - 1, nx // 2, nx + nx // 2])
+        c.mesh = M.Mesh(m.dim, m.geom, m.elem_vertices, m.elem_coords + np.array([0.0, 2.0 * p]),
+                        m.bdr_vertices, m.bdr_attr)
+    offs = np.concatenate([[0], np.cumsum([c.mesh.num_elements for c in bc.cases])]).astype(np.int32)
+    bc = cases.BatchCase(bc.cases, cases.union_mesh([c.mesh for c in bc.cases]), offs, bc.gammas,
+                         bc.covolumes, bc.order, bc.t_end, bc.cfl)
+    ctx = _ctx(bc)
+    xd = torch.tensor(bc.project(ctx.node_coords()), dtype=torch.float64, device="cuda")
+    info = ctx.batch_run(xd, bc.t_end, bc.cfl)
+    x = xd.cpu().numpy().reshape(4, -1)
+    nd, nok = 4, 0
+    for p, c in enumerate(bc.cases):
+        orc = Oracle(c.mesh, c.order)
+        cases.configure_oracle(c, orc)
+        try:
+            xr, ir = orc.run(cases.project(c, orc.node_coords()), c.t_end, c.cfl)
+        except OracleError:
+            assert info["steps"][p] < 0, p
+            continue
+        e0, e1 = bc.offsets[p], bc.offsets[p + 1]
+        xb = x[:, e0 * nd:e1 * nd]
+        single = Context(c.mesh, c.order, device=0, precision=FP64)
+        cases.configure_context(c, single)
+        xs = torch.tensor(cases.project(c, single.node_coords()), dtype=torch.float64, device="cuda")
+        isg = single.run(xs, c.t_end, c.cfl)
+        assert info["steps"][p] == isg["steps"] == ir["steps"], p
+        assert np.array_equal(xb, xs.cpu().numpy().reshape(4, -1)), p
+        assert rel_l1(xb[0], xr[:orc.ndofs]) < 1e-8, p
+        nok += 1
+    assert nok >= 2
+
+
+def test_batch_rejects_problems_joined_by_hanging_faces(cuda):
+    """Offsets that put the two sides of a hanging face into different
+    problems are refused."""
+    from rkdg3d_gb300 import mesh as M
+    from rkdg3d_gb300.solver import RkdgError
+    c = _batch(nprob=1, nmin=8, nmax=8).cases[0]
+    m = M.refine_nc(c.mesh, [31])  # the corner element: its four children are the last elements
+    ctx = Context(m, 1, device=0)
+    cases.configure_context(c, ctx)
+    with pytest.raises(RkdgError, match="hanging face"):
+        ctx.batch_setup([0, m.num_elements - 4, m.num_elements], [1.4, 1.4], [0.0, 0.0])

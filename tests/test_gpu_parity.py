@@ -500,18 +500,13 @@ def test_limiter_nonconforming(cuda, kind, order, lim, ind, fun):
 
 def test_nonconforming_mesh_errors(cuda):
     """A hole (faces with neither a neighbour, a boundary element nor hanging
-    faces covering them) is an invalid mesh; batched problems on meshes with
-    hanging faces are not supported and say so."""
+    faces covering them) is an invalid mesh."""
     from rkdg3d_gb300.solver import RkdgError
     m = M.hex_grid(3, 3, 3, periodic=(False,) * 3)
     keep = [e for e in range(m.num_elements) if e != 13]
     holed = M.Mesh(3, M.GEOM_CUBE, m.elem_vertices[keep], m.elem_coords[keep], m.bdr_vertices, m.bdr_attr)
     with pytest.raises(RkdgError):
         Context(holed, 1, device=0)
-    case = _nc_case("quad", 1)
-    ctx, _ = pair(case)
-    with pytest.raises(RkdgError, match="hanging"):
-        ctx.batch_setup([0, ctx.ne], [1.4], [0.0])
 
 
 @pytest.mark.parametrize("prec", [0, 1])
