@@ -26,6 +26,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -58,7 +59,7 @@ TRAFFIC_BYTES_PER_ELEMENT_LAUNCH = 2979.5
 
 
 def algorithmic_bytes_per_step(N, ne, precision):
-    """Bytes one SSP-RK3 step must move at stored widths (see DESIGN.md):
+    """Bytes one SSP-RK3 step must move at stored widths:
     FP32-bulk: stage 0 reads x_hi, x_lo, writes k0, y1 (16N); stage 1 reads
     y1, x_hi, x_lo, k0, writes k1, y2 (24N); stage 2 reads y2, k0, k1, x_hi,
     x_lo, writes x_hi, x_lo (28N).  FP64: stage 0 reads x, writes k0, y1
@@ -83,7 +84,9 @@ class ClockSampler:
     def __init__(self, gpu_index=0):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # the per-sample log goes to RKDG_CLOCKS_DIR (default: the system temp folder)
+        self.path = os.path.join(os.environ.get("RKDG_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"clocks_bench_{os.getpid()}.csv")
 
     def __enter__(self):
         try:

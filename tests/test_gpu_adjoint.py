@@ -2,7 +2,7 @@
 plain FP64 GPU path (itself parity-checked against the oracle).
 
 Directional check: <v, J^T w> versus (<w, F(x + eps v)> - <w, F(x - eps v)>) / (2 eps)
-with relative tolerance 1e-5 (the benchmark spec's bar for the gradient)."""
+with relative tolerance 1e-5 (the bar set for the gradient)."""
 import numpy as np
 import pytest
 import torch
@@ -187,7 +187,7 @@ def test_adjoint_gradient_full_size(cuda):
     stencil values switch branches and the indicator's absolute +-1e-3
     thresholds (indicator_bj.cpp:49-51) jump, and over 600 limited stages some
     switch usually lies within a few 1e-8 of the state along a random
-    direction.  A direction is therefore judged only when two central
+    direction.  A direction is therefore assessed only when two central
     differences (eps = 4e-6 and 1e-6) agree with each other to 1e-5 -- no
     switch inside the window -- and there the adjoint must agree to 1e-5.
     RKDG_ADJOINT_DIRECTIONS sets the number of random directions (64 for the
@@ -222,16 +222,16 @@ def test_adjoint_gradient_full_size(cuda):
     g = xb.cpu().numpy()
     ndir = int(os.environ.get("RKDG_ADJOINT_DIRECTIONS", "12"))
     rng = np.random.default_rng(5)
-    judged, worst = 0, 0.0
+    assessed, worst = 0, 0.0
     for _ in range(ndir):
         v = rng.normal(size=ctx.n) * 1e-2
         ad = float(np.dot(g, v))
         fd = [(J(x0 + e * v) - J(x0 - e * v)) / (2 * e) for e in (4e-6, 1e-6)]
         if abs(fd[0] - fd[1]) > 1e-5 * abs(fd[1]):
             continue  # a limiter switch inside the difference window
-        judged += 1
+        assessed += 1
         worst = max(worst, abs(ad - fd[1]) / abs(fd[1]))
-    assert judged >= ndir // 3, (judged, ndir)
+    assert assessed >= ndir // 3, (assessed, ndir)
     assert worst <= 1e-5, worst
 
 
