@@ -129,7 +129,11 @@ int rkdg_upload_mesh(rkdg_ctx* ctx, const rkdg_mesh_desc* mesh);
  * which also fires on HLLC's signed max(SL, SR) (rs_hllc.cpp:98) in
  * supersonic flow against the face normal; with this flag only the -1 of a
  * non-physical state is an error. */
-enum { RKDG_QUIRK_HLLC_NEGATIVE_SPEED_OK = 1 };
+/* RKDG_QUIRK_NO_INITIAL_LIMIT: rkdg_run and rkdg_batch_run step the state as
+ * given.  By default they first limit it once, as the reference limits the
+ * projected initial solution before its time loop (main.cpp:264-265); set the
+ * flag to continue a run from a state that was already limited. */
+enum { RKDG_QUIRK_HLLC_NEGATIVE_SPEED_OK = 1, RKDG_QUIRK_NO_INITIAL_LIMIT = 2 };
 int rkdg_set_solver_quirks(rkdg_ctx* ctx, int flags);
 /* Replaces CaseManager::addBoundaryIntegrators (case_manager.cpp:614-820)
  * for one boundary attribute.  state: conservative variables or NULL. */
@@ -194,7 +198,8 @@ int rkdg_cell_means(rkdg_ctx* ctx, const double* x_dev, double* means_dev);
  * (as the reference).  *next_mcs (host, may be NULL) = max_char_speed of the
  * last stage, which the reference turns into the next dt (main.cpp:538-547). */
 int rkdg_step(rkdg_ctx* ctx, double* x_dev, double dt, double* next_mcs);
-/* The time loop of main.cpp:467-553,701-733.
+/* The time loop of main.cpp:467-553,701-733, preceded by the limit of the
+ * initial state (main.cpp:264-265) unless RKDG_QUIRK_NO_INITIAL_LIMIT is set.
  * dt_mode 0: dynamic CFL dt; 1: dt from CFL once at t=0, then constant;
  * 2: constant dt0.  max_steps > 0 stops early.  Outputs (host, may be NULL):
  * steps taken, t as the reference books it (t += new dt), last dt, and the
@@ -225,7 +230,8 @@ int rkdg_riemann_batch(rkdg_ctx* ctx, int n, const double* u1, const double* u2,
  * RKDG_ERR_INVALID.  Quadrilaterals and triangles. */
 int rkdg_batch_setup(rkdg_ctx* ctx, int nprob, const int* elem_offsets,
                      const double* gamma, const double* covolume);
-/* Advance every problem to t_end (dt_mode as rkdg_run, per problem).  With
+/* Advance every problem to t_end (dt_mode as rkdg_run, per problem; the
+ * initial limit as rkdg_run).  With
  * use_graph != 0 the whole multi-step solve is one CUDA-graph launch: the RK
  * step is captured once as the body of a device-controlled while node and the
  * loop ends on the device when the last problem finishes.  Host outputs

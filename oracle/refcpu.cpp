@@ -1750,6 +1750,12 @@ int ref_step(ref_ctx* c, double* x, double dt, double* next_mcs) {
 
 int ref_run(ref_ctx* c, double* x, double t_end, double cfl, double dt0, int dt_mode,
             int max_steps, int* steps_out, double* t_out, double* dt_out, double* sum_dt_out) {
+  // The projected initial state is limited once before the initial dt and the
+  // loop (main.cpp:264-265, `l->update(sol)` after loadInitialSolution).
+  if (!(c->solver_quirks & 2)) {
+    int st = ref_limit(c, x);
+    if (st) return st;
+  }
   const double hmin = (dt_mode == 2) ? 0.0 : ref_hmin(c);
   double dt = dt0;
   if (dt_mode != 2) {
@@ -1813,6 +1819,39 @@ double ref_total_energy(ref_ctx* c, const double* x) {
     tot += te * c->ops[c->op_of[e]].detJ_c;
   }
   return tot;
+}
+
+int ref_pointwise(ref_ctx* c, int what, int n, const double* u1, const double* u2,
+                  const double* nor, double* out) {
+  const int neq = c->neq, dim = c->dim;
+  const Phys& P = c->P;
+  for (int i = 0; i < n; ++i) {
+    double s1[5], s2[5];
+    for (int k = 0; k < neq; ++k) {
+      s1[k] = u1[i * neq + k];
+      s2[k] = u2 ? u2[i * neq + k] : 0.0;
+    }
+    if (what == 0) {
+      double* o = out + (size_t)i * 4;
+      o[0] = pressure(P, s1);
+      o[1] = sound_speed(P, s1);
+      o[2] = max_char_speed_of(P, s1);
+      o[3] = state_is_physical(P, s1) ? 1.0 : 0.0;
+    } else if (what == 1) {
+      flux_full(P, s1, out + (size_t)i * neq * dim);
+    } else if (what == 2 || what == 3) {
+      rotate(dim, s1, &nor[i * dim]);
+      rotate(dim, s2, &nor[i * dim]);
+      if (what == 2)
+        toro_speeds(P, s1, s2, out + (size_t)i * neq);
+      else
+        einfeldt_speeds(P, s1, s2, out + (size_t)i * neq);
+    } else {
+      c->err = "unknown pointwise quantity";
+      return REF_ERR_INVALID;
+    }
+  }
+  return REF_OK;
 }
 
 int ref_riemann(ref_ctx* c, int n, const double* u1, const double* u2, const double* nor,

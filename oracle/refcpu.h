@@ -77,7 +77,9 @@ int ref_set_limiter(ref_ctx* c, int limiter, int indicator, int function,
 int ref_set_tableau(ref_ctx* c, int s, const double* a, const double* b,
                     const double* cc);
 /* bit 0: a negative HLLC wave speed (signed max(SL,SR)) is not treated as a
- * non-physical state (the reference exits on it). */
+ * non-physical state (the reference exits on it); bit 1: ref_run does not
+ * limit the initial state (the reference limits the projected state once
+ * before its time loop, main.cpp:264-265). */
 int ref_set_solver_quirks(ref_ctx* c, int flags);
 void ref_set_threads(int n);
 
@@ -99,7 +101,8 @@ int ref_step(ref_ctx* c, double* x, double dt, double* next_mcs);
  * dt_mode 0: dynamic CFL dt (time.type: dynamic);
  * dt_mode 1: dt computed once from cfl at t=0, then kept constant;
  * dt_mode 2: constant dt = dt0 (time.type: constant).
- * max_steps > 0 stops after that many steps. */
+ * max_steps > 0 stops after that many steps.  Unless solver quirk bit 1 is
+ * set, x is limited once first (main.cpp:264-265). */
 int ref_run(ref_ctx* c, double* x, double t_end, double cfl, double dt0,
             int dt_mode, int max_steps, int* steps_out, double* t_out,
             double* dt_out, double* sum_dt_out);
@@ -108,6 +111,12 @@ double ref_total_energy(ref_ctx* c, const double* x); /* check_total_energy.cpp 
 /* pointwise Riemann solver on n states: u1,u2 [n][neq], nor [n][dim] (unit) */
 int ref_riemann(ref_ctx* c, int n, const double* u1, const double* u2,
                 const double* nor, double* flux, double* speed);
+/* pointwise physics (test hook): what 0 = EoS of u1, out[n][4] = pressure,
+ * sound speed, max characteristic speed, StateIsPhysical; 1 = physical flux
+ * of u1, out[n][neq][dim]; 2 / 3 = TRRS / Einfeldt wave speeds of u1, u2
+ * rotated into nor's frame, out[n][neq]. */
+int ref_pointwise(ref_ctx* c, int what, int n, const double* u1, const double* u2,
+                  const double* nor, double* out);
 const char* ref_last_error(ref_ctx* c);
 
 #ifdef __cplusplus

@@ -64,6 +64,7 @@ def lib():
         L.ref_total_energy.restype = C.c_double
         L.ref_total_energy.argtypes = [C.c_void_p, _dp]
         L.ref_riemann.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp]
+        L.ref_pointwise.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _dp]
         L.ref_last_error.restype = C.c_char_p
         L.ref_last_error.argtypes = [C.c_void_p]
         _lib = L
@@ -141,6 +142,7 @@ class Oracle:
 
     def set_solver_quirks(self, flags):
         self._chk(lib().ref_set_solver_quirks(self.h, int(flags)))
+        self._solver_quirks = int(flags)
 
     def set_tableau(self, s, a, b, c):
         a = np.ascontiguousarray(a if len(a) else [0.0], dtype=np.float64)
@@ -192,7 +194,12 @@ class Oracle:
         self._chk(lib().ref_step(self.h, _d(x), dt, C.byref(m)))
         return x, m.value
 
-    def run(self, x, t_end, cfl=0.3, dt0=0.0, dt_mode=0, max_steps=0):
+    def run(self, x, t_end, cfl=0.3, dt0=0.0, dt_mode=0, max_steps=0, limit_initial=True):
+        """ref_run; limit_initial limits x once first (main.cpp:264-265)."""
+        q = getattr(self, "_solver_quirks", 0)
+        want = (q & ~2) | (0 if limit_initial else 2)
+        if want != q:
+            self.set_solver_quirks(want)
         x = np.array(x, dtype=np.float64, copy=True)
         steps = C.c_int()
         t = C.c_double()
@@ -211,6 +218,20 @@ class Oracle:
     def total_energy(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
         return float(lib().ref_total_energy(self.h, _d(x)))
+
+    def pointwise(self, what, u1, u2=None, nor=None):
+        """ref_pointwise: what 0 EoS [n][4] (p, c, max speed, physical),
+        1 flux [n][neq][dim], 2 TRRS / 3 Einfeldt speeds [n][neq] of u1, u2
+        rotated into nor's frame."""
+        u1 = np.ascontiguousarray(u1, dtype=np.float64)
+        n = u1.shape[0]
+        u2 = None if u2 is None else np.ascontiguousarray(u2, dtype=np.float64)
+        nor = None if nor is None else np.ascontiguousarray(nor, dtype=np.float64)
+        width = {0: 4, 1: self.neq * self.dim, 2: self.neq, 3: self.neq}[what]
+        out = np.zeros((n, width))
+        self._chk(lib().ref_pointwise(self.h, what, n, _d(u1), None if u2 is None else _d(u2),
+                                      None if nor is None else _d(nor), _d(out)))
+        return out
 
     def riemann(self, u1, u2, nor):
         u1 = np.ascontiguousarray(u1, dtype=np.float64)

@@ -294,7 +294,7 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   P.rs = c->rs;
   P.avg = c->avg;
   P.faces_only = faces_only;
-  P.quirks = c->solver_quirks;
+  P.quirks = c->solver_quirks & RKDG_QUIRK_HLLC_NEGATIVE_SPEED_OK;
   int k = 0;
   for (auto& kv : c->bcs) P.bc[k++] = kv.second;
   P.mcs = c->d_mcs + slot;
@@ -796,7 +796,8 @@ int rkdg_set_precision(rkdg_ctx* c, int precision) {
 
 int rkdg_set_solver_quirks(rkdg_ctx* c, int flags) {
   if (!c) return RKDG_ERR_INVALID;
-  if (flags & ~1) return fail(c, RKDG_ERR_INVALID, "unknown solver quirk flag");
+  if (flags & ~(RKDG_QUIRK_HLLC_NEGATIVE_SPEED_OK | RKDG_QUIRK_NO_INITIAL_LIMIT))
+    return fail(c, RKDG_ERR_INVALID, "unknown solver quirk flag");
   c->solver_quirks = flags;
   return RKDG_OK;
 }
@@ -1371,6 +1372,12 @@ int rkdg_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0, int d
   int st = ensure_scratch(c);
   if (st) return st;
   const long long n = c->ndofs * c->neq;
+  // The reference limits the projected initial state once before it forms the
+  // initial dt and enters the loop (main.cpp:264-265).
+  if (!(c->solver_quirks & RKDG_QUIRK_NO_INITIAL_LIMIT)) {
+    st = rkdg_limit(c, x);
+    if (st) return st;
+  }
   double dt = dt0;
   const double denom = 2.0 * c->p + 1.0;
   if (dt_mode != 2) {
@@ -1540,6 +1547,13 @@ int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0,
   {
     std::vector<int> ones(np, 1);
     CUDA_TRY(c, cudaMemcpyAsync(c->d_pactive, ones.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    // each problem's projected state is limited once first (main.cpp:264-265)
+    if (c->limiter_active() && !(c->solver_quirks & RKDG_QUIRK_NO_INITIAL_LIMIT)) {
+      CUDA_TRY(c, rkdg::launch_means(c->geom, c->p, 0, c->ne, c->ndofs, c->d_tab, x, nullptr, c->d_means, c->stream));
+      LimParams L = lim_params_for(c, true);
+      CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 0, L, x, nullptr, c->stream));
+      c->launches += 2;
+    }
     CUDA_TRY(c, zero_slot(c, c->s - 1, true));
     EpiParams<double> ep;
     std::memset(&ep, 0, sizeof ep);

@@ -42,6 +42,8 @@ IND_NOWHERE, IND_EVERYWHERE, IND_BJ, IND_SHU = 0, 1, 2, 3
 FUN_BJ, FUN_VENKATAKRISHNAN, FUN_MICHALAK = 0, 1, 2
 QUIRK_MULTIPLIER_ONCE = 1
 FP64, FP32_BULK = 0, 1
+# flags of set_solver_quirks
+QUIRK_HLLC_NEGATIVE_SPEED_OK, QUIRK_NO_INITIAL_LIMIT = 1, 2
 TUNE_HEX_KERNEL, TUNE_GENERIC_BLOCK, TUNE_LIMITER_BLOCK = 1, 2, 3
 # flags of set_limiter(quirks=...)
 QUIRK_MULTIPLIER_ONCE, LIMITER_LINEARIZE = 1, 2
@@ -201,6 +203,13 @@ class Context:
 
     def set_solver_quirks(self, flags: int):
         self._chk(self._L.rkdg_set_solver_quirks(self.h, flags))
+        self._solver_quirks = int(flags)
+
+    def _initial_limit(self, on: bool):
+        q = getattr(self, "_solver_quirks", 0)
+        q = (q & ~QUIRK_NO_INITIAL_LIMIT) | (0 if on else QUIRK_NO_INITIAL_LIMIT)
+        if q != getattr(self, "_solver_quirks", 0):
+            self.set_solver_quirks(q)
 
     def set_tuning(self, key: int, value: int):
         self._chk(self._L.rkdg_set_tuning(self.h, key, value))
@@ -262,9 +271,13 @@ class Context:
         return m.value
 
     def run(self, x, t_end: float, cfl: float = 0.3, dt0: float = 0.0, dt_mode: int = 0,
-            max_steps: int = 0) -> dict:
+            max_steps: int = 0, limit_initial: bool = True) -> dict:
+        """The reference's time loop (rkdg_run).  limit_initial: limit x once
+        before the first dt, as the reference does with the projected initial
+        state (main.cpp:264-265); False continues from a state as given."""
         if max_steps <= 0 and not (t_end < 1e20):
             raise ValueError("run() needs a finite t_end or max_steps > 0")
+        self._initial_limit(limit_initial)
         steps = C.c_int()
         t = C.c_double()
         dt = C.c_double()
@@ -310,8 +323,9 @@ class Context:
                                            g.ctypes.data_as(_capi._dp), b.ctypes.data_as(_capi._dp)))
 
     def batch_run(self, x, t_end: float, cfl: float = 0.3, dt0: float = 0.0, dt_mode: int = 0,
-                  max_steps: int = 0, use_graph: bool = True) -> dict:
+                  max_steps: int = 0, use_graph: bool = True, limit_initial: bool = True) -> dict:
         np_ = self.nprob
+        self._initial_limit(limit_initial)
         steps = np.zeros(np_, np.int32)
         t = np.zeros(np_)
         sdt = np.zeros(np_)

@@ -155,13 +155,13 @@ def test_adjoint_run_gradient(cuda):
 
     def J(xx):
         y = dev(xx)
-        ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps)
+        ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps, limit_initial=False)
         r = y.cpu().numpy()[:nd] - xt[:nd]
         return 0.5 * float(np.dot(r, r))
 
     xT = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
     y = dev(x0)
-    ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps)
+    ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps, limit_initial=False)
     xbar = np.zeros(ctx.n)
     xbar[:nd] = y.cpu().numpy()[:nd] - xt[:nd]
     xb = dev(xbar)
@@ -202,17 +202,17 @@ def test_adjoint_gradient_full_size(cuda):
     nsteps, every = 200, 20
     dt = case.cfl * ctx.hmin() / ctx.face_speed(dev(x0)) / (2 * case.order + 1)
     yt = dev(cases.project(target, X))
-    ctx.run(yt, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps)
+    ctx.run(yt, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps, limit_initial=False)
     rho_t = yt.cpu().numpy()[:nd]
 
     def J(xx):
         y = dev(xx)
-        ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps)
+        ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps, limit_initial=False)
         r = y.cpu().numpy()[:nd] - rho_t
         return 0.5 * float(np.dot(r, r))
 
     y = dev(x0)
-    ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps)
+    ctx.run(y, 1e30, dt0=dt, dt_mode=2, max_steps=nsteps, limit_initial=False)
     xbar = np.zeros(ctx.n)
     xbar[:nd] = y.cpu().numpy()[:nd] - rho_t
     xb = dev(xbar)
