@@ -138,6 +138,32 @@ struct HexTeamSched {
   int nr;                                                 // rounds used by this CTA
 };
 
+// Tile of the face-once hexahedral kernel (k_rhs_hex_tile): RKDG_TILE_E
+// elements that are consecutive in the Morton order of their centres (on a
+// structured 2^k mesh a 4 x 4 x 2 block).  Per normal axis a of the elements'
+// local faces (0: faces 4/2, 1: faces 1/3, 2: faces 0/5) the tile lists the
+// face evaluations of its face sides on that axis, each face once: a face
+// between two tile elements whose local faces share the axis is evaluated by
+// its Elem1 side; a face to an element outside the tile (or across axes) by
+// the tile side, with the outside element's trace formed from global memory
+// (a "halo"); a boundary face by its element with the boundary condition the
+// context holds at launch time.  One word per evaluation:
+//   bits 0-5 Elem1 side (face side 2*slot + s, or halo index), 6 Elem1 is a
+//   halo, 7-12 Elem2 side (likewise), 13 Elem2 is a halo, 14 boundary face
+//   (no Elem2), 15-17 Elem1's local face, 18-20 Elem2's local face, 21-23
+//   point permutation id, 24 the face geometry is read at the Elem2 side.
+#define RKDG_TILE_E 32
+#define RKDG_TILE_HMAX 64  // = 2 * RKDG_TILE_E: every face side of a tile axis can be a halo
+struct HexTile {
+  int el[RKDG_TILE_E];                      // element of each slot (-1: none)
+  int nel;                                  // slots in use
+  int nev[3];                               // evaluations per axis
+  int nh[3];                                // halo traces per axis
+  unsigned int ev[3][2 * RKDG_TILE_E];      // evaluations (packed, see above)
+  int hel[3][RKDG_TILE_HMAX];               // halo: element outside the tile
+  unsigned char hlf[3][RKDG_TILE_HMAX];     // halo: its local face
+};
+
 // Per-element face table entry codes (fcode): bits 0-2 local face of the
 // other element, bit 3 = 1 if this element is the face's Elem2, bits 4..
 // permutation id.  fnbr: neighbour element id, -1 = boundary face with no
@@ -170,6 +196,8 @@ struct RhsParams {
   int block;            // threads per CTA of the generic kernels (0: default)
   void* fslot;          // hexahedral face-pass flux slots [ne][6][neq][nqf] (or null)
   const HexTeamSched* hsched;  // shared-face hexahedral kernel: one entry per CTA (or null)
+  const HexTile* htile;        // face-once tiled hexahedral kernel: one entry per CTA (or null)
+  int ntile;
   // nonconforming meshes: element -> row of xface (-1: none) and the face
   // terms of the hanging faces, [row][neq][nd] in the kernel's precision,
   // added to the element's face + volume terms before the inverse mass

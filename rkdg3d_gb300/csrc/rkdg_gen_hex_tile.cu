@@ -1,0 +1,36 @@
+// Hexahedra: the face-once tiled right-hand-side kernel (rkdg_hex_tile.cuh),
+// in its own translation unit so that it compiles next to the team kernels.
+#include "rkdg_hex_tile.cuh"
+#include "rkdg_launch.h"
+
+namespace rkdg {
+
+template <int P, typename R>
+static cudaError_t launch_tile(const RhsParams& prm, const R* u, const EpiParams<R>& ep,
+                               cudaStream_t st) {
+  using S = TileSize<P>;
+  const size_t smem = S::template smem_bytes<R>();
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_rhs_hex_tile<P, R>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  k_rhs_hex_tile<P, R><<<prm.ntile, S::NT, smem, st>>>(prm, u, ep);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hex_tile(int p, int prec, const RhsParams& prm, const void* u, const void* ep,
+                            cudaStream_t st) {
+  if (!prm.htile || prm.ntile <= 0) return cudaErrorInvalidValue;
+  if (p == 1)
+    return prec == 0 ? launch_tile<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)
+                     : launch_tile<1, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+  if (p == 2)
+    return prec == 0 ? launch_tile<2, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)
+                     : launch_tile<2, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace rkdg

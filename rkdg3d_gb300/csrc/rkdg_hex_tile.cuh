@@ -1,0 +1,422 @@
+// Face-once tiled hexahedral right-hand side (k_rhs_hex_tile).
+//
+// One CTA per tile of RKDG_TILE_E hexahedra that are consecutive in the Morton
+// order of their centres (HexTile, built on the host).  NEQ * E threads; thread
+// (variable k, slot el) keeps its element's (p+1)^3 values of variable k and
+// the right-hand-side accumulators in registers for the whole stage (a warp
+// holds one variable of 32 elements, so variable-dependent code never
+// diverges).  The faces are processed one normal axis at a time:
+//   1. each thread forms its element's traces on the axis's two faces at the
+//      (p+2)^2 face points (contraction along the normal, then the 2D
+//      interpolation, sum-factorised) into shared memory; threads without a
+//      face job form the traces of the out-of-tile elements across the
+//      tile's faces ("halo", from global memory);
+//   2. the CTA evaluates every face of the axis ONCE, spread over all threads
+//      point by point: a face between two tile elements is evaluated with both
+//      stored traces and its result is written to both sides (the two halves of
+//      the face term of FaceIntegrator::AssembleFaceVector,
+//      face_integrator.cpp:11-276: Elem1, Elem2 argument order, the
+//      Elem1-outward normal, -w|J_f| F on Elem1's side and +w|J_f| F on
+//      Elem2's); a boundary face through its boundary condition's right state
+//      (boundary_integrator.cpp:12-194);
+//   3. each thread lifts its two faces' weighted fluxes into its accumulators.
+// Then the collocated volume term (FE_Evolution::GetFlux and the Aflux product,
+// fe_evolution.cpp:157-171, 219-245), the inverse of the exact mass matrix
+// det J (M1 x M1 x M1) as three 1D sweeps (fe_evolution.cpp:178-208), and the
+// Runge-Kutta stage epilogue with coalesced accesses.
+//
+// Against the five-lane team kernel this evaluates a face inside the tile
+// once instead of twice, forms each trace once, and spreads the pointwise
+// numerical fluxes over every thread of the CTA.
+#pragma once
+
+#include "rkdg_common.h"
+#include "rkdg_generic.cuh"
+#include "rkdg_hex_team.cuh"
+#include "rkdg_physics.cuh"
+
+namespace rkdg {
+
+template <int P>
+struct TileSize {
+  static constexpr int N1 = P + 1, NQ1 = P + 2, ND = N1 * N1 * N1, NQF = NQ1 * NQ1, NEQ = 5,
+                       NF2 = N1 * N1;
+  static constexpr int E = RKDG_TILE_E, NT = NEQ * E, HM = RKDG_TILE_HMAX;
+  // staged DOFs [NEQ][E][ND], own traces / weighted fluxes of one axis
+  // [E][2][NEQ][NQF], halo traces [HM][NEQ][NQF]
+  static constexpr int OFF_T = NEQ * E * ND, OFF_H = OFF_T + E * 2 * NEQ * NQF,
+                       TOTAL = OFF_H + HM * NEQ * NQF;
+  template <typename R>
+  static constexpr size_t smem_bytes() { return sizeof(R) * (size_t)TOTAL; }
+  template <typename R>
+  __host__ __device__ static constexpr int min_ctas() { return sizeof(R) == 4 ? 3 : 2; }
+};
+
+// Local face of axis AX on side SD (MFEM hexahedron numbering).
+__host__ __device__ constexpr int hex_axis_face(int ax, int sd) {
+  return ax == 0 ? (sd ? 2 : 4) : (ax == 1 ? (sd ? 3 : 1) : (sd ? 5 : 0));
+}
+
+// Trace of an out-of-tile element's variable at the points of its local face
+// lfo (tensor order), read from global memory.
+template <int P, typename R>
+__device__ __forceinline__ void tile_halo_trace(const R* __restrict__ src, int lfo, const R* l1d,
+                                                const R* lend, R* dst) {
+  constexpr int N1 = P + 1, ND = N1 * N1 * N1, NF2 = N1 * N1;
+  R nbv[ND];
+  team_gather_any<P, true>(lfo, src, nbv);
+  const int sd = hex_face_side(lfo);
+  R v[NF2];
+#pragma unroll
+  for (int r = 0; r < NF2; ++r) {
+    R s = R(0);
+#pragma unroll
+    for (int jn = 0; jn < N1; ++jn) s += lend[sd * N1 + jn] * nbv[r * N1 + jn];
+    v[r] = s;
+  }
+  team_interp<P, 1>(v, l1d, dst);
+}
+
+// One normal axis AX: traces, face evaluations, lifting.
+template <int P, typename R, int AX>
+__device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restrict__ u,
+                                          long long NDa, const HexTile& T, R* sT, R* sH,
+                                          const unsigned char (*perm)[(P + 2) * (P + 2)],
+                                          const unsigned char (*fab)[(P + 2) * (P + 2)],
+                                          const HexOps<R>& H, int k, int el, bool act,
+                                          const R (&uu)[(P + 1) * (P + 1) * (P + 1)],
+                                          R (&acc)[(P + 1) * (P + 1) * (P + 1)], R& lmax) {
+  using S = TileSize<P>;
+  constexpr int NQF = S::NQF, NEQ = S::NEQ, NF2 = S::NF2, NT = S::NT;
+  constexpr int LF0 = hex_axis_face(AX, 0), LF1 = hex_axis_face(AX, 1);
+  const int tid = threadIdx.x;
+  // 1. own traces (every face side of the tile has exactly one evaluation,
+  // so every stored trace is read once and overwritten by its flux)
+  if (act) {
+    R v[NF2];
+    team_contract<P, LF0>(uu, H.lend, v);
+    team_interp<P, 1>(v, H.l1d, sT + ((el * 2 + 0) * NEQ + k) * NQF);
+    team_contract<P, LF1>(uu, H.lend, v);
+    team_interp<P, 1>(v, H.l1d, sT + ((el * 2 + 1) * NEQ + k) * NQF);
+  }
+  // halo traces, one (halo, variable) per thread
+  const int nh = T.nh[AX];
+  for (int j = tid; j < nh * NEQ; j += NT) {
+    const int h = j / NEQ, kk = j - h * NEQ;
+    tile_halo_trace<P, R>(u + kk * NDa + (long long)T.hel[AX][h] * S::ND, T.hlf[AX][h], H.l1d,
+                          H.lend, sH + (h * NEQ + kk) * NQF);
+  }
+  __syncthreads();
+  // 2. face evaluations, point by point over the CTA
+  const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+  const int nev = T.nev[AX];
+#pragma unroll 1
+  for (int pt = tid; pt < nev * NQF; pt += NT) {
+    const int j = pt / NQF, q = pt - j * NQF;
+    const unsigned d = T.ev[AX][j];
+    const int ia = d & 63, ib = (d >> 7) & 63;
+    const bool ha = (d >> 6) & 1, hb = (d >> 13) & 1, bnd = (d >> 14) & 1;
+    const int lfa = (d >> 15) & 7, lfb = (d >> 18) & 7, pid = (d >> 21) & 7;
+    const bool gb = (d >> 24) & 1;
+    R* TA = (ha ? sH : sT) + ia * (NEQ * NQF);
+    R* TB = (hb ? sH : sT) + ib * (NEQ * NQF);
+    const int ge = T.el[(gb ? ib : ia) >> 1];  // element whose face geometry is read
+    const int glf = gb ? lfb : lfa;
+    const int qa = fab[lfa][q];
+    int nb = 0;
+    if (bnd) {
+      nb = prm.fnbr[glf * prm.ne + ge];
+      if (nb == -1) {  // no boundary integrator on this face: no face term
+#pragma unroll
+        for (int kk = 0; kk < NEQ; ++kk) TA[kk * NQF + qa] = R(0);
+        continue;
+      }
+    }
+    const R* fg = (const R*)prm.fgeo + (long long)(glf * 4) * prm.ne + ge;
+    R n[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) n[c] = __ldg(fg + (long long)c * prm.ne);
+    const R jac = __ldg(fg + 3LL * prm.ne);
+    R s1[NEQ], s2[NEQ];
+#pragma unroll
+    for (int kk = 0; kk < NEQ; ++kk) s1[kk] = TA[kk * NQF + qa];
+    int qb = 0;
+    if (bnd) {
+      const BCSlot& bc = prm.bc[-2 - nb];
+      right_state<3>(bc.type, bc.state, s1, s2, n, gamma, cov, (R)prm.rgas);
+    } else {
+      qb = fab[lfb][perm[pid][q]];
+#pragma unroll
+      for (int kk = 0; kk < NEQ; ++kk) s2[kk] = TB[kk * NQF + qb];
+    }
+    R F[NEQ];
+    const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), ge);
+    lmax = fmax(lmax, sp);
+    const R w = H.wf[q] * jac;
+    if (!ha) {
+#pragma unroll
+      for (int kk = 0; kk < NEQ; ++kk) TA[kk * NQF + qa] = -w * F[kk];
+    }
+    if (!bnd && !hb) {
+#pragma unroll
+      for (int kk = 0; kk < NEQ; ++kk) TB[kk * NQF + qb] = w * F[kk];
+    }
+  }
+  __syncthreads();
+  // 3. lifting of this axis's two faces
+  if (act && !prm.faces_only) {
+    team_lift<P, LF0, 1>(sT + ((el * 2 + 0) * NEQ + k) * NQF, H.l1d, H.lend, acc);
+    team_lift<P, LF1, 1>(sT + ((el * 2 + 1) * NEQ + k) * NQF, H.l1d, H.lend, acc);
+  }
+}
+
+// Volume term of variable K for one element: the nodal Euler flux of all
+// variables at every node (FE_Evolution::GetFlux), its contravariant
+// components of variable K, and the collocated derivative operator applied in
+// scatter form: node m = (mx, my, mz) adds w_my w_mz d1[jx][mx] G_x(m) to
+// (jx, my, mz), and likewise along y and z, so no nodal array is kept.
+template <int P, int K, typename R>
+__device__ __forceinline__ void tile_volume(const R* sUe, int vstride, const R (&adj)[3][3],
+                                            const HexOps<R>& H, R gamma, R cov,
+                                            R (&acc)[(P + 1) * (P + 1) * (P + 1)], R& lmax) {
+  constexpr int N1 = P + 1, NEQ = 5;
+  const R* tD1 = H.d1;
+  const R* tW1 = H.w1;
+#pragma unroll
+  for (int mz = 0; mz < N1; ++mz)
+#pragma unroll
+    for (int my = 0; my < N1; ++my)
+#pragma unroll
+      for (int mx = 0; mx < N1; ++mx) {
+        const int m = mx + N1 * (my + N1 * mz);
+        R st[NEQ];
+#pragma unroll
+        for (int kk = 0; kk < NEQ; ++kk) st[kk] = sUe[kk * vstride + m];
+        R F[NEQ][3];
+        const R sp = flux_and_speed<3>(st, F, gamma, cov);
+        if (K == 0) lmax = fmax(lmax, sp);
+        R g[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) g[r] = adj[r][0] * F[K][0] + adj[r][1] * F[K][1] + adj[r][2] * F[K][2];
+        const R gx = tW1[my] * tW1[mz] * g[0];
+        const R gy = tW1[mx] * tW1[mz] * g[1];
+        const R gz = tW1[mx] * tW1[my] * g[2];
+#pragma unroll
+        for (int j = 0; j < N1; ++j) {
+          acc[j + N1 * (my + N1 * mz)] += tD1[j * N1 + mx] * gx;
+          acc[mx + N1 * (j + N1 * mz)] += tD1[j * N1 + my] * gy;
+          acc[mx + N1 * (my + N1 * j)] += tD1[j * N1 + mz] * gz;
+        }
+      }
+}
+
+template <int P, typename R>
+__global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_ctas<R>())
+    k_rhs_hex_tile(const __grid_constant__ RhsParams prm, const R* __restrict__ u,
+                   const EpiParams<R> ep) {
+  using S = TileSize<P>;
+  constexpr int N1 = S::N1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, E = S::E, NT = S::NT;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ HexTile sTile;
+  __shared__ unsigned char sPerm[RKDG_HEX_MAX_PERM][NQF];
+  __shared__ unsigned char sFab[6][NQF];
+  R* sm = reinterpret_cast<R*>(smraw);
+  R* sU = sm;              // [NEQ][E][ND]; the right-hand side after the volume phase
+  R* sT = sm + S::OFF_T;   // [E][2][NEQ][NQF]
+  R* sH = sm + S::OFF_H;   // [HM][NEQ][NQF]
+  const HexOps<R>& H = hex_ops<R>(prm.hops);
+  const RefTables* RT = prm.tab;
+  const int tid = threadIdx.x;
+  const int ne = prm.ne;
+  {
+    const int* src = reinterpret_cast<const int*>(prm.htile + blockIdx.x);
+    for (int t = tid; t < (int)(sizeof(HexTile) / 4); t += NT) reinterpret_cast<int*>(&sTile)[t] = src[t];
+  }
+  for (int t = tid; t < min(RT->nperm, RKDG_HEX_MAX_PERM) * NQF; t += NT)
+    sPerm[t / NQF][t % NQF] = (unsigned char)RT->perm[t / NQF][t % NQF];
+  for (int t = tid; t < 6 * NQF; t += NT) sFab[t / NQF][t % NQF] = (unsigned char)RT->fab[t / NQF][t % NQF];
+  __syncthreads();
+  const int nel = sTile.nel;
+  const long long NDa = prm.ndofs;
+  // stage the tile's DOFs: runs of ND contiguous values per (variable, element)
+  for (int f = tid; f < NEQ * E * ND; f += NT) {
+    const int k = f / (E * ND), r = f - k * (E * ND), el = r / ND, i = r - el * ND;
+    sU[f] = el < nel ? u[k * NDa + (long long)sTile.el[el] * ND + i] : R(0);
+  }
+  __syncthreads();
+  const int k = tid / E, el = tid - k * E;  // one variable per warp (E = 32)
+  const bool act = el < nel;
+  const int e = act ? sTile.el[el] : 0;
+  R uu[ND], acc[ND];
+#pragma unroll
+  for (int i = 0; i < ND; ++i) {
+    uu[i] = sU[(k * E + el) * ND + i];
+    acc[i] = R(0);
+  }
+  R lmax = R(0);
+  tile_axis<P, R, 0>(prm, u, NDa, sTile, sT, sH, sPerm, sFab, H, k, el, act, uu, acc, lmax);
+  tile_axis<P, R, 1>(prm, u, NDa, sTile, sT, sH, sPerm, sFab, H, k, el, act, uu, acc, lmax);
+  tile_axis<P, R, 2>(prm, u, NDa, sTile, sT, sH, sPerm, sFab, H, k, el, act, uu, acc, lmax);
+  if (prm.faces_only) {
+    block_max_commit<R>(lmax, prm.mcs);
+    return;
+  }
+  R g[ND];
+  if (act) {
+    const R* eg = (const R*)prm.egeo;
+    R adj[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) adj[r][d] = eg[(long long)(r * 3 + d) * ne + e];
+    const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+    const R* sUe = sU + el * ND;
+    switch (k) {  // warp-uniform
+      case 0: tile_volume<P, 0, R>(sUe, E * ND, adj, H, gamma, cov, acc, lmax); break;
+      case 1: tile_volume<P, 1, R>(sUe, E * ND, adj, H, gamma, cov, acc, lmax); break;
+      case 2: tile_volume<P, 2, R>(sUe, E * ND, adj, H, gamma, cov, acc, lmax); break;
+      case 3: tile_volume<P, 3, R>(sUe, E * ND, adj, H, gamma, cov, acc, lmax); break;
+      default: tile_volume<P, 4, R>(sUe, E * ND, adj, H, gamma, cov, acc, lmax); break;
+    }
+    if (prm.ncidx) {  // hanging faces of a nonconforming mesh
+      const int ix = prm.ncidx[e];
+      if (ix >= 0) {
+        const R* xf = (const R*)prm.xface + ((long long)ix * NEQ + k) * ND;
+#pragma unroll
+        for (int i = 0; i < ND; ++i) acc[i] += xf[i];
+      }
+    }
+    // inverse mass: x, y, z sweeps, then 1 / det J
+    const R* tMinv = H.minv1;
+#pragma unroll
+    for (int jz = 0; jz < N1; ++jz)
+#pragma unroll
+      for (int jy = 0; jy < N1; ++jy)
+#pragma unroll
+        for (int jx = 0; jx < N1; ++jx) {
+          R s = R(0);
+#pragma unroll
+          for (int m = 0; m < N1; ++m) s += tMinv[jx * N1 + m] * acc[m + N1 * (jy + N1 * jz)];
+          g[jx + N1 * (jy + N1 * jz)] = s;
+        }
+#pragma unroll
+    for (int jz = 0; jz < N1; ++jz)
+#pragma unroll
+      for (int jy = 0; jy < N1; ++jy)
+#pragma unroll
+        for (int jx = 0; jx < N1; ++jx) {
+          R s = R(0);
+#pragma unroll
+          for (int m = 0; m < N1; ++m) s += tMinv[jy * N1 + m] * g[jx + N1 * (m + N1 * jz)];
+          acc[jx + N1 * (jy + N1 * jz)] = s;
+        }
+    const R idet = eg[(long long)9 * ne + e];
+#pragma unroll
+    for (int jz = 0; jz < N1; ++jz)
+#pragma unroll
+      for (int jy = 0; jy < N1; ++jy)
+#pragma unroll
+        for (int jx = 0; jx < N1; ++jx) {
+          R s = R(0);
+#pragma unroll
+          for (int m = 0; m < N1; ++m) s += tMinv[jz * N1 + m] * acc[jx + N1 * (jy + N1 * m)];
+          g[jx + N1 * (jy + N1 * jz)] = s * idet;
+        }
+  }
+  __syncthreads();  // every thread has read the staged DOFs
+  if (act) {
+#pragma unroll
+    for (int i = 0; i < ND; ++i) sU[(k * E + el) * ND + i] = g[i];
+  }
+  __syncthreads();
+  // Runge-Kutta epilogue over the tile, coalesced within each element's run
+  const bool need_means = ep.mode == 1 && ep.means;
+  R* sLo = sT;  // low parts of the combined state when the limiter needs means
+  const int total = NEQ * nel * ND;
+  if (ep.mode == 1 && !need_means) {
+    constexpr int CH = 8;
+    for (int c0 = tid; c0 < total; c0 += CH * NT) {
+      long long idx[CH];
+      R y[CH], bh[CH], bl[CH], kp[3][CH];
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        const int g = c0 + c * NT;
+        const int gg = g < total ? g : c0;
+        const int kk = gg / (nel * ND), t = gg - kk * (nel * ND);
+        idx[c] = kk * NDa + (long long)sTile.el[t / ND] * ND + t % ND;
+        y[c] = sU[(kk * E + t / ND) * ND + t % ND];
+        if constexpr (std::is_same<R, double>::value) {
+          bh[c] = ep.base ? ep.base[idx[c]] : R(0);
+          bl[c] = R(0);
+        } else {
+          bh[c] = ep.basehi[idx[c]];
+          bl[c] = ep.baselo[idx[c]];
+        }
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj)
+          if (jj < ep.nprev) kp[jj][c] = ep.kprev[jj][idx[c]];
+      }
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        if (c0 + c * NT >= total) break;
+        if constexpr (std::is_same<R, double>::value) {
+          double v = bh[c];
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj)
+            if (jj < ep.nprev) v += ep.cprev[jj] * kp[jj][c];
+          v += ep.ccur * y[c];
+          if (ep.kout) ep.kout[idx[c]] = y[c];
+          if (ep.out64) ep.out64[idx[c]] = v;
+          if (ep.out32) ep.out32[idx[c]] = (float)v;
+        } else if (!ep.final_stage) {
+          float inc = bl[c];
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj)
+            if (jj < ep.nprev) inc = fmaf(ep.cprev_hi[jj], kp[jj][c], inc);
+          inc = fmaf(ep.ccur_hi, y[c], inc);
+          if (ep.kout) ep.kout[idx[c]] = y[c];
+          ep.out32[idx[c]] = bh[c] + inc;
+        } else {
+          float sh = 0.0f, sl = 0.0f, ph, pl;
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj)
+            if (jj < ep.nprev) {
+              ds_mul_f(ep.cprev_hi[jj], ep.cprev_lo[jj], kp[jj][c], ph, pl);
+              ds_add(sh, sl, ph, pl);
+            }
+          ds_mul_f(ep.ccur_hi, ep.ccur_lo, y[c], ph, pl);
+          ds_add(sh, sl, ph, pl);
+          float h = bh[c], l = bl[c];
+          ds_add(h, l, sh, sl);
+          ep.out32[idx[c]] = h;
+          ep.outlo[idx[c]] = l;
+        }
+      }
+    }
+  } else {
+    for (int f = tid; f < total; f += NT) {
+      const int kk = f / (nel * ND), t = f - kk * (nel * ND);
+      const int s = (kk * E + t / ND) * ND + t % ND;
+      R hi, lo;
+      epi_value2<R>(ep, kk * NDa + (long long)sTile.el[t / ND] * ND + t % ND, sU[s], hi, lo);
+      if (need_means) {
+        sU[s] = hi;
+        sLo[s] = lo;
+      }
+    }
+    if (need_means) {
+      __syncthreads();
+      // cell means of the combined state, one (element, variable) per thread
+      for (int t = tid; t < nel * NEQ; t += NT) {
+        const int kk = t / nel, s = t - kk * nel;
+        double m = 0.0;
+        for (int i = 0; i < ND; ++i)
+          m += RT->wmean[i] * ((double)sU[(kk * E + s) * ND + i] + (double)sLo[(kk * E + s) * ND + i]);
+        ep.means[(long long)kk * ne + sTile.el[s]] = m;
+      }
+    }
+  }
+  block_max_commit<R>(lmax, prm.mcs);
+}
+
+}  // namespace rkdg

@@ -38,16 +38,9 @@ uint32_t spread10(uint32_t v) {  // bits 0..9 -> every third bit
   return v;
 }
 
-}  // namespace
-
-bool build_hex_sched(int ne, int nvpe, const double* coords, const std::vector<int>& fnbr,
-                     const std::vector<int>& fcode, std::vector<HexTeamSched>& out,
-                     int* max_rounds) {
-  constexpr int NS = RKDG_TEAM_SLOTS, NR = RKDG_TEAM_MAX_ROUNDS, NONE = 0xFF;
-  out.clear();
-  if (max_rounds) *max_rounds = 0;
-  if (ne <= 0) return true;
-  // ---- Morton order of the element centres ----
+// Elements sorted by the Morton key of their centres (10 bits per axis over
+// the bounding box of the corners); ties keep element order.
+std::vector<std::pair<uint32_t, int>> morton_order(int ne, int nvpe, const double* coords) {
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
   for (long long i = 0; i < (long long)ne * nvpe; ++i)
     for (int d = 0; d < 3; ++d) {
@@ -69,6 +62,19 @@ bool build_hex_sched(int ne, int nvpe, const double* coords, const std::vector<i
     key[e] = {k, e};
   }
   std::sort(key.begin(), key.end());
+  return key;
+}
+
+}  // namespace
+
+bool build_hex_sched(int ne, int nvpe, const double* coords, const std::vector<int>& fnbr,
+                     const std::vector<int>& fcode, std::vector<HexTeamSched>& out,
+                     int* max_rounds) {
+  constexpr int NS = RKDG_TEAM_SLOTS, NR = RKDG_TEAM_MAX_ROUNDS, NONE = 0xFF;
+  out.clear();
+  if (max_rounds) *max_rounds = 0;
+  if (ne <= 0) return true;
+  const std::vector<std::pair<uint32_t, int>> key = morton_order(ne, nvpe, coords);
   const int ncta = (ne + NS - 1) / NS;
   std::vector<int> grp(ne), slot(ne);
   for (int i = 0; i < ne; ++i) {
@@ -200,6 +206,62 @@ bool build_hex_sched(int ne, int nvpe, const double* coords, const std::vector<i
     }
   }
   if (max_rounds) *max_rounds = nr_max;
+  return true;
+}
+
+bool build_hex_tiles(int ne, int nvpe, const double* coords, const std::vector<int>& fnbr,
+                     const std::vector<int>& fcode, std::vector<HexTile>& out) {
+  constexpr int TE = RKDG_TILE_E, HM = RKDG_TILE_HMAX;
+  out.clear();
+  if (ne <= 0) return true;
+  const std::vector<std::pair<uint32_t, int>> key = morton_order(ne, nvpe, coords);
+  const int ntile = (ne + TE - 1) / TE;
+  std::vector<int> tile(ne), slot(ne);
+  for (int i = 0; i < ne; ++i) {
+    tile[key[i].second] = i / TE;
+    slot[key[i].second] = i % TE;
+  }
+  // local faces of each normal axis, by side (MFEM hexahedron numbering)
+  const int axface[3][2] = {{4, 2}, {1, 3}, {0, 5}};
+  out.resize(ntile);
+  for (int b = 0; b < ntile; ++b) {
+    HexTile& T = out[b];
+    std::memset(&T, 0, sizeof T);
+    T.nel = std::min(TE, ne - b * TE);
+    for (int s = 0; s < TE; ++s) T.el[s] = s < T.nel ? key[(size_t)b * TE + s].second : -1;
+    for (int a = 0; a < 3; ++a) {
+      int nev = 0, nh = 0;
+      for (int s = 0; s < T.nel; ++s)
+        for (int sd = 0; sd < 2; ++sd) {
+          const int lf = axface[a][sd], e = T.el[s];
+          const unsigned fs = 2u * s + sd;
+          const int nb = fnbr[(size_t)lf * ne + e];
+          const int code = fcode[(size_t)lf * ne + e];
+          const unsigned lfo = code & 7, elem2 = (code >> 3) & 1, pid = (code >> 4) & 7;
+          if (nb < 0) {  // boundary (condition looked up at launch) or hanging face
+            T.ev[a][nev++] = fs | 1u << 14 | (unsigned)lf << 15;
+            continue;
+          }
+          if (tile[nb] == b && face_axis((int)lfo) == a) {
+            if (elem2) continue;  // evaluated from the partner's (Elem1) entry
+            const unsigned fo = 2u * slot[nb] + (lfo == (unsigned)axface[a][1] ? 1u : 0u);
+            T.ev[a][nev++] = fs | fo << 7 | (unsigned)lf << 15 | lfo << 18 | pid << 21;
+            continue;
+          }
+          if (nh >= HM) return false;
+          T.hel[a][nh] = nb;
+          T.hlf[a][nh] = (unsigned char)lfo;
+          const unsigned h = (unsigned)nh++;
+          if (!elem2)
+            T.ev[a][nev++] = fs | h << 7 | 1u << 13 | (unsigned)lf << 15 | lfo << 18 | pid << 21;
+          else
+            T.ev[a][nev++] = h | 1u << 6 | fs << 7 | lfo << 15 | (unsigned)lf << 18 | pid << 21 |
+                             1u << 24;
+        }
+      T.nev[a] = nev;
+      T.nh[a] = nh;
+    }
+  }
   return true;
 }
 

@@ -18,4 +18,13 @@ bool build_hex_sched(int ne, int nvpe, const double* coords, const std::vector<i
                      const std::vector<int>& fcode, std::vector<HexTeamSched>& out,
                      int* max_rounds);
 
+// Tiles of the face-once hexahedral kernel (HexTile): runs of RKDG_TILE_E
+// elements of the same Morton order, with their per-axis face evaluations and
+// halo lists.  fnbr: topological neighbour (>= 0) or < 0 for a face without
+// an element across (boundary or hanging); fcode as the device table.
+// A tile axis has at most 2 * RKDG_TILE_E face sides, so the halo lists always
+// fit (RKDG_TILE_HMAX); returns false only on inconsistent face tables.
+bool build_hex_tiles(int ne, int nvpe, const double* coords, const std::vector<int>& fnbr,
+                     const std::vector<int>& fcode, std::vector<HexTile>& out);
+
 }  // namespace rkdg

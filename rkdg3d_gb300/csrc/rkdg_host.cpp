@@ -27,6 +27,7 @@
 using rkdg::BCSlot;
 using rkdg::EpiParams;
 using rkdg::HexTeamSched;
+using rkdg::HexTile;
 using rkdg::LimParams;
 using rkdg::RefTables;
 using rkdg::RhsParams;
@@ -53,6 +54,8 @@ struct rkdg_ctx {
   size_t fslot_n = 0;
   HexTeamSched* d_hsched = nullptr;  // per-CTA schedules of the shared-face hexahedral kernel
   int hsched_rounds = 0;
+  HexTile* d_htile = nullptr;  // tiles of the face-once hexahedral kernel
+  int ntile = 0;
   // hanging faces of a nonconforming mesh (see rkdg_nc.cu)
   int nnc = 0, nc_nel = 0;
   // non-parallelogram quadrilaterals: per-node adj(J) and 1/det J
@@ -197,6 +200,8 @@ void free_mesh(rkdg_ctx* c) {
   c->fslot_n = 0;
   dfree(c->d_hsched);
   c->hsched_rounds = 0;
+  dfree(c->d_htile);
+  c->ntile = 0;
   dfree(c->d_nc_face);
   dfree(c->d_nc_bnc);
   dfree(c->d_nc_flux);
@@ -302,6 +307,8 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   P.block = c->gen_block;
   P.fslot = c->d_fslot;
   P.hsched = c->d_hsched;
+  P.htile = c->d_htile;
+  P.ntile = c->ntile;
   P.ncidx = c->nnc ? c->d_ncidx : nullptr;
   P.xface = c->d_xface;
   P.ngeo = c->nonaffine ? (prec == 0 ? (const void*)c->d_ngeo64 : (const void*)c->d_ngeo32) : nullptr;
@@ -804,7 +811,7 @@ int rkdg_set_solver_quirks(rkdg_ctx* c, int flags) {
 
 int rkdg_set_tuning(rkdg_ctx* c, int key, int value) {
   if (!c) return RKDG_ERR_INVALID;
-  if (key == RKDG_TUNE_HEX_KERNEL && value >= 0 && value <= 4) {
+  if (key == RKDG_TUNE_HEX_KERNEL && value >= 0 && value <= 5) {
     if (value == 3 && c->has_mesh) {
       const int st = ensure_fslot(c);
       if (st) return st;
@@ -1246,6 +1253,12 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
       CUDA_TRY(c, dalloc(c->d_hsched, hs.size()));
       CUDA_TRY(c, cudaMemcpy(c->d_hsched, hs.data(), hs.size() * sizeof(HexTeamSched),
                              cudaMemcpyHostToDevice));
+    }
+    std::vector<HexTile> ht;
+    if (rkdg::build_hex_tiles(ne, nvpe, m->elem_coords, c->h_fnbr, c->h_fcode, ht)) {
+      CUDA_TRY(c, dalloc(c->d_htile, ht.size()));
+      CUDA_TRY(c, cudaMemcpy(c->d_htile, ht.data(), ht.size() * sizeof(HexTile), cudaMemcpyHostToDevice));
+      c->ntile = (int)ht.size();
     }
   }
   c->has_mesh = true;
@@ -1934,7 +1947,8 @@ int rkdg_autotune(rkdg_ctx* c, const double* x, int* hex_kernel, int* generic_bl
     if ((st = ensure_fslot(c))) return st;
     int best = 0;
     float tbest = 0.0f;
-    for (int v = 1; v <= (c->d_hsched ? 4 : 3); ++v) {
+    for (int v = 1; v <= 5; ++v) {
+      if ((v == 4 && !c->d_hsched) || (v == 5 && !c->d_htile)) continue;
       c->hex_variant = v;
       float ms = 0.0f;
       if ((st = time_rhs(&ms))) return st;

@@ -124,12 +124,13 @@ def test_rhs_walls(cuda, geom, order, n, bc, rs, avg):
     assert abs(m - m_ref) <= 1e-13 * abs(m_ref)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("walled", [False, True])
 def test_rhs_hex_kernel_variants(cuda, variant, order, walled):
     """The hexahedral kernels (warp per element, five-lane team, face pass +
-    element pass, team kernel with shared-face rounds) in FP64."""
+    element pass, team kernel with shared-face rounds, face-once tiles) in
+    FP64."""
     from rkdg3d_gb300.solver import TUNE_HEX_KERNEL
     case = (walled_case(M.GEOM_CUBE, 3, order, RS_HLLC, AVG_EINFELDT, bc=BC_SLIP) if walled
             else periodic_case(M.GEOM_CUBE, 3, order, RS_LLF))
@@ -147,15 +148,18 @@ def test_rhs_hex_kernel_variants(cuda, variant, order, walled):
     assert rel_l1(xd.cpu().numpy(), xs_ref) < RHS_TOL
 
 
+@pytest.mark.parametrize("variant", [4, 5])
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("order,n,bc", [(2, 8, None), (2, 3, None), (2, 8, BC_SLIP),
-                                        (1, 16, BC_FIXED_PRESSURE_OUTLET)])
-def test_rhs_hex_shared_faces(cuda, prec, order, n, bc):
-    """Shared-face rounds on meshes of several CTAs (faces inside a CTA
-    evaluated once, the others through neighbour traces from global memory;
-    3^3 periodic: rings of three elements inside a CTA need a seventh round
-    that mixes face axes): right-hand side, face-only speed and one step
-    against the oracle.  Dyadic spacings: with the reference's rotation
+                                        (1, 16, BC_FIXED_PRESSURE_OUTLET), (2, 12, None),
+                                        (1, 10, BC_SLIP)])
+def test_rhs_hex_shared_faces(cuda, variant, prec, order, n, bc):
+    """Kernels that evaluate a face inside a CTA once, on meshes of several
+    CTAs: shared-face rounds (4) and face-once tiles (5); the other faces
+    through neighbour traces from global memory (3^3 periodic: rings of three
+    elements inside a CTA need a seventh round that mixes face axes; 12^3 and
+    10^3: Morton groups that are not aligned blocks): right-hand side,
+    face-only speed and one step against the oracle.  Dyadic spacings: with the reference's rotation
     (cos psi = sqrt(1 - n_z^2), quirk Q14) a unit normal one ulp off +-z
     changes the flux by ~1e-8, and the oracle forms normals per point as
     MFEM does where the library forms one per face."""
@@ -167,7 +171,7 @@ def test_rhs_hex_shared_faces(cuda, prec, order, n, bc):
     ctx, orc = pair(case)
     if prec:
         ctx.set_precision(1)
-    ctx.set_tuning(TUNE_HEX_KERNEL, 4)
+    ctx.set_tuning(TUNE_HEX_KERNEL, variant)
     tol = RHS_TOL if prec == 0 else 1e-5
     x = random_state(ctx.node_coords(), seed=23)
     y_ref, m_ref = orc.rhs(x)
@@ -180,6 +184,35 @@ def test_rhs_hex_shared_faces(cuda, prec, order, n, bc):
     xd = dev(x)
     ctx.step(xd, 1e-3)
     assert rel_l1(xd.cpu().numpy(), xs_ref) < tol
+
+
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("order", [1, 2])
+def test_rhs_hex_rotated_elements(cuda, variant, order):
+    """Elements in shuffled order, each with its local numbering rotated by
+    one of the cube's 24 rotations: faces join local faces of different axes
+    and point permutations of every kind (slip walls on the bounded axis)."""
+    from rkdg3d_gb300.solver import TUNE_HEX_KERNEL
+    from tests.test_hex_schedule import cube_rotations
+    rng = np.random.default_rng(7)
+    m = M.hex_grid(6, 5, 7, periodic=(True, False, True))
+    order_ = rng.permutation(m.num_elements)
+    pick = cube_rotations()[rng.integers(0, 24, m.num_elements)]
+    m = M.Mesh(3, M.GEOM_CUBE, np.take_along_axis(m.elem_vertices[order_], pick, 1).astype(np.int32),
+               np.take_along_axis(m.elem_coords[order_], pick[:, :, None], 1), m.bdr_vertices, m.bdr_attr)
+    case = cases.Case("rotated", m, order, RS_HLLC, AVG_TRRS, bcs=[(2, BC_SLIP, None), (4, BC_SLIP, None)])
+    ctx, orc = pair(case)
+    ctx.set_tuning(TUNE_HEX_KERNEL, variant)
+    x = random_state(ctx.node_coords(), seed=31, amp=0.05, vel=0.2)
+    y_ref, m_ref = orc.rhs(x)
+    y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
+    m_ = ctx.rhs(dev(x), y)
+    assert rel_l1(y.cpu().numpy(), y_ref) < RHS_TOL
+    assert abs(m_ - m_ref) <= 1e-13 * m_ref
+    xs_ref, _ = orc.step(x, 1e-3)
+    xd = dev(x)
+    ctx.step(xd, 1e-3)
+    assert rel_l1(xd.cpu().numpy(), xs_ref) < RHS_TOL
 
 
 def test_node_coords_match_oracle(cuda):
@@ -301,7 +334,7 @@ def test_autotune_keeps_parity(cuda, geom, order):
     ctx.rhs(dev(x), before_y)
     choice = ctx.autotune(dev(x))
     if geom == M.GEOM_CUBE:
-        assert choice["hex_kernel"] in (1, 2, 3, 4)
+        assert choice["hex_kernel"] in (1, 2, 3, 4, 5)
     else:
         assert choice["generic_block"] in (64, 128, 256)
         assert choice["limiter_block"] in (64, 128, 256)
@@ -378,7 +411,8 @@ def test_shu_with_multi_is_rejected(cuda):
 @pytest.mark.parametrize("geom,order,prec,variant", [(M.GEOM_SQUARE, 1, 0, 0), (M.GEOM_TRIANGLE, 2, 1, 0),
                                                      (M.GEOM_CUBE, 2, 1, 0), (M.GEOM_CUBE, 2, 0, 0),
                                                      (M.GEOM_CUBE, 1, 0, 0), (M.GEOM_CUBE, 1, 1, 2),
-                                                     (M.GEOM_CUBE, 2, 1, 4), (M.GEOM_CUBE, 1, 0, 4)])
+                                                     (M.GEOM_CUBE, 2, 1, 4), (M.GEOM_CUBE, 1, 0, 4),
+                                                     (M.GEOM_CUBE, 2, 1, 5), (M.GEOM_CUBE, 2, 0, 5)])
 def test_nonphysical_state_is_reported(cuda, geom, order, prec, variant):
     """Where the reference prints the elements and exits on a non-physical
     state (face_integrator.cpp:214-218), every kernel path returns
@@ -447,6 +481,7 @@ def _nc_case(kind, order, rs=RS_HLLC):
 @pytest.mark.parametrize("kind,order,prec,variant", [
     ("hex", 2, 0, 0), ("hex", 2, 1, 0), ("hex", 1, 0, 0), ("hex", 1, 1, 0), ("hex", 2, 0, 1),
     ("hex", 2, 0, 2), ("hex", 1, 0, 3), ("hex", 2, 1, 4), ("hexwall", 2, 0, 0), ("hexwall", 1, 1, 0),
+    ("hex", 2, 0, 5), ("hex", 2, 1, 5), ("hex", 1, 0, 5), ("hexwall", 2, 0, 5),
     ("quad", 2, 0, 0), ("quad", 3, 0, 0), ("quad", 1, 1, 0), ("tri", 1, 0, 0), ("tri", 2, 0, 0),
     ("tri", 2, 1, 0)])
 def test_rhs_nonconforming(cuda, kind, order, prec, variant):
