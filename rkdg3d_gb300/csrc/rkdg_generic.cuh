@@ -561,18 +561,22 @@ __device__ __forceinline__ void shu_indicator(const LimParams& prm, const R* __r
 // LimiterFinDiff::limit (limiter_findiff.cpp:3-33, last equation only, Q6).
 // The update reads only this element's values and the cell means, so it is
 // done in place.  DS = true: the values are a float pair (u = hi, ulo = lo)
-// and the multiplier update runs in double-single arithmetic.
+// and the multiplier update runs in double-single arithmetic.  The indicator
+// (face-point values, stencil min/max, the +-1e-3 switches and the limiter
+// function) is evaluated in FP64 for every state type, from the float state
+// (and its low word) where the state is FP32, so that the FP32-bulk path takes
+// the reference's FP64 branch decisions on the values it holds.
 template <int G, int P, typename R, bool DS>
 __global__ void __launch_bounds__(kGenericMaxBlock)
     k_limit_generic(const LimParams prm, R* __restrict__ u, float* __restrict__ ulo) {
   using E = El<G, P>;
   constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NFPE = E::NFPE, NQL = E::NQL, NV = E::NV;
-  __shared__ R sBl[NFPE][NQL][ND];
+  __shared__ double sBl[NFPE][NQL][ND];
   __shared__ R sBv[NV][ND];
   const RefTables* T = prm.tab;
   for (int t = threadIdx.x; t < NFPE * NQL * ND; t += blockDim.x) {
     const int s = t % ND, q = (t / ND) % NQL, lf = t / (ND * NQL);
-    sBl[lf][q][s] = (R)T->Bl[lf][q][s];
+    sBl[lf][q][s] = T->Bl[lf][q][s];
   }
   for (int t = threadIdx.x; t < NV * ND; t += blockDim.x) sBv[t / ND][t % ND] = (R)T->Bv[t / ND][t % ND];
   __syncthreads();
@@ -605,33 +609,37 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
     umh[k] = (float)m;
     uml[k] = (float)(m - (double)umh[k]);
   }
-  R minValue;
-  R elind[NEQ];
+  double minValue;
+  double elind[NEQ];
   if (prm.indicator == 0) {
-    minValue = R(1);
+    minValue = 1.0;
 #pragma unroll
-    for (int k = 0; k < NEQ; ++k) elind[k] = R(1);
+    for (int k = 0; k < NEQ; ++k) elind[k] = 1.0;
   } else if (prm.indicator == 1) {
-    minValue = R(0);
+    minValue = 0.0;
 #pragma unroll
-    for (int k = 0; k < NEQ; ++k) elind[k] = R(0);
+    for (int k = 0; k < NEQ; ++k) elind[k] = 0.0;
   } else if (prm.indicator == 3) {
-    shu_indicator<G, P, DS>(prm, u, ulo, e, elind);
-    minValue = R(1);  // FinDiff only: the Multi limiter is rejected with Shu
+    R sv[NEQ];
+    shu_indicator<G, P, DS>(prm, u, ulo, e, sv);
+#pragma unroll
+    for (int k = 0; k < NEQ; ++k) elind[k] = (double)sv[k];
+    minValue = 1.0;  // FinDiff only: the Multi limiter is rejected with Shu
   } else {
-    R mI[NEQ], MI[NEQ], yMin[NEQ];
+    double mI[NEQ], MI[NEQ], yMin[NEQ], umd[NEQ];
 #pragma unroll
     for (int k = 0; k < NEQ; ++k) {
-      mI[k] = um[k] < R(1e9) ? um[k] : R(1e9);
-      MI[k] = um[k] > R(-1e9) ? um[k] : R(-1e9);
-      yMin[k] = R(1e9);
+      umd[k] = prm.means[(long long)k * ne + e];
+      mI[k] = umd[k] < 1e9 ? umd[k] : 1e9;
+      MI[k] = umd[k] > -1e9 ? umd[k] : -1e9;
+      yMin[k] = 1e9;
     }
     for (int lf = 0; lf < NFPE; ++lf) {
       const int nb = prm.fnbr[lf * ne + e];
       if (nb < 0) continue;
 #pragma unroll
       for (int k = 0; k < NEQ; ++k) {
-        const R v = (R)prm.means[(long long)k * ne + nb];
+        const double v = prm.means[(long long)k * ne + nb];
         mI[k] = v < mI[k] ? v : mI[k];
         MI[k] = v > MI[k] ? v : MI[k];
       }
@@ -648,7 +656,7 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
         ncfaces |= 1u << prm.nc_face[f * 4 + (side ? 3 : 1)];
 #pragma unroll
         for (int k = 0; k < NEQ; ++k) {
-          const R v = (R)prm.means[(long long)k * ne + nb];
+          const double v = prm.means[(long long)k * ne + nb];
           mI[k] = v < mI[k] ? v : mI[k];
           MI[k] = v > MI[k] ? v : MI[k];
         }
@@ -661,30 +669,30 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
       for (int q = 0; q < NQL; ++q) {
 #pragma unroll
         for (int k = 0; k < NEQ; ++k) {
-          R v = R(0);
+          double v = 0.0;
 #pragma unroll
           for (int j = 0; j < ND; ++j) {
-            v += el[k][j] * sBl[lf][q][j];
-            if constexpr (DS) v += lo[k][j] * sBl[lf][q][j];
+            v += (double)el[k][j] * sBl[lf][q][j];
+            if constexpr (DS) v += (double)lo[k][j] * sBl[lf][q][j];
           }
-          const R diff = v - um[k];
-          R y;
-          if (diff > R(1e-3))
-            y = (MI[k] - um[k]) / diff;
-          else if (diff < R(-1e-3))
-            y = (mI[k] - um[k]) / diff;
+          const double diff = v - umd[k];
+          double y;
+          if (diff > 1e-3)
+            y = (MI[k] - umd[k]) / diff;
+          else if (diff < -1e-3)
+            y = (mI[k] - umd[k]) / diff;
           else
-            y = R(1);
+            y = 1.0;
           if (prm.function == 0) {
             yMin[k] = y < yMin[k] ? y : yMin[k];
-            yMin[k] = yMin[k] > R(1) ? R(1) : yMin[k];
+            yMin[k] = yMin[k] > 1.0 ? 1.0 : yMin[k];
           } else if (prm.function == 1) {
-            const R yc = (y * y + R(2) * y) / (y * y + y + R(2));
+            const double yc = (y * y + 2.0 * y) / (y * y + y + 2.0);
             yMin[k] = yc < yMin[k] ? yc : yMin[k];
           } else {
-            const R ys = R(1.5);
-            const R yr = y / ys;
-            const R yc = y < R(1) ? y + (R(3) - R(2) * ys) * yr * yr + (ys - R(2)) * yr * yr * yr : R(1);
+            const double ys = 1.5;
+            const double yr = y / ys;
+            const double yc = y < 1.0 ? y + (3.0 - 2.0 * ys) * yr * yr + (ys - 2.0) * yr * yr * yr : 1.0;
             yMin[k] = yc < yMin[k] ? yc : yMin[k];
           }
         }
@@ -738,7 +746,7 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
             el[k][j] = (R)ph;
             lo[k][j] = pl;
           } else {
-            el[k][j] = um[k] + minValue * (el[k][j] - um[k]);
+            el[k][j] = um[k] + (R)minValue * (el[k][j] - um[k]);
           }
         }
     if (prm.last_hope) {
@@ -770,7 +778,7 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
       }
     }
   } else {
-    const bool totalInd = elind[NEQ - 1] < R(0.999);
+    const bool totalInd = elind[NEQ - 1] < 0.999;
     if (totalInd) {
 #pragma unroll
       for (int k = 0; k < NEQ; ++k)

@@ -42,10 +42,14 @@ struct TileSize {
   static constexpr int N1 = P + 1, NQ1 = P + 2, ND = N1 * N1 * N1, NQF = NQ1 * NQ1, NEQ = 5,
                        NF2 = N1 * N1;
   static constexpr int E = RKDG_TILE_E, NT = NEQ * E, HM = RKDG_TILE_HMAX;
-  // staged DOFs [NEQ][E][ND], own traces / weighted fluxes of one axis
-  // [E][2][NEQ][NQF], halo traces [HM][NEQ][NQF]
-  static constexpr int OFF_T = NEQ * E * ND, OFF_H = OFF_T + E * 2 * NEQ * NQF,
-                       TOTAL = OFF_H + HM * NEQ * NQF;
+  // staged DOFs [NEQ][E][ND]; own traces / weighted fluxes of one axis
+  // [2][NEQ][NQF][TS] (slot fastest, padded: the threads of a warp -- 32
+  // slots -- store a trace point into distinct banks, and the 16 points of
+  // one face, read by 16 threads, fall into distinct banks too); halo traces
+  // [NEQ][NQF][HS] likewise
+  static constexpr int TS = E + 1, HS = HM + 1;
+  static constexpr int OFF_T = NEQ * E * ND, OFF_H = OFF_T + 2 * NEQ * NQF * TS,
+                       TOTAL = OFF_H + NEQ * NQF * HS;
   template <typename R>
   static constexpr size_t smem_bytes() { return sizeof(R) * (size_t)TOTAL; }
   template <typename R>
@@ -59,7 +63,7 @@ __host__ __device__ constexpr int hex_axis_face(int ax, int sd) {
 
 // Trace of an out-of-tile element's variable at the points of its local face
 // lfo (tensor order), read from global memory.
-template <int P, typename R>
+template <int P, int ST, typename R>
 __device__ __forceinline__ void tile_halo_trace(const R* __restrict__ src, int lfo, const R* l1d,
                                                 const R* lend, R* dst) {
   constexpr int N1 = P + 1, ND = N1 * N1 * N1, NF2 = N1 * N1;
@@ -74,7 +78,7 @@ __device__ __forceinline__ void tile_halo_trace(const R* __restrict__ src, int l
     for (int jn = 0; jn < N1; ++jn) s += lend[sd * N1 + jn] * nbv[r * N1 + jn];
     v[r] = s;
   }
-  team_interp<P, 1>(v, l1d, dst);
+  team_interp<P, ST>(v, l1d, dst);
 }
 
 // One normal axis AX: traces, face evaluations, lifting.
@@ -87,7 +91,7 @@ __device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restr
                                           const R (&uu)[(P + 1) * (P + 1) * (P + 1)],
                                           R (&acc)[(P + 1) * (P + 1) * (P + 1)], R& lmax) {
   using S = TileSize<P>;
-  constexpr int NQF = S::NQF, NEQ = S::NEQ, NF2 = S::NF2, NT = S::NT;
+  constexpr int NQF = S::NQF, NEQ = S::NEQ, NF2 = S::NF2, NT = S::NT, TS = S::TS, HS = S::HS;
   constexpr int LF0 = hex_axis_face(AX, 0), LF1 = hex_axis_face(AX, 1);
   const int tid = threadIdx.x;
   // 1. own traces (every face side of the tile has exactly one evaluation,
@@ -95,16 +99,17 @@ __device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restr
   if (act) {
     R v[NF2];
     team_contract<P, LF0>(uu, H.lend, v);
-    team_interp<P, 1>(v, H.l1d, sT + ((el * 2 + 0) * NEQ + k) * NQF);
+    team_interp<P, TS>(v, H.l1d, sT + (0 * NEQ + k) * NQF * TS + el);
     team_contract<P, LF1>(uu, H.lend, v);
-    team_interp<P, 1>(v, H.l1d, sT + ((el * 2 + 1) * NEQ + k) * NQF);
+    team_interp<P, TS>(v, H.l1d, sT + (1 * NEQ + k) * NQF * TS + el);
   }
-  // halo traces, one (halo, variable) per thread
+  // halo traces, one (variable, halo) per thread, consecutive halos on
+  // consecutive threads
   const int nh = T.nh[AX];
   for (int j = tid; j < nh * NEQ; j += NT) {
-    const int h = j / NEQ, kk = j - h * NEQ;
-    tile_halo_trace<P, R>(u + kk * NDa + (long long)T.hel[AX][h] * S::ND, T.hlf[AX][h], H.l1d,
-                          H.lend, sH + (h * NEQ + kk) * NQF);
+    const int kk = j / nh, h = j - kk * nh;
+    tile_halo_trace<P, HS, R>(u + kk * NDa + (long long)T.hel[AX][h] * S::ND, T.hlf[AX][h], H.l1d,
+                              H.lend, sH + kk * NQF * HS + h);
   }
   __syncthreads();
   // 2. face evaluations, point by point over the CTA
@@ -118,8 +123,11 @@ __device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restr
     const bool ha = (d >> 6) & 1, hb = (d >> 13) & 1, bnd = (d >> 14) & 1;
     const int lfa = (d >> 15) & 7, lfb = (d >> 18) & 7, pid = (d >> 21) & 7;
     const bool gb = (d >> 24) & 1;
-    R* TA = (ha ? sH : sT) + ia * (NEQ * NQF);
-    R* TB = (hb ? sH : sT) + ib * (NEQ * NQF);
+    // a side's value of variable kk at tensor point t: X[kk * xk + t * xq]
+    R* TA = ha ? sH + ia : sT + (ia & 1) * (NEQ * NQF * TS) + (ia >> 1);
+    R* TB = hb ? sH + ib : sT + (ib & 1) * (NEQ * NQF * TS) + (ib >> 1);
+    const int ak = ha ? NQF * HS : NQF * TS, aq = ha ? HS : TS;
+    const int bk = hb ? NQF * HS : NQF * TS, bq = hb ? HS : TS;
     const int ge = T.el[(gb ? ib : ia) >> 1];  // element whose face geometry is read
     const int glf = gb ? lfb : lfa;
     const int qa = fab[lfa][q];
@@ -128,7 +136,7 @@ __device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restr
       nb = prm.fnbr[glf * prm.ne + ge];
       if (nb == -1) {  // no boundary integrator on this face: no face term
 #pragma unroll
-        for (int kk = 0; kk < NEQ; ++kk) TA[kk * NQF + qa] = R(0);
+        for (int kk = 0; kk < NEQ; ++kk) TA[kk * ak + qa * aq] = R(0);
         continue;
       }
     }
@@ -139,7 +147,7 @@ __device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restr
     const R jac = __ldg(fg + 3LL * prm.ne);
     R s1[NEQ], s2[NEQ];
 #pragma unroll
-    for (int kk = 0; kk < NEQ; ++kk) s1[kk] = TA[kk * NQF + qa];
+    for (int kk = 0; kk < NEQ; ++kk) s1[kk] = TA[kk * ak + qa * aq];
     int qb = 0;
     if (bnd) {
       const BCSlot& bc = prm.bc[-2 - nb];
@@ -147,7 +155,7 @@ __device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restr
     } else {
       qb = fab[lfb][perm[pid][q]];
 #pragma unroll
-      for (int kk = 0; kk < NEQ; ++kk) s2[kk] = TB[kk * NQF + qb];
+      for (int kk = 0; kk < NEQ; ++kk) s2[kk] = TB[kk * bk + qb * bq];
     }
     R F[NEQ];
     const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), ge);
@@ -155,18 +163,18 @@ __device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restr
     const R w = H.wf[q] * jac;
     if (!ha) {
 #pragma unroll
-      for (int kk = 0; kk < NEQ; ++kk) TA[kk * NQF + qa] = -w * F[kk];
+      for (int kk = 0; kk < NEQ; ++kk) TA[kk * ak + qa * aq] = -w * F[kk];
     }
     if (!bnd && !hb) {
 #pragma unroll
-      for (int kk = 0; kk < NEQ; ++kk) TB[kk * NQF + qb] = w * F[kk];
+      for (int kk = 0; kk < NEQ; ++kk) TB[kk * bk + qb * bq] = w * F[kk];
     }
   }
   __syncthreads();
   // 3. lifting of this axis's two faces
   if (act && !prm.faces_only) {
-    team_lift<P, LF0, 1>(sT + ((el * 2 + 0) * NEQ + k) * NQF, H.l1d, H.lend, acc);
-    team_lift<P, LF1, 1>(sT + ((el * 2 + 1) * NEQ + k) * NQF, H.l1d, H.lend, acc);
+    team_lift<P, LF0, TS>(sT + (0 * NEQ + k) * NQF * TS + el, H.l1d, H.lend, acc);
+    team_lift<P, LF1, TS>(sT + (1 * NEQ + k) * NQF * TS + el, H.l1d, H.lend, acc);
   }
 }
 
@@ -222,8 +230,8 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
   __shared__ unsigned char sFab[6][NQF];
   R* sm = reinterpret_cast<R*>(smraw);
   R* sU = sm;              // [NEQ][E][ND]; the right-hand side after the volume phase
-  R* sT = sm + S::OFF_T;   // [E][2][NEQ][NQF]
-  R* sH = sm + S::OFF_H;   // [HM][NEQ][NQF]
+  R* sT = sm + S::OFF_T;   // [2][NEQ][NQF][TS]
+  R* sH = sm + S::OFF_H;   // [NEQ][NQF][HS]
   const HexOps<R>& H = hex_ops<R>(prm.hops);
   const RefTables* RT = prm.tab;
   const int tid = threadIdx.x;

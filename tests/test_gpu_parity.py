@@ -166,6 +166,8 @@ def test_rhs_hex_shared_faces(cuda, variant, prec, order, n, bc):
     from rkdg3d_gb300.solver import TUNE_HEX_KERNEL
     case = (periodic_case(M.GEOM_CUBE, n, order, RS_HLL) if bc is None
             else walled_case(M.GEOM_CUBE, n, order, RS_HLLC, AVG_EINFELDT, bc=bc))
+    if n in (10, 12):  # n elements of h = 1/16 (dyadic spacing)
+        case.mesh = M.hex_grid(n, n, n, box=((0.0, n / 16),) * 3, periodic=(bc is None,) * 3)
     if bc in BC_PARAMS:
         case.bcs = [(a, bc, BC_PARAMS[bc]) for a, _, _ in case.bcs]
     ctx, orc = pair(case)
