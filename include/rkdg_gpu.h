@@ -274,8 +274,11 @@ long long rkdg_kernel_launches(rkdg_ctx* ctx);
  * Meshes with neq * NE > RKDG_LIMIT_STATIC_MAX_VALUES are rejected with
  * RKDG_ERR_INVALID and x is left untouched.  The first call on a device looks
  * up the array's device address (cudaGetSymbolAddress), so make that first
- * call before any stream capture.  The array is shared by every context on a
- * device: calls that overlap in time on one device (other host threads, other
+ * call before any stream capture; the address stays cached for the life of
+ * the process, so a device reset (cudaDeviceReset) ends the use of this entry
+ * point in that process.  The call returns once the limiter has finished on
+ * the context's stream.  The array is shared by every context on a device:
+ * calls that overlap in time on one device (other host threads, other
  * streams) race on it and must be serialised by the caller. */
 #define RKDG_LIMIT_STATIC_MAX_VALUES (1u << 21)
 int rkdg_limit_static(rkdg_ctx* ctx, double* x_dev);

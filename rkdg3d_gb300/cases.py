@@ -140,6 +140,25 @@ def gaussian_pulses(n=32, order=1, seed=0, steps=200, cfl=0.2, npulse=8) -> Case
                 t_end=1e30, cfl=cfl, dt_mode=1, max_steps=steps, ic=ic)
 
 
+def gaussian_pulses_perturbed(n=32, order=1, seed=0, perturb_seed=1, scale=0.25, steps=200,
+                              cfl=0.2) -> Case:
+    """The target of the adjoint workload: the seed-``seed`` pulses of
+    gaussian_pulses with a seed-``perturb_seed`` perturbation added,
+    rho = rho_seed + scale * (rho_perturb_seed - 1), p = rho^gamma, u = 0."""
+    base = gaussian_pulses(n, order, seed, steps, cfl)
+    pert = gaussian_pulses(n, order, perturb_seed, steps, cfl)
+    gamma = base.gamma
+
+    def ic(x):
+        rho = base.ic(x)[0] + scale * (pert.ic(x)[0] - 1.0)
+        z = np.zeros_like(rho)
+        return rho, z, z, z, rho ** gamma
+
+    base.name = f"gaussian_pulses{seed}_perturbed{perturb_seed}"
+    base.ic = ic
+    return base
+
+
 def double_mach(nx=1024, ny=256, order=1, jitter=0.2, seed=0, t_end=0.2, cfl=0.25) -> Case:
     """Double Mach reflection on [0,4]x[0,1]: jittered triangulation of an
     nx x ny grid; Mach-10 shock at 60 degrees through (1/6, 0); pre-shock

@@ -81,44 +81,41 @@ __device__ __forceinline__ void tile_halo_trace(const R* __restrict__ src, int l
   team_interp<P, ST>(v, l1d, dst);
 }
 
-// One normal axis AX: traces, face evaluations, lifting.
-template <int P, typename R, int AX>
-__device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restrict__ u,
-                                          long long NDa, const HexTile& T, R* sT, R* sH,
-                                          const unsigned char (*perm)[(P + 2) * (P + 2)],
-                                          const unsigned char (*fab)[(P + 2) * (P + 2)],
-                                          const HexOps<R>& H, int k, int el, bool act,
-                                          const R (&uu)[(P + 1) * (P + 1) * (P + 1)],
-                                          R (&acc)[(P + 1) * (P + 1) * (P + 1)], R& lmax) {
+// Own traces (AX compile-time: the face pair and its tensor offsets) of the
+// thread's variable on the two faces of axis AX, slot-fastest rows.
+template <int P, int TS, int AX, typename R>
+__device__ __forceinline__ void tile_own_traces(const R (&uu)[(P + 1) * (P + 1) * (P + 1)],
+                                                const HexOps<R>& H, R* row0, R* row1) {
+  constexpr int NF2 = (P + 1) * (P + 1);
+  R v[NF2];
+  team_contract<P, hex_axis_face(AX, 0)>(uu, H.lend, v);
+  team_interp<P, TS>(v, H.l1d, row0);
+  team_contract<P, hex_axis_face(AX, 1)>(uu, H.lend, v);
+  team_interp<P, TS>(v, H.l1d, row1);
+}
+
+template <int P, int TS, int AX, typename R>
+__device__ __forceinline__ void tile_own_lift(const R* row0, const R* row1, const HexOps<R>& H,
+                                              R (&acc)[(P + 1) * (P + 1) * (P + 1)]) {
+  team_lift<P, hex_axis_face(AX, 0), TS>(row0, H.l1d, H.lend, acc);
+  team_lift<P, hex_axis_face(AX, 1), TS>(row1, H.l1d, H.lend, acc);
+}
+
+// Face evaluations of axis ax, point by point over the CTA (one copy of the
+// pointwise code for all three axes).
+template <int P, typename R>
+__device__ __forceinline__ void tile_fluxes(const RhsParams& prm, const HexTile& T, int ax, R* sT,
+                                            R* sH, const unsigned char (*perm)[(P + 2) * (P + 2)],
+                                            const unsigned char (*fab)[(P + 2) * (P + 2)],
+                                            const R* wf, R& lmax) {
   using S = TileSize<P>;
-  constexpr int NQF = S::NQF, NEQ = S::NEQ, NF2 = S::NF2, NT = S::NT, TS = S::TS, HS = S::HS;
-  constexpr int LF0 = hex_axis_face(AX, 0), LF1 = hex_axis_face(AX, 1);
-  const int tid = threadIdx.x;
-  // 1. own traces (every face side of the tile has exactly one evaluation,
-  // so every stored trace is read once and overwritten by its flux)
-  if (act) {
-    R v[NF2];
-    team_contract<P, LF0>(uu, H.lend, v);
-    team_interp<P, TS>(v, H.l1d, sT + (0 * NEQ + k) * NQF * TS + el);
-    team_contract<P, LF1>(uu, H.lend, v);
-    team_interp<P, TS>(v, H.l1d, sT + (1 * NEQ + k) * NQF * TS + el);
-  }
-  // halo traces, one (variable, halo) per thread, consecutive halos on
-  // consecutive threads
-  const int nh = T.nh[AX];
-  for (int j = tid; j < nh * NEQ; j += NT) {
-    const int kk = j / nh, h = j - kk * nh;
-    tile_halo_trace<P, HS, R>(u + kk * NDa + (long long)T.hel[AX][h] * S::ND, T.hlf[AX][h], H.l1d,
-                              H.lend, sH + kk * NQF * HS + h);
-  }
-  __syncthreads();
-  // 2. face evaluations, point by point over the CTA
+  constexpr int NQF = S::NQF, NEQ = S::NEQ, NT = S::NT, TS = S::TS, HS = S::HS;
   const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
-  const int nev = T.nev[AX];
+  const int nev = T.nev[ax];
 #pragma unroll 1
-  for (int pt = tid; pt < nev * NQF; pt += NT) {
+  for (int pt = threadIdx.x; pt < nev * NQF; pt += NT) {
     const int j = pt / NQF, q = pt - j * NQF;
-    const unsigned d = T.ev[AX][j];
+    const unsigned d = T.ev[ax][j];
     const int ia = d & 63, ib = (d >> 7) & 63;
     const bool ha = (d >> 6) & 1, hb = (d >> 13) & 1, bnd = (d >> 14) & 1;
     const int lfa = (d >> 15) & 7, lfb = (d >> 18) & 7, pid = (d >> 21) & 7;
@@ -160,7 +157,7 @@ __device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restr
     R F[NEQ];
     const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), ge);
     lmax = fmax(lmax, sp);
-    const R w = H.wf[q] * jac;
+    const R w = wf[q] * jac;
     if (!ha) {
 #pragma unroll
       for (int kk = 0; kk < NEQ; ++kk) TA[kk * ak + qa * aq] = -w * F[kk];
@@ -170,51 +167,33 @@ __device__ __forceinline__ void tile_axis(const RhsParams& prm, const R* __restr
       for (int kk = 0; kk < NEQ; ++kk) TB[kk * bk + qb * bq] = w * F[kk];
     }
   }
-  __syncthreads();
-  // 3. lifting of this axis's two faces
-  if (act && !prm.faces_only) {
-    team_lift<P, LF0, TS>(sT + (0 * NEQ + k) * NQF * TS + el, H.l1d, H.lend, acc);
-    team_lift<P, LF1, TS>(sT + (1 * NEQ + k) * NQF * TS + el, H.l1d, H.lend, acc);
-  }
 }
 
-// Volume term of variable K for one element: the nodal Euler flux of all
-// variables at every node (FE_Evolution::GetFlux), its contravariant
-// components of variable K, and the collocated derivative operator applied in
-// scatter form: node m = (mx, my, mz) adds w_my w_mz d1[jx][mx] G_x(m) to
-// (jx, my, mz), and likewise along y and z, so no nodal array is kept.
-template <int P, int K, typename R>
-__device__ __forceinline__ void tile_volume(const R* sUe, int vstride, const R (&adj)[3][3],
-                                            const HexOps<R>& H, R gamma, R cov,
-                                            R (&acc)[(P + 1) * (P + 1) * (P + 1)], R& lmax) {
-  constexpr int N1 = P + 1, NEQ = 5;
+// Collocated derivative sweep along direction R of variable values g (the
+// contravariant flux component along R at the nodes), added to acc with the
+// other two directions' node weights.
+template <int P, int DIR, typename R>
+__device__ __forceinline__ void tile_sweep(const R (&g)[(P + 1) * (P + 1) * (P + 1)],
+                                           const HexOps<R>& H, R (&acc)[(P + 1) * (P + 1) * (P + 1)]) {
+  constexpr int N1 = P + 1;
   const R* tD1 = H.d1;
   const R* tW1 = H.w1;
 #pragma unroll
-  for (int mz = 0; mz < N1; ++mz)
+  for (int jz = 0; jz < N1; ++jz)
 #pragma unroll
-    for (int my = 0; my < N1; ++my)
+    for (int jy = 0; jy < N1; ++jy)
 #pragma unroll
-      for (int mx = 0; mx < N1; ++mx) {
-        const int m = mx + N1 * (my + N1 * mz);
-        R st[NEQ];
+      for (int jx = 0; jx < N1; ++jx) {
+        R s = R(0);
 #pragma unroll
-        for (int kk = 0; kk < NEQ; ++kk) st[kk] = sUe[kk * vstride + m];
-        R F[NEQ][3];
-        const R sp = flux_and_speed<3>(st, F, gamma, cov);
-        if (K == 0) lmax = fmax(lmax, sp);
-        R g[3];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) g[r] = adj[r][0] * F[K][0] + adj[r][1] * F[K][1] + adj[r][2] * F[K][2];
-        const R gx = tW1[my] * tW1[mz] * g[0];
-        const R gy = tW1[mx] * tW1[mz] * g[1];
-        const R gz = tW1[mx] * tW1[my] * g[2];
-#pragma unroll
-        for (int j = 0; j < N1; ++j) {
-          acc[j + N1 * (my + N1 * mz)] += tD1[j * N1 + mx] * gx;
-          acc[mx + N1 * (j + N1 * mz)] += tD1[j * N1 + my] * gy;
-          acc[mx + N1 * (my + N1 * j)] += tD1[j * N1 + mz] * gz;
+        for (int m = 0; m < N1; ++m) {
+          const int src = DIR == 0 ? m + N1 * (jy + N1 * jz)
+                                   : (DIR == 1 ? jx + N1 * (m + N1 * jz) : jx + N1 * (jy + N1 * m));
+          const int jd = DIR == 0 ? jx : (DIR == 1 ? jy : jz);
+          s += tD1[jd * N1 + m] * g[src];
         }
+        const R w = DIR == 0 ? tW1[jy] * tW1[jz] : (DIR == 1 ? tW1[jx] * tW1[jz] : tW1[jx] * tW1[jy]);
+        acc[jx + N1 * (jy + N1 * jz)] += w * s;
       }
 }
 
@@ -224,8 +203,10 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
                    const EpiParams<R> ep) {
   using S = TileSize<P>;
   constexpr int N1 = S::N1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, E = S::E, NT = S::NT;
+  constexpr int TS = S::TS, HS = S::HS;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ HexTile sTile;
+  __shared__ R sGeo[E][10];  // per slot: adj(J) (row r, col d) and 1/det J
   __shared__ unsigned char sPerm[RKDG_HEX_MAX_PERM][NQF];
   __shared__ unsigned char sFab[6][NQF];
   R* sm = reinterpret_cast<R*>(smraw);
@@ -251,6 +232,10 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
     const int k = f / (E * ND), r = f - k * (E * ND), el = r / ND, i = r - el * ND;
     sU[f] = el < nel ? u[k * NDa + (long long)sTile.el[el] * ND + i] : R(0);
   }
+  for (int t = tid; t < nel * 10; t += NT) {
+    const int sl = t / 10, c = t - sl * 10;
+    sGeo[sl][c] = ((const R*)prm.egeo)[(long long)c * ne + sTile.el[sl]];
+  }
   __syncthreads();
   const int k = tid / E, el = tid - k * E;  // one variable per warp (E = 32)
   const bool act = el < nel;
@@ -262,30 +247,78 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
     acc[i] = R(0);
   }
   R lmax = R(0);
-  tile_axis<P, R, 0>(prm, u, NDa, sTile, sT, sH, sPerm, sFab, H, k, el, act, uu, acc, lmax);
-  tile_axis<P, R, 1>(prm, u, NDa, sTile, sT, sH, sPerm, sFab, H, k, el, act, uu, acc, lmax);
-  tile_axis<P, R, 2>(prm, u, NDa, sTile, sT, sH, sPerm, sFab, H, k, el, act, uu, acc, lmax);
+  R* row0 = sT + (0 * NEQ + k) * NQF * TS + el;
+  R* row1 = sT + (1 * NEQ + k) * NQF * TS + el;
+#pragma unroll 1
+  for (int ax = 0; ax < 3; ++ax) {
+    // 1. traces: own (every face side of the tile has exactly one evaluation,
+    // so every stored trace is read once and overwritten by its flux), then
+    // the halo, one (variable, halo) per thread
+    if (act) {
+      switch (ax) {
+        case 0: tile_own_traces<P, TS, 0>(uu, H, row0, row1); break;
+        case 1: tile_own_traces<P, TS, 1>(uu, H, row0, row1); break;
+        default: tile_own_traces<P, TS, 2>(uu, H, row0, row1); break;
+      }
+    }
+    const int nh = sTile.nh[ax];
+    for (int j = tid; j < nh * NEQ; j += NT) {
+      const int kk = j / nh, h = j - kk * nh;
+      tile_halo_trace<P, HS, R>(u + kk * NDa + (long long)sTile.hel[ax][h] * ND, sTile.hlf[ax][h],
+                                H.l1d, H.lend, sH + kk * NQF * HS + h);
+    }
+    __syncthreads();
+    // 2. every face of the axis once
+    tile_fluxes<P, R>(prm, sTile, ax, sT, sH, sPerm, sFab, H.wf, lmax);
+    __syncthreads();
+    // 3. lifting of the thread's two faces
+    if (act && !prm.faces_only) {
+      switch (ax) {
+        case 0: tile_own_lift<P, TS, 0>(row0, row1, H, acc); break;
+        case 1: tile_own_lift<P, TS, 1>(row0, row1, H, acc); break;
+        default: tile_own_lift<P, TS, 2>(row0, row1, H, acc); break;
+      }
+    }
+  }
   if (prm.faces_only) {
     block_max_commit<R>(lmax, prm.mcs);
     return;
   }
+  // volume term, one direction at a time: the contravariant component along
+  // direction r of every variable's nodal flux (FE_Evolution::GetFlux), one
+  // (element, node) per thread, into the trace region; then each thread's
+  // collocated sweep along r
+  R* sG = sT;  // [NEQ][E][ND]
+  const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+#pragma unroll 1
+  for (int r = 0; r < 3; ++r) {
+    __syncthreads();  // the lifts (r = 0) or the previous sweeps are done with sT
+    for (int t = tid; t < nel * ND; t += NT) {
+      const int sl = t / ND, m = t - sl * ND;
+      R st[NEQ];
+#pragma unroll
+      for (int kk = 0; kk < NEQ; ++kk) st[kk] = sU[(kk * E + sl) * ND + m];
+      R F[NEQ][3];
+      const R sp = flux_and_speed<3>(st, F, gamma, cov);
+      if (r == 0) lmax = fmax(lmax, sp);
+      const R a0 = sGeo[sl][3 * r], a1 = sGeo[sl][3 * r + 1], a2 = sGeo[sl][3 * r + 2];
+#pragma unroll
+      for (int kk = 0; kk < NEQ; ++kk) sG[(kk * E + sl) * ND + m] = a0 * F[kk][0] + a1 * F[kk][1] + a2 * F[kk][2];
+    }
+    __syncthreads();
+    if (act) {
+      R gv[ND];
+#pragma unroll
+      for (int i = 0; i < ND; ++i) gv[i] = sG[(k * E + el) * ND + i];
+      switch (r) {
+        case 0: tile_sweep<P, 0>(gv, H, acc); break;
+        case 1: tile_sweep<P, 1>(gv, H, acc); break;
+        default: tile_sweep<P, 2>(gv, H, acc); break;
+      }
+    }
+  }
   R g[ND];
   if (act) {
-    const R* eg = (const R*)prm.egeo;
-    R adj[3][3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) adj[r][d] = eg[(long long)(r * 3 + d) * ne + e];
-    const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
-    const R* sUe = sU + el * ND;
-    switch (k) {  // warp-uniform
-      case 0: tile_volume<P, 0, R>(sUe, E * ND, adj, H, gamma, cov, acc, lmax); break;
-      case 1: tile_volume<P, 1, R>(sUe, E * ND, adj, H, gamma, cov, acc, lmax); break;
-      case 2: tile_volume<P, 2, R>(sUe, E * ND, adj, H, gamma, cov, acc, lmax); break;
-      case 3: tile_volume<P, 3, R>(sUe, E * ND, adj, H, gamma, cov, acc, lmax); break;
-      default: tile_volume<P, 4, R>(sUe, E * ND, adj, H, gamma, cov, acc, lmax); break;
-    }
     if (prm.ncidx) {  // hanging faces of a nonconforming mesh
       const int ix = prm.ncidx[e];
       if (ix >= 0) {
@@ -318,7 +351,7 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
           for (int m = 0; m < N1; ++m) s += tMinv[jy * N1 + m] * g[jx + N1 * (m + N1 * jz)];
           acc[jx + N1 * (jy + N1 * jz)] = s;
         }
-    const R idet = eg[(long long)9 * ne + e];
+    const R idet = sGeo[el][9];
 #pragma unroll
     for (int jz = 0; jz < N1; ++jz)
 #pragma unroll

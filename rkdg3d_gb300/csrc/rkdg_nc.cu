@@ -86,7 +86,9 @@ __global__ void __launch_bounds__(kNcFaceThreads) k_nc_face(const __grid_constan
 #pragma unroll
     for (int k = 0; k < NEQ; ++k) sF[lf][q][k] = (F[k] * wq) * jac;
   }
-  if (prm.prob) {  // per-problem maximum; a face point of an idle problem commits nothing
+  if (prm.prob) {
+    // per-problem maximum; a face point of an idle problem keeps lmax = 0,
+    // and atomic_max_nonneg issues no atomic for a speed that is not positive
     if (pb >= 0) atomic_max_nonneg(prm.pmcs + pb, (double)lmax);
     __syncthreads();  // sF is complete after it
   } else {

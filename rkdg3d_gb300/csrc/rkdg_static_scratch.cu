@@ -8,8 +8,10 @@
 // doubles (16 MiB), which every GPU that loads the library holds until the
 // process exits.  In host code the array's name is only a stand-in, not a
 // device address: the first rkdg_limit_static call on a device looks the
-// address up with cudaGetSymbolAddress (that device current) and caches it, so
-// that first call should come before any stream capture.  Every context on a
+// address up with cudaGetSymbolAddress (that device current) and caches it for
+// the life of the process, so that first call should come before any stream
+// capture, and a device reset (which would invalidate the cached address) ends
+// the use of rkdg_limit_static in the process.  Every context on a
 // device shares the array, so two rkdg_limit_static calls in flight at the
 // same time on one device (two host threads, or two contexts on different
 // streams) overwrite each other's means; nothing in it needs to start at zero,

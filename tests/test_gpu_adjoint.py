@@ -181,20 +181,21 @@ def test_adjoint_gradient_full_size(cuda):
     """Adjoint workload at full size: 32^3 periodic Q1 hexes, eight Gaussian
     density pulses, HLLC, Venkatakrishnan, SSP-RK3 with dt fixed from CFL 0.2,
     200 steps checkpointed every 20.  J = 1/2 ||rho(T) - rho_target(T)||^2 with
-    the target run from the seed-1 pulses.
+    the target run from the seed-0 pulses plus a seed-1 perturbation.
 
     The reference's limiter makes J only piecewise smooth: the min/max over
     stencil values switch branches and the indicator's absolute +-1e-3
     thresholds (indicator_bj.cpp:49-51) jump, and over 600 limited stages some
-    switch usually lies within a few 1e-8 of the state along a random
-    direction.  A direction is therefore assessed only when two central
-    differences (eps = 4e-6 and 1e-6) agree with each other to 1e-5 -- no
-    switch inside the window -- and there the adjoint must agree to 1e-5.
-    RKDG_ADJOINT_DIRECTIONS sets the number of random directions (64 for the
-    full check; default 12)."""
+    switch can lie within a few 1e-8 of the state along a random direction.
+    Each direction therefore picks its finite-difference step: the first two
+    consecutive central differences of eps = 4e-6, 1e-6, 2.5e-7 that agree
+    with each other to 1e-5 (no switch inside the window) assess it, and there
+    the adjoint must agree to 1e-5.  RKDG_ADJOINT_DIRECTIONS sets the number
+    of random directions (default 64); at least three quarters must be
+    assessed."""
     import os
     case = cases.gaussian_pulses(n=32, seed=0)
-    target = cases.gaussian_pulses(n=32, seed=1)
+    target = cases.gaussian_pulses_perturbed(n=32, seed=0, perturb_seed=1)
     ctx = ctx_for(case)
     X = ctx.node_coords()
     x0 = cases.project(case, X)
@@ -220,18 +221,22 @@ def test_adjoint_gradient_full_size(cuda):
     ctx.adjoint_run(dev(x0), nsteps, dt, every, xb, xT)
     assert torch.allclose(xT, y, rtol=0, atol=1e-12)
     g = xb.cpu().numpy()
-    ndir = int(os.environ.get("RKDG_ADJOINT_DIRECTIONS", "12"))
+    ndir = int(os.environ.get("RKDG_ADJOINT_DIRECTIONS", "64"))
     rng = np.random.default_rng(5)
     assessed, worst = 0, 0.0
     for _ in range(ndir):
         v = rng.normal(size=ctx.n) * 1e-2
         ad = float(np.dot(g, v))
-        fd = [(J(x0 + e * v) - J(x0 - e * v)) / (2 * e) for e in (4e-6, 1e-6)]
-        if abs(fd[0] - fd[1]) > 1e-5 * abs(fd[1]):
-            continue  # a limiter switch inside the difference window
-        assessed += 1
-        worst = max(worst, abs(ad - fd[1]) / abs(fd[1]))
-    assert assessed >= ndir // 3, (assessed, ndir)
+        prev = None
+        for e in (4e-6, 1e-6, 2.5e-7):
+            fd = (J(x0 + e * v) - J(x0 - e * v)) / (2 * e)
+            if prev is not None and abs(fd - prev) <= 1e-5 * abs(fd):
+                assessed += 1
+                worst = max(worst, abs(ad - fd) / abs(fd))
+                break
+            prev = fd
+    print(f"adjoint FD check: {assessed} of {ndir} directions assessed, worst relative error {worst:.2e}")
+    assert assessed >= (3 * ndir) // 4, (assessed, ndir)
     assert worst <= 1e-5, worst
 
 

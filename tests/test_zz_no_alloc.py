@@ -74,6 +74,23 @@ def test_limit_static_equals_limit(cuda, geom, order, lim, fun):
     assert torch.equal(b, c)
 
 
+def test_limit_static_allocates_nothing(cuda):
+    """After one warm call (module load, address look-up), further calls
+    leave the device's free memory unchanged: the cell means go to the fixed
+    array, nothing is allocated or freed."""
+    case = _case(M.GEOM_SQUARE, 1, LIM_MULTI, FUN_BJ)
+    ctx = Context(case.mesh, case.order, device=0)
+    cases.configure_context(case, ctx)
+    x = _state(ctx, case, 13)
+    ctx.limit_static(x)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        ctx.limit_static(x)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_limit_static_rejects_oversize_mesh(cuda):
     # 725 x 725 quads, 4 equations: 2,102,500 > 2^21 means
     mesh = M.quad_grid(725, 725, 0, 1, 0, 1, periodic=(True, True))
