@@ -55,8 +55,14 @@ enum {
   RKDG_BC_SUBSONIC_INLET_TOTAL_PRESSURE = 6, /* ..._subsonic_inlet_total_pressure.cpp:10-40 */
   RKDG_BC_SUBSONIC_INLET_FIXED_PRESSURE = 7, /* ..._subsonic_inlet_fixed_pressure.cpp:10-36 */
   RKDG_BC_FIXED_PRESSURE_OUTLET = 8,         /* boundary_integrator_open_fixed_pressure.cpp:10-30 */
-  RKDG_BC_TOTAL_PRESSURE_OUTLET = 9          /* boundary_integrator_open_total_pressure.cpp:10-40;
+  RKDG_BC_TOTAL_PRESSURE_OUTLET = 9,         /* boundary_integrator_open_total_pressure.cpp:10-40;
                                                 m.n uses the normal's own components */
+  /* boundary_integrator_char_outlet.cpp:14-57; state = the outer
+   * conservative state.  The reference's ghost vector enters its
+   * computeRightState unassigned (the previous boundary point's ghost state,
+   * uninitialised memory at the first); here it enters as the interior
+   * state at every point. */
+  RKDG_BC_CHAR_OUTLET = 10
 };
 enum { RKDG_LIM_FINDIFF = 0, RKDG_LIM_MULTI = 1 };
 /* RKDG_IND_SHU: IndicatorShu (indicator_shu.cpp:13-74) with the extrapolated

@@ -897,6 +897,31 @@ void compute_right_state(const ref_ctx* c, const BC& bc, const double* s1, doubl
       s2[0] = rho;
       break;
     }
+    case 10: {  // charOutlet, boundary_integrator_char_outlet.cpp:14-57
+      // The reference rotates and reads its ghost vector before it assigns it
+      // (the previous boundary point's ghost state, or uninitialised memory at
+      // the first point); here it enters as the interior state s1.  bc.state
+      // holds the outer state (cOut, UOut from it, as the constructor does).
+      const double g = c->P.gamma, b = c->P.b;
+      const double cOut = sound_speed(c->P, bc.state);
+      const double UOut = bc.state[1] / bc.state[0];
+      const double cIn = sound_speed(c->P, s1);
+      rotate(dim, s2, nor);
+      const double UIn = s2[1] / s2[0];
+      const double UB = 0.5 * (UIn + UOut) - (cOut - cIn) / (g - 1.0);
+      const double cB = -0.25 * (g - 1.0) * (UOut - UIn) + 0.5 * (cOut + cIn);
+      const double sB = s2[1] < 0 ? cOut * cOut / std::pow(bc.state[0], g - 1.0) / g
+                                  : cIn * cIn / std::pow(s2[0], g - 1.0) / g;
+      const double rhoB = std::pow(cB * cB / sB / g, 1.0 / (g - 1.0));
+      const double pB = rhoB * cB * cB / g;
+      s2[0] = rhoB;
+      s2[1] = UB;  // a velocity in the momentum slot, as the reference stores it
+      const double v = s2[2] / s2[0], w = dim == 3 ? s2[3] / s2[0] : 0.0;
+      // ComputeEnergy, physics.cpp:128-131
+      s2[neq - 1] = pB / (g - 1.0) * (1.0 - rhoB * b) + 0.5 * rhoB * (UB * UB + v * v + w * w);
+      inverse_rotate(dim, s2, nor);
+      break;
+    }
   }
 }
 
@@ -1336,7 +1361,7 @@ int ref_set_physics(ref_ctx* c, int rsolver, int averaging, double gamma, double
 }
 
 int ref_set_bc(ref_ctx* c, int attr, int type, const double* state) {
-  if (type < 0 || type > 9) return REF_ERR_INVALID;
+  if (type < 0 || type > 10) return REF_ERR_INVALID;
   if (!state && (type == 2 || type == 3 || type >= 5)) return REF_ERR_INVALID;
   BC bc;
   bc.type = type;

@@ -60,9 +60,11 @@ int ref_set_physics(ref_ctx* c, int rsolver, int averaging, double gamma,
  * 4 wall (same as slip), 5 subsonic inlet (fixed rotated-frame state),
  * 6 subsonicInletTotalPressure {pTot, TTot}, 7 subsonicInletFixedPressure
  * {pFix, TTot}, 8 fixedPressureOutlet {pFix}, 9
- * totalPressureFixedTemperatureOutlet {pTot, TFix}.  state (neq values) =
- * conservative variables (types 2, 3, 5), the listed parameters in its first
- * entries (6-9), or NULL. */
+ * totalPressureFixedTemperatureOutlet {pTot, TFix}, 10 charOutlet (outer
+ * conservative state; the ghost vector, which the reference reads before it
+ * assigns it, enters as the interior state).  state (neq values) =
+ * conservative variables (types 2, 3, 5, 10), the listed parameters in its
+ * first entries (6-9), or NULL. */
 int ref_set_bc(ref_ctx* c, int attr, int type, const double* state);
 /* computeRightState of attribute attr's boundary condition for the state s1
  * and the unit outward normal nor (test hook). */

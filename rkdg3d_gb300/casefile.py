@@ -26,7 +26,7 @@ import numpy as np
 
 from . import cases as C
 from . import mesh as M
-from .solver import (AVG_TRRS, BC_FIXED_PRESSURE_OUTLET, BC_OPEN, BC_SLIP,
+from .solver import (AVG_TRRS, BC_CHAR_OUTLET, BC_FIXED_PRESSURE_OUTLET, BC_OPEN, BC_SLIP,
                      BC_SUBSONIC_INLET_FIXED_PRESSURE, BC_SUBSONIC_INLET_TOTAL_PRESSURE,
                      BC_SUPERSONIC_INLET, BC_TOTAL_PRESSURE_OUTLET, FUN_MICHALAK, IND_BJ,
                      IND_EVERYWHERE, IND_NOWHERE, IND_SHU, LIM_FINDIFF, LIM_MULTI,
@@ -200,8 +200,13 @@ def _bc(patch: dict, dim: int, gamma: float):
     if t == "fixedPressureOutlet":
         return BC_FIXED_PRESSURE_OUTLET, [float(patch["pFix"])]
     if t == "charOutlet":
-        raise CaseError("charOutlet is not supported (the reference reads its ghost state "
-                        "before assigning it)")
+        # case_manager.cpp:779-802: rho, rho u, rho v, rho w, then the energy
+        # without the third velocity component (in 2D it overwrites rho w)
+        rho = float(patch["rhoI"])
+        u = [float(v) for v in patch["UI"]] + [0.0, 0.0]
+        p = float(patch["pI"])
+        E = p / (gamma - 1.0) + 0.5 * rho * (u[0] * u[0] + u[1] * u[1])
+        return BC_CHAR_OUTLET, [rho] + [rho * v for v in u[:dim]] + [E]
     raise CaseError(f"unknown boundary condition type {t!r} (the reference exits here)")
 
 

@@ -2,10 +2,11 @@
 //
 // One CTA per tile of RKDG_TILE_E hexahedra that are consecutive in the Morton
 // order of their centres (HexTile, built on the host).  NEQ * E threads; thread
-// (variable k, slot el) keeps its element's (p+1)^3 values of variable k and
-// the right-hand-side accumulators in registers for the whole stage (a warp
-// holds one variable of 32 elements, so variable-dependent code never
-// diverges).  The faces are processed one normal axis at a time:
+// (variable k, slot el) keeps its element's right-hand-side accumulators of
+// variable k in registers for the whole stage, and reads the element's staged
+// values from shared memory (a warp holds one variable of 32 elements, so
+// variable-dependent code never diverges).  The faces are processed one normal
+// axis at a time:
 //   1. each thread forms its element's traces on the axis's two faces at the
 //      (p+2)^2 face points (contraction along the normal, then the 2D
 //      interpolation, sum-factorised) into shared memory; threads without a
@@ -84,13 +85,12 @@ __device__ __forceinline__ void tile_halo_trace(const R* __restrict__ src, int l
 // Own traces (AX compile-time: the face pair and its tensor offsets) of the
 // thread's variable on the two faces of axis AX, slot-fastest rows.
 template <int P, int TS, int AX, typename R>
-__device__ __forceinline__ void tile_own_traces(const R (&uu)[(P + 1) * (P + 1) * (P + 1)],
-                                                const HexOps<R>& H, R* row0, R* row1) {
+__device__ __forceinline__ void tile_own_traces(const R* su, const HexOps<R>& H, R* row0, R* row1) {
   constexpr int NF2 = (P + 1) * (P + 1);
   R v[NF2];
-  team_contract<P, hex_axis_face(AX, 0)>(uu, H.lend, v);
+  team_contract_s<P, hex_axis_face(AX, 0)>(su, H.lend, v);
   team_interp<P, TS>(v, H.l1d, row0);
-  team_contract<P, hex_axis_face(AX, 1)>(uu, H.lend, v);
+  team_contract_s<P, hex_axis_face(AX, 1)>(su, H.lend, v);
   team_interp<P, TS>(v, H.l1d, row1);
 }
 
@@ -101,71 +101,98 @@ __device__ __forceinline__ void tile_own_lift(const R* row0, const R* row1, cons
   team_lift<P, hex_axis_face(AX, 1), TS>(row1, H.l1d, H.lend, acc);
 }
 
+// One face point of an evaluation: both states (the Elem2 side through the
+// boundary condition on a boundary face), the Elem1-outward normal, the
+// weight w_q |J_f|, and where each side's weighted flux goes.
+template <typename R>
+struct TilePoint {
+  R s1[5], s2[5], n[3], w;
+  R* pa;   // Elem1 side's flux (variable kk at pa[kk * ka]); null: a halo side
+  R* pb;   // Elem2 side's; null: a halo side or a boundary face
+  int ka, kb, ge;
+  bool zero;  // boundary face without an integrator: no face term
+};
+
+template <int P, typename R>
+__device__ __forceinline__ void tile_point(const RhsParams& prm, const HexTile& T, int ax, int pt,
+                                           R* sT, R* sH, const R (*eg)[4],
+                                           const unsigned char (*perm)[(P + 2) * (P + 2)],
+                                           const unsigned char (*fab)[(P + 2) * (P + 2)],
+                                           const R* wf, R gamma, R cov, TilePoint<R>& X) {
+  using S = TileSize<P>;
+  constexpr int NQF = S::NQF, NEQ = S::NEQ, TS = S::TS, HS = S::HS;
+  const int j = pt / NQF, q = pt - j * NQF;
+  const unsigned d = T.ev[ax][j];
+  const int ia = d & 63, ib = (d >> 7) & 63;
+  const bool ha = (d >> 6) & 1, hb = (d >> 13) & 1, bnd = (d >> 14) & 1;
+  const int lfa = (d >> 15) & 7, lfb = (d >> 18) & 7, pid = (d >> 21) & 7;
+  const bool gb = (d >> 24) & 1;
+  // a side's value of variable kk at tensor point t: base[kk * k_ + t * q_]
+  const int ak = ha ? NQF * HS : NQF * TS, aq = ha ? HS : TS;
+  const int bk = hb ? NQF * HS : NQF * TS, bq = hb ? HS : TS;
+  R* TA = (ha ? sH + ia : sT + (ia & 1) * (NEQ * NQF * TS) + (ia >> 1)) + fab[lfa][q] * aq;
+  X.ge = T.el[(gb ? ib : ia) >> 1];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) X.n[c] = eg[j][c];
+  X.w = wf[q] * eg[j][3];
+#pragma unroll
+  for (int kk = 0; kk < NEQ; ++kk) X.s1[kk] = TA[kk * ak];
+  X.pa = ha ? nullptr : TA;
+  X.ka = ak;
+  X.zero = false;
+  if (bnd) {
+    const int nb = prm.fnbr[lfa * prm.ne + X.ge];
+    X.pb = nullptr;
+    X.kb = 0;
+    if (nb == -1) {
+      X.zero = true;
+#pragma unroll
+      for (int kk = 0; kk < NEQ; ++kk) X.s2[kk] = X.s1[kk];
+    } else {
+      const BCSlot& bc = prm.bc[-2 - nb];
+      right_state<3>(bc.type, bc.state, X.s1, X.s2, X.n, gamma, cov, (R)prm.rgas);
+    }
+  } else {
+    R* TB = (hb ? sH + ib : sT + (ib & 1) * (NEQ * NQF * TS) + (ib >> 1)) + fab[lfb][perm[pid][q]] * bq;
+#pragma unroll
+    for (int kk = 0; kk < NEQ; ++kk) X.s2[kk] = TB[kk * bk];
+    X.pb = hb ? nullptr : TB;
+    X.kb = bk;
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void tile_point_store(const TilePoint<R>& X, const R (&F)[5]) {
+  if (X.pa) {
+#pragma unroll
+    for (int kk = 0; kk < 5; ++kk) X.pa[kk * X.ka] = X.zero ? R(0) : -X.w * F[kk];
+  }
+  if (X.pb) {
+#pragma unroll
+    for (int kk = 0; kk < 5; ++kk) X.pb[kk * X.kb] = X.w * F[kk];
+  }
+}
+
 // Face evaluations of axis ax, point by point over the CTA (one copy of the
 // pointwise code for all three axes).
 template <int P, typename R>
 __device__ __forceinline__ void tile_fluxes(const RhsParams& prm, const HexTile& T, int ax, R* sT,
-                                            R* sH, const unsigned char (*perm)[(P + 2) * (P + 2)],
+                                            R* sH, const R (*eg)[4],
+                                            const unsigned char (*perm)[(P + 2) * (P + 2)],
                                             const unsigned char (*fab)[(P + 2) * (P + 2)],
                                             const R* wf, R& lmax) {
   using S = TileSize<P>;
-  constexpr int NQF = S::NQF, NEQ = S::NEQ, NT = S::NT, TS = S::TS, HS = S::HS;
+  constexpr int NQF = S::NQF, NT = S::NT;
   const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
-  const int nev = T.nev[ax];
+  const int npt = T.nev[ax] * NQF;
 #pragma unroll 1
-  for (int pt = threadIdx.x; pt < nev * NQF; pt += NT) {
-    const int j = pt / NQF, q = pt - j * NQF;
-    const unsigned d = T.ev[ax][j];
-    const int ia = d & 63, ib = (d >> 7) & 63;
-    const bool ha = (d >> 6) & 1, hb = (d >> 13) & 1, bnd = (d >> 14) & 1;
-    const int lfa = (d >> 15) & 7, lfb = (d >> 18) & 7, pid = (d >> 21) & 7;
-    const bool gb = (d >> 24) & 1;
-    // a side's value of variable kk at tensor point t: X[kk * xk + t * xq]
-    R* TA = ha ? sH + ia : sT + (ia & 1) * (NEQ * NQF * TS) + (ia >> 1);
-    R* TB = hb ? sH + ib : sT + (ib & 1) * (NEQ * NQF * TS) + (ib >> 1);
-    const int ak = ha ? NQF * HS : NQF * TS, aq = ha ? HS : TS;
-    const int bk = hb ? NQF * HS : NQF * TS, bq = hb ? HS : TS;
-    const int ge = T.el[(gb ? ib : ia) >> 1];  // element whose face geometry is read
-    const int glf = gb ? lfb : lfa;
-    const int qa = fab[lfa][q];
-    int nb = 0;
-    if (bnd) {
-      nb = prm.fnbr[glf * prm.ne + ge];
-      if (nb == -1) {  // no boundary integrator on this face: no face term
-#pragma unroll
-        for (int kk = 0; kk < NEQ; ++kk) TA[kk * ak + qa * aq] = R(0);
-        continue;
-      }
-    }
-    const R* fg = (const R*)prm.fgeo + (long long)(glf * 4) * prm.ne + ge;
-    R n[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) n[c] = __ldg(fg + (long long)c * prm.ne);
-    const R jac = __ldg(fg + 3LL * prm.ne);
-    R s1[NEQ], s2[NEQ];
-#pragma unroll
-    for (int kk = 0; kk < NEQ; ++kk) s1[kk] = TA[kk * ak + qa * aq];
-    int qb = 0;
-    if (bnd) {
-      const BCSlot& bc = prm.bc[-2 - nb];
-      right_state<3>(bc.type, bc.state, s1, s2, n, gamma, cov, (R)prm.rgas);
-    } else {
-      qb = fab[lfb][perm[pid][q]];
-#pragma unroll
-      for (int kk = 0; kk < NEQ; ++kk) s2[kk] = TB[kk * bk + qb * bq];
-    }
-    R F[NEQ];
-    const R sp = checked_speed(prm, riemann<3>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), ge);
-    lmax = fmax(lmax, sp);
-    const R w = wf[q] * jac;
-    if (!ha) {
-#pragma unroll
-      for (int kk = 0; kk < NEQ; ++kk) TA[kk * ak + qa * aq] = -w * F[kk];
-    }
-    if (!bnd && !hb) {
-#pragma unroll
-      for (int kk = 0; kk < NEQ; ++kk) TB[kk * bk + qb * bq] = w * F[kk];
-    }
+  for (int pt = threadIdx.x; pt < npt; pt += NT) {
+    TilePoint<R> A;
+    tile_point<P, R>(prm, T, ax, pt, sT, sH, eg, perm, fab, wf, gamma, cov, A);
+    R F[5];
+    const R sp = riemann<3>(A.s1, A.s2, A.n, F, gamma, cov, prm.rs, prm.avg);
+    if (!A.zero) lmax = fmax(lmax, checked_speed(prm, sp, A.ge));
+    tile_point_store(A, F);
   }
 }
 
@@ -207,6 +234,7 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ HexTile sTile;
   __shared__ R sGeo[E][10];  // per slot: adj(J) (row r, col d) and 1/det J
+  __shared__ R sEG[2 * E][4];  // per evaluation of the current axis: normal, |J_f|
   __shared__ unsigned char sPerm[RKDG_HEX_MAX_PERM][NQF];
   __shared__ unsigned char sFab[6][NQF];
   R* sm = reinterpret_cast<R*>(smraw);
@@ -227,10 +255,20 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
   __syncthreads();
   const int nel = sTile.nel;
   const long long NDa = prm.ndofs;
-  // stage the tile's DOFs: runs of ND contiguous values per (variable, element)
-  for (int f = tid; f < NEQ * E * ND; f += NT) {
-    const int k = f / (E * ND), r = f - k * (E * ND), el = r / ND, i = r - el * ND;
-    sU[f] = el < nel ? u[k * NDa + (long long)sTile.el[el] * ND + i] : R(0);
+  // stage the tile's DOFs (runs of ND contiguous values per variable and
+  // element): every thread issues all its loads before it stores any
+  {
+    constexpr int IT = NEQ * E * ND / NT;
+    static_assert(IT * NT == NEQ * E * ND, "whole rounds of the CTA");
+    R tmp[IT];
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      const int f = tid + it * NT;
+      const int k = f / (E * ND), r = f - k * (E * ND), el = r / ND, i = r - el * ND;
+      tmp[it] = el < nel ? __ldg(u + k * NDa + (long long)sTile.el[el] * ND + i) : R(0);
+    }
+#pragma unroll
+    for (int it = 0; it < IT; ++it) sU[tid + it * NT] = tmp[it];
   }
   for (int t = tid; t < nel * 10; t += NT) {
     const int sl = t / 10, c = t - sl * 10;
@@ -240,12 +278,10 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
   const int k = tid / E, el = tid - k * E;  // one variable per warp (E = 32)
   const bool act = el < nel;
   const int e = act ? sTile.el[el] : 0;
-  R uu[ND], acc[ND];
+  const R* su = sU + (k * E + el) * ND;  // this thread's staged values
+  R acc[ND];
 #pragma unroll
-  for (int i = 0; i < ND; ++i) {
-    uu[i] = sU[(k * E + el) * ND + i];
-    acc[i] = R(0);
-  }
+  for (int i = 0; i < ND; ++i) acc[i] = R(0);
   R lmax = R(0);
   R* row0 = sT + (0 * NEQ + k) * NQF * TS + el;
   R* row1 = sT + (1 * NEQ + k) * NQF * TS + el;
@@ -256,10 +292,20 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
     // the halo, one (variable, halo) per thread
     if (act) {
       switch (ax) {
-        case 0: tile_own_traces<P, TS, 0>(uu, H, row0, row1); break;
-        case 1: tile_own_traces<P, TS, 1>(uu, H, row0, row1); break;
-        default: tile_own_traces<P, TS, 2>(uu, H, row0, row1); break;
+        case 0: tile_own_traces<P, TS, 0>(su, H, row0, row1); break;
+        case 1: tile_own_traces<P, TS, 1>(su, H, row0, row1); break;
+        default: tile_own_traces<P, TS, 2>(su, H, row0, row1); break;
       }
+    }
+    // face geometry of the axis's evaluations (Elem1-outward normal, |J_f|)
+    for (int j = tid; j < sTile.nev[ax]; j += NT) {
+      const unsigned d = sTile.ev[ax][j];
+      const bool gb = (d >> 24) & 1;
+      const int ge = sTile.el[(gb ? (d >> 7) & 63 : d & 63) >> 1];
+      const int glf = gb ? (d >> 18) & 7 : (d >> 15) & 7;
+      const R* fg = (const R*)prm.fgeo + (long long)(glf * 4) * ne + ge;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) sEG[j][c] = __ldg(fg + (long long)c * ne);
     }
     const int nh = sTile.nh[ax];
     for (int j = tid; j < nh * NEQ; j += NT) {
@@ -269,7 +315,7 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
     }
     __syncthreads();
     // 2. every face of the axis once
-    tile_fluxes<P, R>(prm, sTile, ax, sT, sH, sPerm, sFab, H.wf, lmax);
+    tile_fluxes<P, R>(prm, sTile, ax, sT, sH, sEG, sPerm, sFab, H.wf, lmax);
     __syncthreads();
     // 3. lifting of the thread's two faces
     if (act && !prm.faces_only) {

@@ -730,7 +730,7 @@ int rkdg_set_physics(rkdg_ctx* c, int rsolver, int averaging, double gamma, doub
 
 int rkdg_set_bc(rkdg_ctx* c, int attr, int type, const double* state) {
   if (!c) return RKDG_ERR_INVALID;
-  if (type < 0 || type > 9 || attr < 1) return fail(c, RKDG_ERR_INVALID, "invalid boundary condition");
+  if (type < 0 || type > 10 || attr < 1) return fail(c, RKDG_ERR_INVALID, "invalid boundary condition");
   if ((type == RKDG_BC_FIXED_ROTATED || type == RKDG_BC_SUPERSONIC_INLET || type >= 5) && !state)
     return fail(c, RKDG_ERR_INVALID, "this boundary condition needs a state or its parameters");
   if (!c->bcs.count(attr) && (int)c->bcs.size() >= RKDG_MAX_BC)

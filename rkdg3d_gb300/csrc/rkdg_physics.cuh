@@ -517,6 +517,30 @@ __device__ __forceinline__ void right_state(int type, const double* st, const R*
 #pragma unroll
     for (int d = 0; d < DIM; d++) s2[1 + d] = s1[1 + d] * fdv(rho, s1[0]);
     s2[0] = rho;
+  } else if (type == 10) {
+    // charOutlet (boundary_integrator_char_outlet.cpp:14-57) with the ghost
+    // vector entering as the interior state (the reference reads the previous
+    // boundary point's ghost state there); st is the outer state
+    R fx[NEQ];
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) fx[i] = (R)st[i];
+    const R cOut = sound_speed_p<DIM>(fx, pressure<DIM>(fx, gamma, b), gamma, b);
+    const R UOut = fdv(fx[1], fx[0]);
+    const R cIn = sound_speed_p<DIM>(s1, pressure<DIM>(s1, gamma, b), gamma, b);
+    rotate<DIM>(s2, n);
+    const R UIn = fdv(s2[1], s2[0]);
+    const R UB = R(0.5) * (UIn + UOut) - fdv(cOut - cIn, gamma - R(1));
+    const R cB = R(-0.25) * (gamma - R(1)) * (UOut - UIn) + R(0.5) * (cOut + cIn);
+    const R sB = s2[1] < R(0) ? fdv(fdv(cOut * cOut, powr(fx[0], gamma - R(1))), gamma)
+                              : fdv(fdv(cIn * cIn, powr(s2[0], gamma - R(1))), gamma);
+    const R rhoB = powr(fdv(fdv(cB * cB, sB), gamma), fdv(R(1), gamma - R(1)));
+    const R pB = fdv(rhoB * cB * cB, gamma);
+    s2[0] = rhoB;
+    s2[1] = UB;  // a velocity in the momentum slot, as the reference stores it
+    const R v = fdv(s2[2], s2[0]);
+    const R w = DIM == 3 ? fdv(s2[DIM == 3 ? 3 : 2], s2[0]) : R(0);
+    s2[NEQ - 1] = fdv(pB, gamma - R(1)) * (R(1) - rhoB * b) + R(0.5) * rhoB * (UB * UB + v * v + w * w);
+    inverse_rotate<DIM>(s2, n);
   }
 }
 

@@ -37,6 +37,10 @@ BC_SLIP, BC_OPEN, BC_FIXED_ROTATED, BC_SUPERSONIC_INLET, BC_WALL = 0, 1, 2, 3, 4
 # parameters in state: {pTot, TTot}, {pFix, TTot}, {pFix}, {pTot, TFix}
 (BC_SUBSONIC_INLET, BC_SUBSONIC_INLET_TOTAL_PRESSURE, BC_SUBSONIC_INLET_FIXED_PRESSURE,
  BC_FIXED_PRESSURE_OUTLET, BC_TOTAL_PRESSURE_OUTLET) = 5, 6, 7, 8, 9
+# characteristic outlet, state = the outer conservative state (the ghost state
+# enters its computation as the interior state, where the reference reads the
+# previous boundary point's)
+BC_CHAR_OUTLET = 10
 LIM_FINDIFF, LIM_MULTI = 0, 1
 IND_NOWHERE, IND_EVERYWHERE, IND_BJ, IND_SHU = 0, 1, 2, 3
 FUN_BJ, FUN_VENKATAKRISHNAN, FUN_MICHALAK = 0, 1, 2

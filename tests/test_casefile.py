@@ -154,7 +154,6 @@ def test_initial_field_known_answers():
 
 @pytest.mark.parametrize("edit,msg", [
     (("spatial", "limiter", "type", "BJ"), "limiter type"),
-    (("boundaryField", "right", "type", "charOutlet"), "charOutlet"),
     (("boundaryField", "right", "type", "subsonicInlet"), "boundary condition type"),
     (("mesh", "adaptive", None, 1), "adaptive"),
     (("time", "order", None, 4), "time order"),
@@ -169,6 +168,19 @@ def test_refusals(tube, edit, msg):
         s[a][b][c] = val
     with pytest.raises(CF.CaseError, match=msg):
         CF.load_case(tube, s)
+
+
+def test_char_outlet_factory(tube):
+    """charOutlet (case_manager.cpp:779-802): the outer state from rhoI, UI,
+    pI; the energy omits the third velocity component, and in 2D it takes the
+    slot the reference first fills with rho w."""
+    from rkdg3d_gb300.solver import BC_CHAR_OUTLET
+    s = CF.read_settings(os.path.join(tube, "settings.yml"))
+    s["boundaryField"]["right"] = {"type": "charOutlet", "rhoI": 0.8, "UI": [0.3, 0.1, 0.2], "pI": 0.7}
+    case = CF.load_case(tube, s)
+    t, st = [(t, st) for a, t, st in case.bcs if t == BC_CHAR_OUTLET][0]
+    rho, u, v = 0.8, 0.3, 0.1
+    assert np.allclose(st, [rho, rho * u, rho * v, 0.7 / 0.4 + 0.5 * rho * (u * u + v * v)], rtol=1e-15)
 
 
 def test_serial_refinement(tube):

@@ -72,12 +72,15 @@ def test_rhs_vjp_fd(cuda, geom, order, rs, walled):
 
 
 @pytest.mark.parametrize("bc,params", [(6, [1.2, 1.1]), (7, [0.9, 1.1]), (8, [0.95]),
-                                       (9, [1.1, 1.0])])
+                                       (9, [1.1, 1.0]), (10, None)])
 @pytest.mark.parametrize("geom", [M.GEOM_SQUARE, M.GEOM_CUBE])
 def test_rhs_vjp_pressure_bcs_fd(cuda, bc, params, geom):
-    """Subsonic inlets and pressure outlets (their ghost states through dual
-    numbers) on every side of a box."""
+    """Subsonic inlets, pressure outlets and the characteristic outlet
+    (their ghost states through dual numbers) on every side of a box."""
     case = walled_case(geom, 3, 1, RS_HLLC, bc=bc)
+    if params is None:  # the characteristic outlet's outer state
+        dim = case.dim
+        params = [0.9, 0.18, -0.045] + ([0.027] if dim == 3 else []) + [2.05]
     case.bcs = [(a, bc, params) for a, _, _ in case.bcs]
     ctx = ctx_for(case)
     x = random_state(ctx.node_coords(), seed=4, amp=0.1, vel=0.2)

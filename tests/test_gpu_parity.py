@@ -15,7 +15,8 @@ from rkdg3d_gb300.solver import (AVG_EINFELDT, AVG_TRRS, BC_FIXED_PRESSURE_OUTLE
                                  BC_FIXED_ROTATED, BC_OPEN, BC_SLIP, BC_SUBSONIC_INLET,
                                  BC_SUBSONIC_INLET_FIXED_PRESSURE,
                                  BC_SUBSONIC_INLET_TOTAL_PRESSURE, BC_SUPERSONIC_INLET,
-                                 BC_TOTAL_PRESSURE_OUTLET, FUN_BJ, FUN_MICHALAK, FUN_VENKATAKRISHNAN,
+                                 BC_TOTAL_PRESSURE_OUTLET, BC_CHAR_OUTLET, FUN_BJ, FUN_MICHALAK,
+                                 FUN_VENKATAKRISHNAN,
                                  IND_BJ, IND_EVERYWHERE, IND_NOWHERE, LIM_FINDIFF, LIM_MULTI,
                                  RS_HLL, RS_HLLC, RS_LLF, RS_RUSANOV, TABLEAU_REFERENCE_RK3,
                                  TABLEAU_SSPRK3, Context, IND_SHU)
@@ -100,7 +101,7 @@ BC_PARAMS = {BC_SUBSONIC_INLET_TOTAL_PRESSURE: [1.2, 1.1], BC_SUBSONIC_INLET_FIX
 @pytest.mark.parametrize("bc", [BC_SLIP, BC_OPEN, BC_FIXED_ROTATED, BC_SUPERSONIC_INLET,
                                 BC_SUBSONIC_INLET, BC_SUBSONIC_INLET_TOTAL_PRESSURE,
                                 BC_SUBSONIC_INLET_FIXED_PRESSURE, BC_FIXED_PRESSURE_OUTLET,
-                                BC_TOTAL_PRESSURE_OUTLET])
+                                BC_TOTAL_PRESSURE_OUTLET, BC_CHAR_OUTLET])
 @pytest.mark.parametrize("rs,avg", [(RS_HLLC, AVG_EINFELDT), (RS_HLL, AVG_TRRS), (RS_RUSANOV, 0)])
 def test_rhs_walls(cuda, geom, order, n, bc, rs, avg):
     case = walled_case(geom, n, order, rs, avg, covolume=0.005, bc=bc)
@@ -112,6 +113,11 @@ def test_rhs_walls(cuda, geom, order, n, bc, rs, avg):
         # a subsonic inflow state in the face frame (2 * fixed - own stays physical)
         vel = [np.array([-0.1]), np.array([0.05])] + ([np.array([0.02])] if dim == 3 else [])
         st = cases.conservative([np.array([1.0]), *vel, np.array([1.0])], 1.4, 0.0).ravel()
+        case.bcs = [(a, bc, st) for a, _, _ in case.bcs]
+    elif bc == BC_CHAR_OUTLET:
+        # outer state of the characteristic outlet (conservative)
+        vel = [np.array([0.2]), np.array([-0.05])] + ([np.array([0.03])] if dim == 3 else [])
+        st = cases.conservative([np.array([0.9]), *vel, np.array([0.8])], 1.4, 0.005).ravel()
         case.bcs = [(a, bc, st) for a, _, _ in case.bcs]
     elif bc in BC_PARAMS:
         case.bcs = [(a, bc, BC_PARAMS[bc]) for a, _, _ in case.bcs]

@@ -67,6 +67,8 @@ def test_reference_library_reproduces_fixture(dim, eos):
     for bc in range(10):
         prm = g[f"{key}/bc{bc}/prm"] if f"{key}/bc{bc}/prm" in g else None
         assert np.array_equal(refpin.right_state(bc, s1, bnor, prm=prm), g[f"{key}/bc{bc}"])
+    outer = g[f"{key}/bc/outer"]
+    assert np.array_equal(refpin.right_state(10, s1, bnor, prm=outer, s2_in=s1), g[f"{key}/bc10"])
 
 
 @pytest.mark.parametrize("dim,eos", KEYS, ids=IDS)
@@ -110,15 +112,19 @@ def test_oracle_riemann_matches_reference(dim, eos, rs):
 
 
 BC_NAMES = ["slip", "open", "constant", "supersonic_inlet", "wall", "subsonic_inlet",
-            "subsonic_inlet_total_p", "subsonic_inlet_fixed_p", "fixed_p_outlet", "total_p_outlet"]
+            "subsonic_inlet_total_p", "subsonic_inlet_fixed_p", "fixed_p_outlet", "total_p_outlet",
+            "char_outlet"]
 
 
-@pytest.mark.parametrize("bc", range(10), ids=BC_NAMES)
+@pytest.mark.parametrize("bc", range(11), ids=BC_NAMES)
 @pytest.mark.parametrize("dim,eos", KEYS, ids=IDS)
 def test_oracle_ghost_states_match_reference(dim, eos, bc):
-    """computeRightState of every boundary condition of the factory (but the
-    characteristic outlet).  The total-pressure outlet reads the normal one
-    past its end (nor[1..dim], boundary_integrator_open_total_pressure.cpp);
+    """computeRightState of every boundary condition of the factory.  The
+    characteristic outlet reads its ghost vector before assigning it; the
+    library and the oracle let it enter as the interior state, and the
+    fixture called the reference's code with that entry value.  The
+    total-pressure outlet reads the normal one past its end (nor[1..dim],
+    boundary_integrator_open_total_pressure.cpp);
     the oracle forms m.n from the normal's own components, so it is compared
     where both give m.n the same sign (the only use of m.n)."""
     g = np.load(GOLD)
@@ -126,6 +132,8 @@ def test_oracle_ghost_states_match_reference(dim, eos, bc):
     _, gamma, b, R = eos
     o = _oracle(dim, gamma, b, R)
     prm = g[f"{key}/bc{bc}/prm"] if f"{key}/bc{bc}/prm" in g else None
+    if bc == 10:
+        prm = g[f"{key}/bc/outer"]
     o.set_bc(1, bc, prm)
     s1, nor, ref = g[f"{key}/bc/s1"], g[f"{key}/bc/nor"], g[f"{key}/bc{bc}"]
     keep = np.ones(len(s1), bool)
