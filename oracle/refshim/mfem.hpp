@@ -1,6 +1,8 @@
 // Test-only stand-in for the few pieces of MFEM's interface that the
 // reference's pointwise physics, Riemann-solver and boundary-state sources
-// use (physics/physics.cpp, riemannsolvers/rs_*.cpp, bc/boundary_integrator_*.cpp).
+// use (physics/physics.cpp, riemannsolvers/rs_*.cpp, bc/boundary_integrator_*.cpp),
+// and that the library's MFEM adapter (rkdg3d_gb300/adapters/mfem) uses:
+// the adapter is compile-checked against it (tests/test_mfem_adapter.py).
 //
 // It exists so that those reference files compile UNMODIFIED into
 // oracle/_ref/librefpin.so (recipe: oracle/Makefile, target `ref`), which the
@@ -25,6 +27,7 @@
 #include <cstring>
 #include <iostream>
 #include <limits>
+#include <vector>
 
 #define MFEM_ASSERT(cond, msg) ((void)0)
 
@@ -76,6 +79,10 @@ class Vector {
     for (int i = 0; i < size_; ++i) data_[i] *= a;
     return *this;
   }
+  // MFEM's memory-manager accessors (here: the host data)
+  const double* Read(bool on_dev = true) const { (void)on_dev; return data_; }
+  double* Write(bool on_dev = true) { (void)on_dev; return data_; }
+  double* ReadWrite(bool on_dev = true) { (void)on_dev; return data_; }
   double Norml2() const {
     double s = 0;
     for (int i = 0; i < size_; ++i) s += data_[i] * data_[i];
@@ -171,6 +178,7 @@ class FiniteElement {
 
 struct ElementTransformation {
   int OrderW() const { return 0; }
+  void Transform(const IntegrationPoint&, Vector& x) { x = 0.0; }
   const DenseMatrix& Jacobian() { return J_; }
   void SetIntPoint(const IntegrationPoint*) {}
   DenseMatrix J_;
@@ -193,6 +201,78 @@ inline void CalcOrtho(const DenseMatrix&, Vector&) {}
 class NonlinearFormIntegrator {
  public:
   virtual ~NonlinearFormIntegrator() = default;
+};
+
+// ---- what the adapter uses (declared for compilation) -------------------------
+template <class T>
+class Array {
+ public:
+  int Size() const { return (int)v_.size(); }
+  void SetSize(int n) { v_.resize(n); }
+  T& operator[](int i) { return v_[i]; }
+  const T& operator[](int i) const { return v_[i]; }
+  T* GetData() { return v_.data(); }
+
+ private:
+  std::vector<T> v_;
+};
+
+class Geometry {
+ public:
+  enum Type { INVALID = -1, POINT = 0, SEGMENT, TRIANGLE, SQUARE, TETRAHEDRON, CUBE };
+  static constexpr int NumVerts[8] = {1, 2, 3, 4, 4, 8, 6, 5};
+  const IntegrationRule* GetVertices(int) const { return &r_; }
+
+ private:
+  IntegrationRule r_;
+};
+inline Geometry Geometries;
+
+class Mesh {
+ public:
+  int Dimension() const { return 0; }
+  int GetNE() const { return 0; }
+  Geometry::Type GetElementBaseGeometry(int) const { return Geometry::SQUARE; }
+  void GetElementVertices(int, Array<int>& v) const { v.SetSize(0); }
+  ElementTransformation* GetElementTransformation(int) { return &T_; }
+  int GetNBE() const { return 0; }
+  void GetBdrElementVertices(int, Array<int>& v) const { v.SetSize(0); }
+  int GetBdrAttribute(int) const { return 1; }
+
+ private:
+  ElementTransformation T_;
+};
+
+class Operator {
+ public:
+  explicit Operator(int s = 0) : height(s), width(s) {}
+  virtual ~Operator() = default;
+  int Height() const { return height; }
+  int Width() const { return width; }
+  virtual void Mult(const Vector& x, Vector& y) const = 0;
+
+ protected:
+  int height, width;
+};
+
+class TimeDependentOperator : public Operator {
+ public:
+  explicit TimeDependentOperator(int n = 0, double t_ = 0.0) : Operator(n), t(t_) {}
+  virtual void SetTime(double t_) { t = t_; }
+  double GetTime() const { return t; }
+
+ protected:
+  double t;
+};
+
+class ODESolver {
+ public:
+  virtual ~ODESolver() = default;
+  virtual void Init(TimeDependentOperator& f_) { f = &f_; }
+  virtual void Step(Vector& x, double& t, double& dt) = 0;
+
+ protected:
+  TimeDependentOperator* f = nullptr;
 };
 
 }  // namespace mfem
