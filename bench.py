@@ -153,6 +153,18 @@ def barrier_max(val, world):
     return float(t.item())
 
 
+def _peak_hbm():
+    """Measured HBM bandwidth of the GB300s (MEASURED_PEAKS.json),
+    else the fallback figure; (GB/s, source)."""
+    try:
+        v = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+        if v:
+            return float(v), "measured"
+    except Exception:
+        pass
+    return 6800.0, "fallback"
+
+
 def oracle_rate(case, x0, dt, steps, threads):
     """Reference CPU algorithm (FP64 oracle) on the full mesh for `steps`
     Runge-Kutta steps; returns (rate, seconds)."""
@@ -316,7 +328,9 @@ def run_ours(args, rank, world, local):
             "traffic": args.traffic_per_launch or TRAFFIC_BYTES_PER_ELEMENT_LAUNCH * ctx32.ne,
             "traffic_source": "ncu dram bytes, 48^3 capture scaled by elements"
                               if not args.traffic_per_launch else "command line",
-            "peak_source": peak_src, "kernel": "k_rhs_hex_team<2,float,0> (fused stage kernel, 3 launches per step)",
+            "peak_source": peak_src,
+            "kernel": ("k_rhs_hex_tile<2,float> (face-once tiled stage kernel, 3 launches per step)"
+                       if args.hex_kernel in (0, 5) else f"hexahedral kernel variant {args.hex_kernel}"),
             "algorithmic_bytes_per_launch": bps / STAGES}
 
     cpu = None
@@ -418,6 +432,24 @@ def run_config(args, local):
             n, nd = ctx.n, ctx.ndofs
         line["unknowns"] = n
         line["error_fp32_bulk_vs_fp64"] = errors(out["fp32_bulk"][0], out["fp64"][0], nd)
+        # at matched step counts: dt fixed from the FP64 CFL evaluation of the
+        # initial state, the same in both arms; and the FP64 path's own spread
+        # when its initial state is perturbed by 1e-7 (FP32 rounding) relative
+        matched = {}
+        for name, prec, pert in (("fp64", FP64, 0.0), ("fp32_bulk", FP32_BULK, 0.0),
+                                 ("fp64_perturbed_1e-7", FP64, 1e-7)):
+            ctx = context(case, prec)
+            xh = cases.project(case, ctx.node_coords())
+            if pert:
+                xh = xh * (1.0 + pert * np.random.default_rng(1).uniform(-1, 1, xh.size))
+            x = torch.tensor(xh, dtype=torch.float64, device=dev)
+            inf = ctx.run(x, case.t_end, case.cfl, dt_mode=1, **kw)
+            matched[name] = (x.cpu().numpy(), inf["steps"])
+        line["matched_steps"] = {
+            "steps": matched["fp64"][1], "dt": "fixed from the FP64 CFL of the initial state",
+            "fp32_bulk_vs_fp64": errors(matched["fp32_bulk"][0], matched["fp64"][0], nd),
+            "fp64_perturbed_1e-7_vs_fp64": errors(matched["fp64_perturbed_1e-7"][0],
+                                                  matched["fp64"][0], nd)}
         orc = refcpu.Oracle(case.mesh, case.order)
         cases.configure_oracle(case, orc)
         xo = cases.project(case, orc.node_coords())
@@ -444,7 +476,24 @@ def run_config(args, local):
             units = float((per_problem * steps).sum()) * STAGES
             line[name] = {"value": units / sec, "seconds": sec, "problems": len(steps),
                           "failed": int((np.asarray(info["steps"]) < 0).sum()),
-                          "max_steps": int(steps.max())}
+                          "max_steps": int(steps.max()),
+                          "active_fraction": float((np.diff(bc.offsets) * steps).sum() /
+                                                   (bc.mesh.num_elements * steps.max()))}
+            if prec == FP32_BULK:
+                # algorithmic bytes of the problems' own steps (stored widths):
+                # the stage kernel's state streams (68 N per RK step, as the
+                # C2 accounting), the limiter's read and write of each stage
+                # output (8 N + 8 N + 16 N), and the cell means (8 B written,
+                # read by the element and its 4 neighbours, per variable, stage
+                # and element)
+                ne_p = np.diff(bc.offsets)
+                bytes_p = 100.0 * per_problem + 3 * 48.0 * 4 * ne_p
+                achieved = float((bytes_p * steps).sum()) / sec / 1e9
+                peak = _peak_hbm()
+                line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak[0],
+                                    "unit": "GB/s", "frac": achieved / peak[0], "peak_source": peak[1],
+                                    "note": "whole batched run: algorithmic bytes of the active "
+                                            "problems' steps / run time"}
             if name == "fp64":
                 a64 = x.cpu().numpy()
                 ok64 = np.asarray(info["steps"]) > 0
@@ -458,6 +507,32 @@ def run_config(args, local):
                 line["error_fp32_bulk_vs_fp64"] = errors(x.cpu().numpy()[sel], a64[sel], int(keep.sum()))
                 line["error_fp32_bulk_vs_fp64"]["problems_compared"] = int(ok.sum())
         line["unknowns"] = int(ctx.n)
+        # matched step counts: dt fixed per problem from the FP64 CFL of its
+        # initial state (the same in both arms), and the FP64 path's spread
+        # under a 1e-7 relative perturbation of the initial state
+        matched = {}
+        for name, prec, pert in (("fp64", FP64, 0.0), ("fp32_bulk", FP32_BULK, 0.0),
+                                 ("fp64_perturbed_1e-7", FP64, 1e-7)):
+            ctx = Context(bc.mesh, bc.order, device=local, precision=prec)
+            cases.configure_batch(bc, ctx)
+            ctx.set_stream(stream.cuda_stream)
+            xh = bc.project(ctx.node_coords())
+            if pert:
+                xh = xh * (1.0 + pert * np.random.default_rng(1).uniform(-1, 1, xh.size))
+            x = torch.tensor(xh, dtype=torch.float64, device=dev)
+            inf = ctx.batch_run(x, bc.t_end, bc.cfl, dt_mode=1)
+            matched[name] = (x.cpu().numpy(), np.asarray(inf["steps"]))
+        okm = np.all([m[1] > 0 for m in matched.values()], axis=0)
+        keep = np.repeat(okm, np.diff(bc.offsets) * 4)
+        sel = np.concatenate([keep] * 4)
+        nk = int(keep.sum())
+        line["matched_steps"] = {
+            "dt": "fixed per problem from the FP64 CFL of its initial state",
+            "problems_compared": int(okm.sum()),
+            "steps_equal": bool(np.array_equal(matched["fp64"][1], matched["fp32_bulk"][1])),
+            "fp32_bulk_vs_fp64": errors(matched["fp32_bulk"][0][sel], matched["fp64"][0][sel], nk),
+            "fp64_perturbed_1e-7_vs_fp64": errors(matched["fp64_perturbed_1e-7"][0][sel],
+                                                  matched["fp64"][0][sel], nk)}
         small = int(np.argmin(np.diff(bc.offsets)))
         c = bc.cases[small]
         orc = refcpu.Oracle(c.mesh, c.order)

@@ -198,6 +198,7 @@ struct RhsParams {
   const HexTeamSched* hsched;  // shared-face hexahedral kernel: one entry per CTA (or null)
   const HexTile* htile;        // face-once tiled hexahedral kernel: one entry per CTA (or null)
   int ntile;
+  int tile_hs;                 // its halo-buffer stride: the largest halo list, odd
   // nonconforming meshes: element -> row of xface (-1: none) and the face
   // terms of the hanging faces, [row][neq][nd] in the kernel's precision,
   // added to the element's face + volume terms before the inverse mass

@@ -68,9 +68,10 @@ static cudaError_t launch_hex_shared(const RhsParams& prm, const R* u, const Epi
   return launch_hex_team_mode<P, R, 3>(prm, u, ep, st);
 }
 
-// Defaults (64^3 periodic pulse on a GB300, per RK step): FP32 -- the fused
-// team kernel (Q1 1.39 ms against 1.57 split and 1.42 shared-face; Q2 3.20
-// ms against 3.25 shared-face); FP64 Q1 -- face pass + element pass, whose
+// Defaults (64^3 periodic pulse on a GB300, per RK step): FP32 Q2 -- the
+// face-once tiled kernel (2.39 ms against 3.15 for the fused team kernel);
+// FP32 Q1 -- the fused team kernel (1.39 ms against 1.57 split and 1.42
+// shared-face); FP64 Q1 -- face pass + element pass, whose
 // FP64 fluxes are evaluated once per face (21.6 ms against 27.4 shared-face
 // and 36.3 fused; the fused kernel where the context holds no flux slots);
 // FP64 Q2 -- shared-face rounds (55.7 ms against 68.3 fused and 125.5 warp
@@ -87,6 +88,7 @@ cudaError_t launch_rhs_t<5, 2>(int prec, const RhsParams& prm, const void* u, co
                                cudaStream_t st) {
   if (prec == 0)
     return launch_hex_shared<2, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st);
+  if (prm.htile) return launch_hex_tile(2, 1, prm, u, ep, st);
   return launch_hex_team<2, float>(prm, (const float*)u, *(const EpiParams<float>*)ep, st);
 }
 

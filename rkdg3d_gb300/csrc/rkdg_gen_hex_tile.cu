@@ -9,11 +9,12 @@ template <int P, typename R>
 static cudaError_t launch_tile(const RhsParams& prm, const R* u, const EpiParams<R>& ep,
                                cudaStream_t st) {
   using S = TileSize<P>;
-  const size_t smem = S::template smem_bytes<R>();
+  if (prm.tile_hs < 1 || prm.tile_hs > RKDG_TILE_HMAX + 1) return cudaErrorInvalidValue;
+  const size_t smem = S::template smem_bytes<R>(prm.tile_hs);
   static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_rhs_hex_tile<P, R>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (!configured) {  // room for the largest halo stride
+    cudaError_t e = cudaFuncSetAttribute(k_rhs_hex_tile<P, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)S::template smem_bytes<R>(RKDG_TILE_HMAX + 1));
     if (e != cudaSuccess) return e;
     configured = true;
   }

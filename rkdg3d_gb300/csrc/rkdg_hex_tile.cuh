@@ -47,14 +47,15 @@ struct TileSize {
   // [2][NEQ][NQF][TS] (slot fastest, padded: the threads of a warp -- 32
   // slots -- store a trace point into distinct banks, and the 16 points of
   // one face, read by 16 threads, fall into distinct banks too); halo traces
-  // [NEQ][NQF][HS] likewise
-  static constexpr int TS = E + 1, HS = HM + 1;
-  static constexpr int OFF_T = NEQ * E * ND, OFF_H = OFF_T + 2 * NEQ * NQF * TS,
-                       TOTAL = OFF_H + NEQ * NQF * HS;
+  // [NEQ][NQF][hs] likewise, hs (odd) = the mesh's largest halo list, so
+  // that a structured mesh (32 halos on an axis of a 4 x 4 x 2 tile) keeps
+  // four CTAs of the FP32 kernel on an SM
+  static constexpr int TS = E + 1;
+  static constexpr int OFF_T = NEQ * E * ND, OFF_H = OFF_T + 2 * NEQ * NQF * TS;
   template <typename R>
-  static constexpr size_t smem_bytes() { return sizeof(R) * (size_t)TOTAL; }
+  static constexpr size_t smem_bytes(int hs) { return sizeof(R) * (size_t)(OFF_H + NEQ * NQF * hs); }
   template <typename R>
-  __host__ __device__ static constexpr int min_ctas() { return sizeof(R) == 4 ? 3 : 2; }
+  __host__ __device__ static constexpr int min_ctas() { return sizeof(R) == 4 ? 4 : 2; }
 };
 
 // Local face of axis AX on side SD (MFEM hexahedron numbering).
@@ -64,9 +65,9 @@ __host__ __device__ constexpr int hex_axis_face(int ax, int sd) {
 
 // Trace of an out-of-tile element's variable at the points of its local face
 // lfo (tensor order), read from global memory.
-template <int P, int ST, typename R>
+template <int P, typename R>
 __device__ __forceinline__ void tile_halo_trace(const R* __restrict__ src, int lfo, const R* l1d,
-                                                const R* lend, R* dst) {
+                                                const R* lend, R* dst, int st) {
   constexpr int N1 = P + 1, ND = N1 * N1 * N1, NF2 = N1 * N1;
   R nbv[ND];
   team_gather_any<P, true>(lfo, src, nbv);
@@ -79,7 +80,27 @@ __device__ __forceinline__ void tile_halo_trace(const R* __restrict__ src, int l
     for (int jn = 0; jn < N1; ++jn) s += lend[sd * N1 + jn] * nbv[r * N1 + jn];
     v[r] = s;
   }
-  team_interp<P, ST>(v, l1d, dst);
+  // 2D interpolation to the face points, tensor order a + NQ1*b at stride st
+  constexpr int NQ1 = P + 2;
+  R w[NQ1][N1];
+#pragma unroll
+  for (int a = 0; a < NQ1; ++a)
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1) {
+      R acc = R(0);
+#pragma unroll
+      for (int i0 = 0; i0 < N1; ++i0) acc += l1d[a * N1 + i0] * v[i0 * N1 + i1];
+      w[a][i1] = acc;
+    }
+#pragma unroll
+  for (int b = 0; b < NQ1; ++b)
+#pragma unroll
+    for (int a = 0; a < NQ1; ++a) {
+      R acc = R(0);
+#pragma unroll
+      for (int i1 = 0; i1 < N1; ++i1) acc += l1d[b * N1 + i1] * w[a][i1];
+      dst[(a + NQ1 * b) * st] = acc;
+    }
 }
 
 // Own traces (AX compile-time: the face pair and its tensor offsets) of the
@@ -120,7 +141,8 @@ __device__ __forceinline__ void tile_point(const RhsParams& prm, const HexTile& 
                                            const unsigned char (*fab)[(P + 2) * (P + 2)],
                                            const R* wf, R gamma, R cov, TilePoint<R>& X) {
   using S = TileSize<P>;
-  constexpr int NQF = S::NQF, NEQ = S::NEQ, TS = S::TS, HS = S::HS;
+  constexpr int NQF = S::NQF, NEQ = S::NEQ, TS = S::TS;
+  const int HS = prm.tile_hs;
   const int j = pt / NQF, q = pt - j * NQF;
   const unsigned d = T.ev[ax][j];
   const int ia = d & 63, ib = (d >> 7) & 63;
@@ -230,7 +252,8 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
                    const EpiParams<R> ep) {
   using S = TileSize<P>;
   constexpr int N1 = S::N1, ND = S::ND, NQF = S::NQF, NEQ = S::NEQ, E = S::E, NT = S::NT;
-  constexpr int TS = S::TS, HS = S::HS;
+  constexpr int TS = S::TS;
+  const int HS = prm.tile_hs;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ HexTile sTile;
   __shared__ R sGeo[E][10];  // per slot: adj(J) (row r, col d) and 1/det J
@@ -240,7 +263,7 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
   R* sm = reinterpret_cast<R*>(smraw);
   R* sU = sm;              // [NEQ][E][ND]; the right-hand side after the volume phase
   R* sT = sm + S::OFF_T;   // [2][NEQ][NQF][TS]
-  R* sH = sm + S::OFF_H;   // [NEQ][NQF][HS]
+  R* sH = sm + S::OFF_H;   // [NEQ][NQF][hs]
   const HexOps<R>& H = hex_ops<R>(prm.hops);
   const RefTables* RT = prm.tab;
   const int tid = threadIdx.x;
@@ -310,8 +333,8 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
     const int nh = sTile.nh[ax];
     for (int j = tid; j < nh * NEQ; j += NT) {
       const int kk = j / nh, h = j - kk * nh;
-      tile_halo_trace<P, HS, R>(u + kk * NDa + (long long)sTile.hel[ax][h] * ND, sTile.hlf[ax][h],
-                                H.l1d, H.lend, sH + kk * NQF * HS + h);
+      tile_halo_trace<P, R>(u + kk * NDa + (long long)sTile.hel[ax][h] * ND, sTile.hlf[ax][h],
+                            H.l1d, H.lend, sH + kk * NQF * HS + h, HS);
     }
     __syncthreads();
     // 2. every face of the axis once

@@ -56,6 +56,7 @@ struct rkdg_ctx {
   int hsched_rounds = 0;
   HexTile* d_htile = nullptr;  // tiles of the face-once hexahedral kernel
   int ntile = 0;
+  int tile_hs = 1;             // halo-buffer stride of its CTAs (odd)
   // hanging faces of a nonconforming mesh (see rkdg_nc.cu)
   int nnc = 0, nc_nel = 0;
   // non-parallelogram quadrilaterals: per-node adj(J) and 1/det J
@@ -309,6 +310,7 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   P.hsched = c->d_hsched;
   P.htile = c->d_htile;
   P.ntile = c->ntile;
+  P.tile_hs = c->tile_hs;
   P.ncidx = c->nnc ? c->d_ncidx : nullptr;
   P.xface = c->d_xface;
   P.ngeo = c->nonaffine ? (prec == 0 ? (const void*)c->d_ngeo64 : (const void*)c->d_ngeo32) : nullptr;
@@ -1259,6 +1261,10 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
       CUDA_TRY(c, dalloc(c->d_htile, ht.size()));
       CUDA_TRY(c, cudaMemcpy(c->d_htile, ht.data(), ht.size() * sizeof(HexTile), cudaMemcpyHostToDevice));
       c->ntile = (int)ht.size();
+      int mh = 1;
+      for (const HexTile& t : ht)
+        for (int a = 0; a < 3; ++a) mh = std::max(mh, t.nh[a]);
+      c->tile_hs = mh | 1;
     }
   }
   c->has_mesh = true;
