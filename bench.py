@@ -343,6 +343,18 @@ def run_ours(args, rank, world, local):
             cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"{ks} RK steps of the full {args.n}^3 mesh, FP64 oracle "
                              f"({sec:.1f} s)"}
+            # one thread, the reference's one-rank behaviour: one RK step of the
+            # same pulse on a 32^3 mesh (the rate per unknown does not depend
+            # on the mesh size for this element-local work)
+            small = cases.pulse3d(n=min(32, args.n), order=2, steps=1, cfl=0.2)
+            from oracle import refcpu
+            o1 = refcpu.Oracle(small.mesh, small.order)
+            cases.configure_oracle(small, o1)
+            xs = cases.project(small, o1.node_coords())
+            dts = 0.2 * o1.hmin() / o1.face_speed(xs) / 5.0
+            r1, s1 = oracle_rate(small, xs, dts, 1, 1)
+            cpu["one_thread"] = {"value": r1, "cores": 1,
+                                 "sample": f"1 RK step of the {min(32, args.n)}^3 pulse ({s1:.1f} s)"}
         except Exception as exc:  # pragma: no cover
             cpu = {"value": None, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"failed: {exc}"}
@@ -477,8 +489,8 @@ def run_config(args, local):
             line[name] = {"value": units / sec, "seconds": sec, "problems": len(steps),
                           "failed": int((np.asarray(info["steps"]) < 0).sum()),
                           "max_steps": int(steps.max()),
-                          "active_fraction": float((np.diff(bc.offsets) * steps).sum() /
-                                                   (bc.mesh.num_elements * steps.max()))}
+                          "active_fraction": float((np.diff(bc.offsets).astype(np.float64) * steps).sum()
+                                                   / (float(bc.mesh.num_elements) * float(steps.max())))}
             if prec == FP32_BULK:
                 # algorithmic bytes of the problems' own steps (stored widths):
                 # the stage kernel's state streams (68 N per RK step, as the

@@ -148,9 +148,10 @@ def gaussian_pulses_perturbed(n=32, order=1, seed=0, perturb_seed=1, scale=0.25,
     base = gaussian_pulses(n, order, seed, steps, cfl)
     pert = gaussian_pulses(n, order, perturb_seed, steps, cfl)
     gamma = base.gamma
+    base_ic, pert_ic = base.ic, pert.ic
 
     def ic(x):
-        rho = base.ic(x)[0] + scale * (pert.ic(x)[0] - 1.0)
+        rho = base_ic(x)[0] + scale * (pert_ic(x)[0] - 1.0)
         z = np.zeros_like(rho)
         return rho, z, z, z, rho ** gamma
 

@@ -193,6 +193,14 @@ struct RhsParams {
   const int* pactive;
   unsigned long long* pmcs;
   int* pfail;           // per-problem failure flag (non-physical state)
+  // batched problems, map of the active work (null: every element is
+  // launched and idle problems' elements exit): the active problems in
+  // order (act_pid[0 .. *act_n)), the exclusive prefix sums of their element
+  // counts (act_cum[0 .. *act_n]) and the problems' element offsets
+  const int* act_cum;
+  const int* act_pid;
+  const int* act_n;
+  const int* poff;
   int block;            // threads per CTA of the generic kernels (0: default)
   void* fslot;          // hexahedral face-pass flux slots [ne][6][neq][nqf] (or null)
   const HexTeamSched* hsched;  // shared-face hexahedral kernel: one entry per CTA (or null)
@@ -272,6 +280,10 @@ struct LimParams {
   const double* pgamma;
   const double* pcov;
   const int* pactive;
+  const int* act_cum;   // map of the active work (as RhsParams; or null)
+  const int* act_pid;
+  const int* act_n;
+  const int* poff;
   int block;            // threads per CTA (0: default)
   // hanging faces (nonconforming meshes; null otherwise): element -> CSR row
   // of its slave-face entries (2 * face + side) and the faces [nnc][4]
@@ -295,6 +307,11 @@ struct BatchState {
   int* nactive;         // [1]
   const unsigned long long* mcs_last;  // [nprob] max speed of the last stage
   int* fail;            // [nprob] set by the kernels on a non-physical state
+  // map of the active work, rebuilt after every step (see RhsParams)
+  int* act_cum;         // [nprob + 1]
+  int* act_pid;         // [nprob]
+  int* act_n;           // [1]
+  const int* poff;      // [nprob + 1] element offsets
 };
 
 }  // namespace rkdg

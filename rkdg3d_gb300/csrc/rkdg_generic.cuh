@@ -105,6 +105,22 @@ __device__ __forceinline__ void segmented_max_commit(double v, int pb,
   if (pb >= 0 && (lane == 0 || prev != pb)) atomic_max_nonneg(&pmcs[pb], v);
 }
 
+// Batched problems with a map of the active work: the i-th element of the
+// active problems (in problem order), and its problem pb.
+__device__ __forceinline__ int active_element(const int* cum, const int* pid, const int* poff, int na,
+                                              int i, int& pb) {
+  int lo = 0, hi = na;  // cum[lo] <= i < cum[lo + 1]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (cum[mid] <= i)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  pb = pid[lo];
+  return poff[pb] + (i - cum[lo]);
+}
+
 // Split c*s (c a tableau coefficient, s a problem's dt) into a float pair.
 __device__ __forceinline__ void split_scaled(double c, double s, float& hi, float& lo) {
   const double v = c * s;
@@ -202,6 +218,8 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
   __shared__ R sWm[ND];
   __shared__ unsigned char sPerm[RKDG_MAX_PERM][NQF];
   const RefTables* T = prm.tab;
+  // batched problems with a map of the active work: CTAs past it are idle
+  if (prm.act_cum && (int)(blockIdx.x * blockDim.x) >= prm.act_cum[*prm.act_n]) return;
   for (int t = threadIdx.x; t < NFPE * NQF * ND; t += blockDim.x) {
     const int s = t % ND, q = (t / ND) % NQF, lf = t / (ND * NQF);
     sB[lf][q][s] = (R)T->B[lf][q][s];
@@ -220,13 +238,18 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
   const int ne = prm.ne;
   const long long NDa = prm.ndofs;
   R gamma = (R)prm.gamma, cov = (R)prm.covolume;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
   R lmax = R(0);
   bool live = e < ne;
   int pb = -1;
   double dts = 1.0;
+  if (prm.act_cum) {
+    const int na = *prm.act_n;
+    live = e < prm.act_cum[na];
+    if (live) e = active_element(prm.act_cum, prm.act_pid, prm.poff, na, e, pb);
+  }
   if (live && prm.prob) {
-    pb = prm.prob[e];
+    if (!prm.act_cum) pb = prm.prob[e];
     live = prm.pactive[pb] != 0;
     gamma = (R)prm.pgamma[pb];
     cov = (R)prm.pcov[pb];
@@ -574,6 +597,8 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
   __shared__ double sBl[NFPE][NQL][ND];
   __shared__ R sBv[NV][ND];
   const RefTables* T = prm.tab;
+  // batched problems with a map of the active work: CTAs past it are idle
+  if (prm.act_cum && (int)(blockIdx.x * blockDim.x) >= prm.act_cum[*prm.act_n]) return;
   for (int t = threadIdx.x; t < NFPE * NQL * ND; t += blockDim.x) {
     const int s = t % ND, q = (t / ND) % NQL, lf = t / (ND * NQL);
     sBl[lf][q][s] = T->Bl[lf][q][s];
@@ -581,12 +606,18 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
   for (int t = threadIdx.x; t < NV * ND; t += blockDim.x) sBv[t / ND][t % ND] = (R)T->Bv[t / ND][t % ND];
   __syncthreads();
   const int ne = prm.ne;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  int pmap = -1;
+  if (prm.act_cum) {  // batched problems: the i-th element of the active ones
+    const int na = *prm.act_n;
+    if (e >= prm.act_cum[na]) return;
+    e = active_element(prm.act_cum, prm.act_pid, prm.poff, na, e, pmap);
+  }
   if (e >= ne) return;
   const long long NDa = prm.ndofs;
   R gamma = (R)prm.gamma, cov = (R)prm.covolume;
   if (prm.prob) {
-    const int pb = prm.prob[e];
+    const int pb = prm.act_cum ? pmap : prm.prob[e];
     if (!prm.pactive[pb]) return;
     gamma = (R)prm.pgamma[pb];
     cov = (R)prm.pcov[pb];

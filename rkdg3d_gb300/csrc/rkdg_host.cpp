@@ -124,6 +124,11 @@ struct rkdg_ctx {
   int* d_pactive = nullptr;
   int* d_psteps = nullptr;
   int* d_nactive = nullptr;
+  // map of the active work of a batched run (see RhsParams)
+  int* d_act_cum = nullptr;
+  int* d_act_pid = nullptr;
+  int* d_act_n = nullptr;
+  int* d_poff = nullptr;
   int* d_pfail = nullptr;
   unsigned long long* d_pmcs = nullptr;  // [4][nprob]
   // discrete adjoint scratch (FP64)
@@ -193,6 +198,10 @@ void free_mesh(rkdg_ctx* c) {
   dfree(c->d_pactive);
   dfree(c->d_psteps);
   dfree(c->d_nactive);
+  dfree(c->d_act_cum);
+  dfree(c->d_act_pid);
+  dfree(c->d_act_n);
+  dfree(c->d_poff);
   dfree(c->d_pfail);
   dfree(c->d_pmcs);
   dfree(c->d_adj);
@@ -393,6 +402,10 @@ void set_batch(rkdg_ctx* c, RhsParams& P, int slot) {
   P.pgamma = c->d_pgamma;
   P.pcov = c->d_pcov;
   P.pactive = c->d_pactive;
+  P.act_cum = c->d_act_cum;
+  P.act_pid = c->d_act_pid;
+  P.act_n = c->d_act_n;
+  P.poff = c->d_poff;
   P.pmcs = c->d_pmcs + (size_t)slot * c->nprob;
   P.pfail = c->d_pfail;
 }
@@ -472,6 +485,10 @@ LimParams lim_params_for(rkdg_ctx* c, bool batch) {
     L.pgamma = c->d_pgamma;
     L.pcov = c->d_pcov;
     L.pactive = c->d_pactive;
+    L.act_cum = c->d_act_cum;
+    L.act_pid = c->d_act_pid;
+    L.act_n = c->d_act_n;
+    L.poff = c->d_poff;
   }
   return L;
 }
@@ -1522,6 +1539,11 @@ int rkdg_batch_setup(rkdg_ctx* c, int nprob, const int* elem_offsets, const doub
   CUDA_TRY(c, dalloc(c->d_pactive, (size_t)nprob));
   CUDA_TRY(c, dalloc(c->d_psteps, (size_t)nprob));
   CUDA_TRY(c, dalloc(c->d_nactive, (size_t)1));
+  CUDA_TRY(c, dalloc(c->d_act_cum, (size_t)nprob + 1));
+  CUDA_TRY(c, dalloc(c->d_act_pid, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_act_n, (size_t)1));
+  CUDA_TRY(c, dalloc(c->d_poff, (size_t)nprob + 1));
+  CUDA_TRY(c, cudaMemcpy(c->d_poff, elem_offsets, (nprob + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CUDA_TRY(c, dalloc(c->d_pfail, (size_t)nprob));
   CUDA_TRY(c, dalloc(c->d_pmcs, (size_t)4 * nprob));
   CUDA_TRY(c, cudaMemcpy(c->d_prob, prob.data(), prob.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -1559,6 +1581,10 @@ int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0,
   bs.active = c->d_pactive;
   bs.steps = c->d_psteps;
   bs.nactive = c->d_nactive;
+  bs.act_cum = c->d_act_cum;
+  bs.act_pid = c->d_act_pid;
+  bs.act_n = c->d_act_n;
+  bs.poff = c->d_poff;
   bs.mcs_last = c->d_pmcs + (size_t)(c->s - 1) * np;
   bs.fail = c->d_pfail;
   CUDA_TRY(c, cudaMemsetAsync(c->d_pfail, 0, np * sizeof(int), c->stream));
@@ -1566,6 +1592,9 @@ int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0,
   {
     std::vector<int> ones(np, 1);
     CUDA_TRY(c, cudaMemcpyAsync(c->d_pactive, ones.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    // the map of the active work (every problem) before any batched launch
+    CUDA_TRY(c, rkdg::launch_batch_map(bs, c->stream));
+    c->launches++;
     // each problem's projected state is limited once first (main.cpp:264-265)
     if (c->limiter_active() && !(c->solver_quirks & RKDG_QUIRK_NO_INITIAL_LIMIT)) {
       CUDA_TRY(c, rkdg::launch_means(c->geom, c->p, 0, c->ne, c->ndofs, c->d_tab, x, nullptr, c->d_means, c->stream));
@@ -1580,7 +1609,7 @@ int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0,
     set_batch(c, P, c->s - 1);
     CUDA_TRY(c, launch_rhs_nc(c, 0, P, x, &ep));
     CUDA_TRY(c, rkdg::launch_batch_init(bs, dt0, c->stream));
-    c->launches += 2;
+    c->launches += 3;  // face speeds, per-problem dt, map of the active work
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   }
   if (fp32) {

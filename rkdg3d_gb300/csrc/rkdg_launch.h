@@ -47,6 +47,8 @@ cudaError_t launch_totals(int nd, int neq, int ne, long long ndofs, const RefTab
                           cudaStream_t st);
 
 cudaError_t launch_batch_init(const BatchState& bs, double dt0, cudaStream_t st);
+// Rebuild the map of the active work from the problems' active flags.
+cudaError_t launch_batch_map(const BatchState& bs, cudaStream_t st);
 cudaError_t launch_batch_control(const BatchState& bs, cudaGraphConditionalHandle h,
                                  int use_handle, cudaStream_t st);
 

@@ -69,8 +69,10 @@ __global__ void k_riemann_batch(int n, const double* u1, const double* u2, const
   for (int d = 0; d < DIM; ++d) nn[d] = (R)nor[(long long)i * DIM + d];
   const R sp = riemann<DIM>(s1, s2, nn, F, (R)gamma, (R)cov, rs, avg);
   speed[i] = (double)sp;
+  // -1 flags a non-physical state; HLLC's signed max(SL, SR) may be negative
+  // with a valid flux
 #pragma unroll
-  for (int k = 0; k < NEQ; ++k) flux[(long long)i * NEQ + k] = sp < R(0) ? 0.0 : (double)F[k];
+  for (int k = 0; k < NEQ; ++k) flux[(long long)i * NEQ + k] = sp == R(-1) ? 0.0 : (double)F[k];
 }
 
 cudaError_t launch_riemann_batch(int dim, int prec, int n, const double* u1, const double* u2,
@@ -178,6 +180,42 @@ __device__ __forceinline__ double bits_to_double(unsigned long long b) {
 
 // Initial dt per problem from its face-only max speed (main.cpp:467-484) or
 // the given constant, and the first step's dt_real.
+// Map of the active work for the stage kernels: the active problems in order
+// and the exclusive prefix sums of their element counts, by the first warp of
+// a single CTA (a warp scan over runs of 32 problems).
+__device__ void build_active_map(const BatchState& bs) {
+  if (!bs.act_cum || threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  int run = 0, na = 0;
+  for (int base = 0; base < bs.nprob; base += 32) {
+    const int p = base + lane;
+    const bool a = p < bs.nprob && bs.active[p];
+    const int sz = a ? bs.poff[p + 1] - bs.poff[p] : 0;
+    int cs = sz, cf = a ? 1 : 0;  // inclusive scans of sizes and of active flags
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int ts = __shfl_up_sync(0xffffffffu, cs, o);
+      const int tf = __shfl_up_sync(0xffffffffu, cf, o);
+      if (lane >= o) {
+        cs += ts;
+        cf += tf;
+      }
+    }
+    if (a) {
+      bs.act_pid[na + cf - 1] = p;
+      bs.act_cum[na + cf - 1] = run + cs - sz;
+    }
+    run += __shfl_sync(0xffffffffu, cs, 31);
+    na += __shfl_sync(0xffffffffu, cf, 31);
+  }
+  if (lane == 0) {
+    bs.act_cum[na] = run;
+    bs.act_n[0] = na;
+  }
+}
+
+__global__ void k_batch_map(BatchState bs) { build_active_map(bs); }
+
 __global__ void k_batch_init(BatchState bs, double dt0) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < bs.nprob; p += gridDim.x * blockDim.x) {
     double dt = dt0;
@@ -229,10 +267,16 @@ __global__ void k_batch_control(BatchState bs, cudaGraphConditionalHandle handle
     bs.nactive[0] = cnt;
     if (use_handle) cudaGraphSetConditional(handle, cnt > 0 ? 1u : 0u);
   }
+  build_active_map(bs);
 }
 
 cudaError_t launch_batch_init(const BatchState& bs, double dt0, cudaStream_t st) {
   k_batch_init<<<(bs.nprob + 127) / 128, 128, 0, st>>>(bs, dt0);
+  if (bs.act_cum) k_batch_map<<<1, 32, 0, st>>>(bs);
+  return cudaGetLastError();
+}
+cudaError_t launch_batch_map(const BatchState& bs, cudaStream_t st) {
+  k_batch_map<<<1, 32, 0, st>>>(bs);
   return cudaGetLastError();
 }
 cudaError_t launch_batch_control(const BatchState& bs, cudaGraphConditionalHandle h, int use_handle,

@@ -83,7 +83,8 @@ def test_rhs_vjp_pressure_bcs_fd(cuda, bc, params, geom):
         params = [1.0, 0.1, 0.0] + ([0.0] if dim == 3 else []) + [2.505]
     case.bcs = [(a, bc, params) for a, _, _ in case.bcs]
     ctx = ctx_for(case)
-    x = random_state(ctx.node_coords(), seed=4, amp=0.1, vel=0.2)
+    amp, vel = (0.05, 0.1) if bc == 10 else (0.1, 0.2)  # charOutlet ghost stays physical
+    x = random_state(ctx.node_coords(), seed=4, amp=amp, vel=vel)
 
     def apply(xx):
         y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
@@ -193,7 +194,8 @@ def test_adjoint_gradient_full_size(cuda):
     Each direction therefore picks its finite-difference step: the first two
     consecutive central differences of eps = 4e-6, 1e-6, 2.5e-7 that agree
     with each other to 1e-5 (no switch inside the window) assess it, and there
-    the adjoint must agree to 1e-5.  RKDG_ADJOINT_DIRECTIONS sets the number
+    the adjoint must agree to 1e-5 with their Richardson extrapolation.
+    RKDG_ADJOINT_DIRECTIONS sets the number
     of random directions (default 64); at least three quarters must be
     assessed."""
     import os
@@ -234,8 +236,11 @@ def test_adjoint_gradient_full_size(cuda):
         for e in (4e-6, 1e-6, 2.5e-7):
             fd = (J(x0 + e * v) - J(x0 - e * v)) / (2 * e)
             if prev is not None and abs(fd - prev) <= 1e-5 * abs(fd):
+                # central differences err by O(eps^2): Richardson's
+                # extrapolation of the pair (steps 4:1) removes that term
+                rich = (16.0 * fd - prev) / 15.0
                 assessed += 1
-                worst = max(worst, abs(ad - fd) / abs(fd))
+                worst = max(worst, abs(ad - rich) / abs(rich))
                 break
             prev = fd
     print(f"adjoint FD check: {assessed} of {ndir} directions assessed, worst relative error {worst:.2e}")

@@ -125,7 +125,11 @@ def test_rhs_walls(cuda, geom, order, n, bc, rs, avg):
     elif bc in BC_PARAMS:
         case.bcs = [(a, bc, BC_PARAMS[bc]) for a, _, _ in case.bcs]
     ctx, orc = pair(case)
-    x = random_state(ctx.node_coords(), b=0.005, seed=7)
+    # the characteristic outlet's ghost state (a linearised characteristic
+    # split) leaves the physical range for large interior departures from the
+    # outer state in 3D, where the reference stops as well: milder noise there
+    amp, vel = (0.05, 0.1) if bc == BC_CHAR_OUTLET else (0.15, 0.3)
+    x = random_state(ctx.node_coords(), b=0.005, seed=7, amp=amp, vel=vel)
     y_ref, m_ref = orc.rhs(x)
     y = torch.empty(ctx.n, dtype=torch.float64, device="cuda")
     m = ctx.rhs(dev(x), y)
