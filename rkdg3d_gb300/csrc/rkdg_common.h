@@ -4,6 +4,15 @@
 
 #include <cstdint>
 
+#if __has_include(<vector_types.h>)
+#include <vector_types.h>
+#else
+// host-only tools built without the CUDA headers (same layout as CUDA's)
+struct alignas(8) float2 {
+  float x, y;
+};
+#endif
+
 #define RKDG_MAX_ND 27    // hex Q2 = 27 nodes
 #define RKDG_MAX_NFPE 6
 #define RKDG_MAX_NQF 16   // hex Q2 face rule: 4x4
@@ -261,11 +270,28 @@ struct EpiParams {
   double ccur;
   float ccur_hi, ccur_lo;
   double* means;
+  // cell means of the FP32-bulk path as float pairs (hi, lo) whose sum is
+  // the mean; written instead of `means` when set
+  float2* means32;
   // batched problems: when pdt is set, cprev/ccur hold the unscaled tableau
   // coefficients and are multiplied by the problem's dt (pdt[prob[e]])
   const int* prob;
   const double* pdt;
 };
+
+#ifdef __CUDACC__
+// Store one cell mean: as a double, or as a normalised float pair (hi, lo)
+// where the FP32-bulk path asked for pairs.
+template <typename R>
+__device__ __forceinline__ void store_mean(const EpiParams<R>& ep, long long i, double m) {
+  if (ep.means32) {
+    const float h = (float)m;
+    ep.means32[i] = make_float2(h, (float)(m - (double)h));
+  } else {
+    ep.means[i] = m;
+  }
+}
+#endif
 
 struct LimParams {
   int ne;
@@ -274,6 +300,8 @@ struct LimParams {
   const RefTables* tab;
   const double* eaff;   // [dim*dim + dim][ne]: J (row i, col r) and vertex 0
   const double* means;  // [neq][ne]
+  // the FP32-bulk limiter's means: float pairs (the RHS epilogue's output)
+  const float2* means32;  // [neq][ne]
   double gamma, covolume;
   int limiter, indicator, function, last_hope, quirks;
   const int* prob;      // batched problems (or null)

@@ -39,6 +39,52 @@ __device__ __forceinline__ void ds_mul_f(float ch, float cl, float k, float& ph,
   pl = fmaf(ch, k, -ph) + cl * k;
 }
 
+// ---- vector access to the element rows of float arrays ------------------------
+// An element's ND values of one variable are contiguous (byNODES layout, offset
+// (k * ne + e) * ND).  The float arrays the FP32-bulk path reads and writes are
+// the library's own allocations (256-byte aligned), so a row is 16-byte
+// aligned when ND % 4 == 0 and 8-byte aligned when ND % 2 == 0.  Double
+// arrays may be the caller's and are accessed element by element.
+template <typename T, int ND>
+struct RowVec {
+  static constexpr int W = std::is_same<T, float>::value ? (ND % 4 == 0 ? 4 : (ND % 2 == 0 ? 2 : 1)) : 1;
+};
+template <int W, typename T>
+__device__ __forceinline__ void ld_vec(const T* __restrict__ p, T* v) {
+  if constexpr (W == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  } else if constexpr (W == 2) {
+    const float2 t = *reinterpret_cast<const float2*>(p);
+    v[0] = t.x; v[1] = t.y;
+  } else {
+    v[0] = p[0];
+  }
+}
+template <int W, typename T>
+__device__ __forceinline__ void st_vec(T* __restrict__ p, const T* v) {
+  if constexpr (W == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  } else if constexpr (W == 2) {
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+  } else {
+    p[0] = v[0];
+  }
+}
+// a whole row of N values
+template <int N, typename T>
+__device__ __forceinline__ void ld_row(const T* __restrict__ p, T* v) {
+  constexpr int W = RowVec<T, N>::W;
+#pragma unroll
+  for (int i = 0; i < N; i += W) ld_vec<W>(p + i, v + i);
+}
+template <int N, typename T>
+__device__ __forceinline__ void st_row(T* __restrict__ p, const T* v) {
+  constexpr int W = RowVec<T, N>::W;
+#pragma unroll
+  for (int i = 0; i < N; i += W) st_vec<W>(p + i, v + i);
+}
+
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
   if (!(v > 0.0)) return;
   atomicMax(addr, (unsigned long long)__double_as_longlong(v));
@@ -92,17 +138,17 @@ __device__ __forceinline__ R checked_speed(const RhsParams& prm, R sp, int e, in
 // Per-problem max wave speed for batched problems: elements of one problem
 // are contiguous, so a warp holds a few contiguous runs; a segmented shuffle
 // reduction leaves each run's max in its first lane, which commits it.
-__device__ __forceinline__ void segmented_max_commit(double v, int pb,
-                                                     unsigned long long* pmcs) {
+template <typename R>
+__device__ __forceinline__ void segmented_max_commit(R v, int pb, unsigned long long* pmcs) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
-    const double o = __shfl_down_sync(0xffffffffu, v, off);
+    const R o = __shfl_down_sync(0xffffffffu, v, off);
     const int opb = __shfl_down_sync(0xffffffffu, pb, off);
     if (lane + off < 32 && opb == pb) v = fmax(v, o);
   }
   const int prev = __shfl_up_sync(0xffffffffu, pb, 1);
-  if (pb >= 0 && (lane == 0 || prev != pb)) atomic_max_nonneg(&pmcs[pb], v);
+  if (pb >= 0 && (lane == 0 || prev != pb)) atomic_max_nonneg(&pmcs[pb], (double)v);
 }
 
 // Batched problems with a map of the active work: the i-th element of the
@@ -121,19 +167,24 @@ __device__ __forceinline__ int active_element(const int* cum, const int* pid, co
   return poff[pb] + (i - cum[lo]);
 }
 
-// Split c*s (c a tableau coefficient, s a problem's dt) into a float pair.
-__device__ __forceinline__ void split_scaled(double c, double s, float& hi, float& lo) {
-  const double v = c * s;
-  hi = (float)v;
-  lo = (float)(v - (double)hi);
+// (ch, cl) * (sh, sl) as a float pair: a tableau coefficient times a
+// problem's dt, both float pairs.
+__device__ __forceinline__ void ds_mul(float ch, float cl, float sh, float sl, float& ph, float& pl) {
+  const float p = ch * sh;
+  float e = fmaf(ch, sh, -p);
+  e = fmaf(ch, sl, e);
+  e = fmaf(cl, sh, e);
+  ph = p + e;
+  pl = e - (ph - p);
 }
 
 // Epilogue for one element and one equation: y[i], i < ND.  dts scales the
-// coefficients of batched problems (1 otherwise).
+// coefficients of batched problems (1 otherwise): a double for a double
+// state, a float pair (dts2) for the float path.
 template <int ND, typename R>
 __device__ __forceinline__ void epilogue(const EpiParams<R>& ep, long long base_idx,
                                          const R* y, const R* wmean, int ne, int e, int k,
-                                         double dts) {
+                                         double dts, float2 dts2) {
   if (ep.mode == 0) {
 #pragma unroll
     for (int i = 0; i < ND; ++i) ep.out64[base_idx + i] = (double)y[i];
@@ -152,56 +203,99 @@ __device__ __forceinline__ void epilogue(const EpiParams<R>& ep, long long base_
       if (ep.out32) ep.out32[idx] = (float)v;
       m += wmean[i] * v;
     }
-    if (ep.means) ep.means[(long long)k * ne + e] = m;
+    if (ep.means || ep.means32) store_mean(ep, (long long)k * ne + e, m);
   } else {
+    // rows in vectors of W values; at most three previous stages (the
+    // tableaux have up to four stages), unrolled so the coefficients stay in
+    // registers
+    constexpr int W = RowVec<float, ND>::W;
     float mh = 0.0f, ml = 0.0f;
-    float ch[3], cl[3], cch, ccl;
-    if (ep.pdt) {
-      for (int j = 0; j < ep.nprev; ++j) split_scaled(ep.cprev[j], dts, ch[j], cl[j]);
-      split_scaled(ep.ccur, dts, cch, ccl);
-    } else {
-      for (int j = 0; j < ep.nprev; ++j) {
-        ch[j] = ep.cprev_hi[j];
-        cl[j] = ep.cprev_lo[j];
-      }
-      cch = ep.ccur_hi;
-      ccl = ep.ccur_lo;
+    float ch[3], cl[3], cch = ep.ccur_hi, ccl = ep.ccur_lo;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      ch[j] = ep.cprev_hi[j];
+      cl[j] = ep.cprev_lo[j];
+    }
+    if (ep.pdt) {  // unscaled tableau coefficients times the problem's dt
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        if (j < ep.nprev) ds_mul(ch[j], cl[j], dts2.x, dts2.y, ch[j], cl[j]);
+      ds_mul(cch, ccl, dts2.x, dts2.y, cch, ccl);
     }
     if (!ep.final_stage) {
 #pragma unroll
-      for (int i = 0; i < ND; ++i) {
-        const long long idx = base_idx + i;
-        float inc = ep.baselo[idx];
-        for (int j = 0; j < ep.nprev; ++j) inc = fmaf(ch[j], ep.kprev[j][idx], inc);
-        inc = fmaf(cch, y[i], inc);
-        const float v = ep.basehi[idx] + inc;
-        if (ep.kout) ep.kout[idx] = y[i];
-        ep.out32[idx] = v;
-        float ph, pl;
-        ds_mul_f(wmean[i], 0.0f, v, ph, pl);
-        ds_add(mh, ml, ph, pl);
+      for (int i0 = 0; i0 < ND; i0 += W) {
+        const long long idx = base_idx + i0;
+        float inc[W], bh[W], kp[W], v[W];
+        ld_vec<W>(ep.baselo + idx, inc);
+        ld_vec<W>(ep.basehi + idx, bh);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          if (j < ep.nprev) {
+            ld_vec<W>(ep.kprev[j] + idx, kp);
+#pragma unroll
+            for (int w = 0; w < W; ++w) inc[w] = fmaf(ch[j], kp[w], inc[w]);
+          }
+        }
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          inc[w] = fmaf(cch, y[i0 + w], inc[w]);
+          v[w] = bh[w] + inc[w];
+        }
+        if (ep.kout) st_vec<W>(ep.kout + idx, y + i0);
+        st_vec<W>(ep.out32 + idx, v);
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          float ph, pl;
+          ds_mul_f(wmean[i0 + w], 0.0f, v[w], ph, pl);
+          ds_add(mh, ml, ph, pl);
+        }
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < ND; ++i) {
-        const long long idx = base_idx + i;
-        float sh = 0.0f, sl = 0.0f, ph, pl;
-        for (int j = 0; j < ep.nprev; ++j) {
-          ds_mul_f(ch[j], cl[j], ep.kprev[j][idx], ph, pl);
-          ds_add(sh, sl, ph, pl);
+      for (int i0 = 0; i0 < ND; i0 += W) {
+        const long long idx = base_idx + i0;
+        float sh[W], sl[W], kp[W], h[W], l[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) sh[w] = sl[w] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          if (j < ep.nprev) {
+            ld_vec<W>(ep.kprev[j] + idx, kp);
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+              float ph, pl;
+              ds_mul_f(ch[j], cl[j], kp[w], ph, pl);
+              ds_add(sh[w], sl[w], ph, pl);
+            }
+          }
         }
-        ds_mul_f(cch, ccl, y[i], ph, pl);
-        ds_add(sh, sl, ph, pl);
-        float h = ep.basehi[idx], l = ep.baselo[idx];
-        ds_add(h, l, sh, sl);
-        ep.out32[idx] = h;
-        ep.outlo[idx] = l;
-        ds_mul_f(wmean[i], 0.0f, h, ph, pl);
-        ds_add(mh, ml, ph, pl);
-        ds_add(mh, ml, wmean[i] * l, 0.0f);
+        ld_vec<W>(ep.basehi + idx, h);
+        ld_vec<W>(ep.baselo + idx, l);
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          float ph, pl;
+          ds_mul_f(cch, ccl, y[i0 + w], ph, pl);
+          ds_add(sh[w], sl[w], ph, pl);
+          ds_add(h[w], l[w], sh[w], sl[w]);
+        }
+        st_vec<W>(ep.out32 + idx, h);
+        st_vec<W>(ep.outlo + idx, l);
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          float ph, pl;
+          ds_mul_f(wmean[i0 + w], 0.0f, h[w], ph, pl);
+          ds_add(mh, ml, ph, pl);
+          ds_add(mh, ml, wmean[i0 + w] * l[w], 0.0f);
+        }
       }
     }
-    if (ep.means) ep.means[(long long)k * ne + e] = (double)mh + (double)ml;
+    // (mh, ml) stays normalised through ds_add: it is the float pair of the
+    // mean as it stands
+    if (ep.means32)
+      ep.means32[(long long)k * ne + e] = make_float2(mh, ml);
+    else if (ep.means)
+      ep.means[(long long)k * ne + e] = (double)mh + (double)ml;
   }
 }
 
@@ -243,6 +337,7 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
   bool live = e < ne;
   int pb = -1;
   double dts = 1.0;
+  float2 dts2 = make_float2(1.0f, 0.0f);
   if (prm.act_cum) {
     const int na = *prm.act_n;
     live = e < prm.act_cum[na];
@@ -253,7 +348,13 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
     live = prm.pactive[pb] != 0;
     gamma = (R)prm.pgamma[pb];
     cov = (R)prm.pcov[pb];
-    if (ep.pdt) dts = ep.pdt[pb];
+    if (ep.pdt) {
+      dts = ep.pdt[pb];
+      if constexpr (std::is_same<R, float>::value) {
+        const float h = (float)dts;
+        dts2 = make_float2(h, (float)(dts - (double)h));
+      }
+    }
   }
   if (live) {
     R acc[NEQ][ND];
@@ -261,60 +362,129 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
     for (int k = 0; k < NEQ; ++k)
 #pragma unroll
       for (int s = 0; s < ND; ++s) acc[k][s] = R(0);
+    // small float elements (Q1 quads, P1 triangles): the element's own rows
+    // are loaded once, with vector loads, for its faces and volume term, and
+    // each neighbour's rows once per face
+    constexpr bool HOIST = std::is_same<R, float>::value && NEQ * ND <= 16;
+    R own[HOIST ? NEQ : 1][HOIST ? ND : 1];
+    if constexpr (HOIST) {
+#pragma unroll
+      for (int k = 0; k < NEQ; ++k) ld_row<ND>(u + k * NDa + (long long)e * ND, own[k]);
+    }
     const R* fg = (const R*)prm.fgeo;
     for (int lf = 0; lf < NFPE; ++lf) {
       const int nb = prm.fnbr[lf * ne + e];
       if (nb == -1) continue;
       const int code = prm.fcode[lf * ne + e];
-      R n[DIM];
+      if constexpr (HOIST) {
+        R n[DIM];
 #pragma unroll
-      for (int c = 0; c < DIM; ++c) n[c] = fg[(long long)(lf * (DIM + 1) + c) * ne + e];
-      const R jac = fg[(long long)(lf * (DIM + 1) + DIM) * ne + e];
-      const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
-      int e1 = e, lf1 = lf, e2 = nb, lf2 = lfo;
-      if (nb >= 0 && side) {
-        e1 = nb;
-        lf1 = lfo;
-        e2 = e;
-        lf2 = lf;
-      }
-      const R sg = side ? R(1) : R(-1);
-      for (int q = 0; q < NQF; ++q) {
-        const int q2 = sPerm[pid][q];
-        R s1[NEQ], s2[NEQ];
-        const R* B1 = sB[lf1][q];
-#pragma unroll
-        for (int k = 0; k < NEQ; ++k) {
-          const R* uk = u + k * NDa + (long long)e1 * ND;
-          R v = R(0);
-#pragma unroll
-          for (int s = 0; s < ND; ++s) v += uk[s] * B1[s];
-          s1[k] = v;
-        }
+        for (int c = 0; c < DIM; ++c) n[c] = fg[(long long)(lf * (DIM + 1) + c) * ne + e];
+        const R jac = fg[(long long)(lf * (DIM + 1) + DIM) * ne + e];
+        const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
+        // sw: this element is side 2 of the face (the trace order of the
+        // Riemann solver), as in the general path below
+        const bool sw = nb >= 0 && side;
+        R nbr[NEQ][ND];
         if (nb >= 0) {
-          const R* B2 = sB[lf2][q2];
+#pragma unroll
+          for (int k = 0; k < NEQ; ++k) ld_row<ND>(u + k * NDa + (long long)nb * ND, nbr[k]);
+        }
+        const R sg = side ? R(1) : R(-1);
+        for (int q = 0; q < NQF; ++q) {
+          const int q2 = sPerm[pid][q];
+          R to[NEQ], tn[NEQ], s1[NEQ], s2[NEQ];
+          const R* Bw = sB[lf][sw ? q2 : q];
 #pragma unroll
           for (int k = 0; k < NEQ; ++k) {
-            const R* uk = u + k * NDa + (long long)e2 * ND;
             R v = R(0);
 #pragma unroll
-            for (int s = 0; s < ND; ++s) v += uk[s] * B2[s];
-            s2[k] = v;
+            for (int j = 0; j < ND; ++j) v += own[k][j] * Bw[j];
+            to[k] = v;
           }
-        } else {
-          const BCSlot& bc = prm.bc[-2 - nb];
-          right_state<DIM>(bc.type, bc.state, s1, s2, n, gamma, cov, (decltype(gamma))prm.rgas);
+          if (nb >= 0) {
+            const R* Bn = sB[lfo][sw ? q : q2];
+#pragma unroll
+            for (int k = 0; k < NEQ; ++k) {
+              R v = R(0);
+#pragma unroll
+              for (int j = 0; j < ND; ++j) v += nbr[k][j] * Bn[j];
+              tn[k] = v;
+            }
+#pragma unroll
+            for (int k = 0; k < NEQ; ++k) {
+              s1[k] = sw ? tn[k] : to[k];
+              s2[k] = sw ? to[k] : tn[k];
+            }
+          } else {
+#pragma unroll
+            for (int k = 0; k < NEQ; ++k) s1[k] = to[k];
+            const BCSlot& bc = prm.bc[-2 - nb];
+            right_state<DIM>(bc.type, bc.state, s1, s2, n, gamma, cov, (decltype(gamma))prm.rgas);
+          }
+          R F[NEQ];
+          const R sp = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e, pb);
+          lmax = fmax(lmax, sp);
+          const R* Bo = sB[lf][side ? q2 : q];
+          const R wq = sW[q];
+#pragma unroll
+          for (int k = 0; k < NEQ; ++k) {
+            const R t = sg * (F[k] * wq) * jac;
+#pragma unroll
+            for (int j = 0; j < ND; ++j) acc[k][j] += t * Bo[j];
+          }
         }
-        R F[NEQ];
-        const R sp = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e, pb);
-        lmax = fmax(lmax, sp);
-        const R* Bo = sB[lf][side ? q2 : q];
-        const R wq = sW[q];
+      } else {
+        R n[DIM];
 #pragma unroll
-        for (int k = 0; k < NEQ; ++k) {
-          const R t = sg * (F[k] * wq) * jac;
+        for (int c = 0; c < DIM; ++c) n[c] = fg[(long long)(lf * (DIM + 1) + c) * ne + e];
+        const R jac = fg[(long long)(lf * (DIM + 1) + DIM) * ne + e];
+        const int side = (code >> 3) & 1, lfo = code & 7, pid = code >> 4;
+        int e1 = e, lf1 = lf, e2 = nb, lf2 = lfo;
+        if (nb >= 0 && side) {
+          e1 = nb;
+          lf1 = lfo;
+          e2 = e;
+          lf2 = lf;
+        }
+        const R sg = side ? R(1) : R(-1);
+        for (int q = 0; q < NQF; ++q) {
+          const int q2 = sPerm[pid][q];
+          R s1[NEQ], s2[NEQ];
+          const R* B1 = sB[lf1][q];
 #pragma unroll
-          for (int s = 0; s < ND; ++s) acc[k][s] += t * Bo[s];
+          for (int k = 0; k < NEQ; ++k) {
+            const R* uk = u + k * NDa + (long long)e1 * ND;
+            R v = R(0);
+#pragma unroll
+            for (int s = 0; s < ND; ++s) v += uk[s] * B1[s];
+            s1[k] = v;
+          }
+          if (nb >= 0) {
+            const R* B2 = sB[lf2][q2];
+#pragma unroll
+            for (int k = 0; k < NEQ; ++k) {
+              const R* uk = u + k * NDa + (long long)e2 * ND;
+              R v = R(0);
+#pragma unroll
+              for (int s = 0; s < ND; ++s) v += uk[s] * B2[s];
+              s2[k] = v;
+            }
+          } else {
+            const BCSlot& bc = prm.bc[-2 - nb];
+            right_state<DIM>(bc.type, bc.state, s1, s2, n, gamma, cov, (decltype(gamma))prm.rgas);
+          }
+          R F[NEQ];
+          const R sp = checked_speed(prm, riemann<DIM>(s1, s2, n, F, gamma, cov, prm.rs, prm.avg), e, pb);
+          lmax = fmax(lmax, sp);
+          const R* Bo = sB[lf][side ? q2 : q];
+          const R wq = sW[q];
+#pragma unroll
+          for (int k = 0; k < NEQ; ++k) {
+            const R t = sg * (F[k] * wq) * jac;
+#pragma unroll
+            for (int s = 0; s < ND; ++s) acc[k][s] += t * Bo[s];
+          }
         }
       }
     }
@@ -337,7 +507,12 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
         }
         R st[NEQ];
 #pragma unroll
-        for (int k = 0; k < NEQ; ++k) st[k] = u[k * NDa + (long long)e * ND + m];
+        for (int k = 0; k < NEQ; ++k) {
+          if constexpr (HOIST)
+            st[k] = own[k][m];
+          else
+            st[k] = u[k * NDa + (long long)e * ND + m];
+        }
         R F[NEQ][DIM];
         const R sp = flux_and_speed<DIM>(st, F, gamma, cov);
         lmax = fmax(lmax, sp);
@@ -378,20 +553,42 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
           R wl[ND];
 #pragma unroll
           for (int i = 0; i < ND; ++i) wl[i] = (R)T->wmn_e[(long long)e * ND + i];
-          epilogue<ND, R>(ep, k * NDa + (long long)e * ND, y, wl, ne, e, k, dts);
+          epilogue<ND, R>(ep, k * NDa + (long long)e * ND, y, wl, ne, e, k, dts, dts2);
         } else {
-          epilogue<ND, R>(ep, k * NDa + (long long)e * ND, y, sWm, ne, e, k, dts);
+          epilogue<ND, R>(ep, k * NDa + (long long)e * ND, y, sWm, ne, e, k, dts, dts2);
         }
       }
     }
   }
   if (prm.prob)
-    segmented_max_commit((double)lmax, live ? pb : -1, prm.pmcs);
+    segmented_max_commit<R>(lmax, live ? pb : -1, prm.pmcs);
   else
     block_max_commit<R>(lmax, prm.mcs);
 }
 
 // ---- limiter ------------------------------------------------------------------
+// Cell means for the limiter: FP64, or the FP32 path's float pairs.
+__device__ __forceinline__ bool mean_lt(double a, double b) { return a < b; }
+__device__ __forceinline__ bool mean_lt(float2 a, float2 b) {
+  return a.x < b.x || (a.x == b.x && a.y < b.y);
+}
+template <bool F32>
+__device__ __forceinline__ typename std::conditional<F32, float2, double>::type load_mean(
+    const LimParams& prm, long long i) {
+  if constexpr (F32)
+    return prm.means32[i];
+  else
+    return prm.means[i];
+}
+// a mean as a double (either representation)
+__device__ __forceinline__ double mean_value(const LimParams& prm, long long i) {
+  if (prm.means32) {
+    const float2 m = prm.means32[i];
+    return (double)m.x + (double)m.y;
+  }
+  return prm.means[i];
+}
+
 // Nodal basis of the reference element at an arbitrary reference point (the
 // tensor GL Lagrange basis, or the triangle basis from its monomial expansion).
 template <int G, int P>
@@ -464,7 +661,7 @@ __device__ __forceinline__ void shu_indicator(const LimParams& prm, const R* __r
   }
 #pragma unroll
   for (int k = 0; k < NEQ; ++k) {
-    ume[k] = prm.means[(long long)k * ne + e];
+    ume[k] = mean_value(prm, (long long)k * ne + e);
     sum[k] = 0.0;
   }
   double wsum = 0.0;
@@ -585,23 +782,36 @@ __device__ __forceinline__ void shu_indicator(const LimParams& prm, const R* __r
 // The update reads only this element's values and the cell means, so it is
 // done in place.  DS = true: the values are a float pair (u = hi, ulo = lo)
 // and the multiplier update runs in double-single arithmetic.  The indicator
-// (face-point values, stencil min/max, the +-1e-3 switches and the limiter
-// function) is evaluated in FP64 for every state type, from the float state
-// (and its low word) where the state is FP32, so that the FP32-bulk path takes
-// the reference's FP64 branch decisions on the values it holds.
+// takes its branch decisions (face-point value minus mean against the +-1e-3
+// switches, stencil min/max) on the values the state holds: in FP64 for a
+// double state; for a float state in double-single arithmetic (face-point
+// values from the float state and its low word with the float-pair basis
+// table, about 44 significant bits, so a switch differs from FP64 only within
+// ~1e-13 relative of its threshold), and the ratio and limiter function,
+// which only scale the float multiplier, in FP32.  GB300's FP64 rate is a
+// small fraction of its FP32 rate, and an FP64 indicator made the limiter
+// the FP32 path's largest kernel.
 template <int G, int P, typename R, bool DS>
 __global__ void __launch_bounds__(kGenericMaxBlock)
     k_limit_generic(const LimParams prm, R* __restrict__ u, float* __restrict__ ulo) {
   using E = El<G, P>;
   constexpr int DIM = E::DIM, ND = E::ND, NEQ = E::NEQ, NFPE = E::NFPE, NQL = E::NQL, NV = E::NV;
-  __shared__ double sBl[NFPE][NQL][ND];
+  constexpr bool F32 = std::is_same<R, float>::value;
+  // face-point basis: FP64, or a float pair (hi, lo) for a float state
+  __shared__ typename std::conditional<F32, float2, double>::type sBl[NFPE][NQL][ND];
   __shared__ R sBv[NV][ND];
   const RefTables* T = prm.tab;
   // batched problems with a map of the active work: CTAs past it are idle
   if (prm.act_cum && (int)(blockIdx.x * blockDim.x) >= prm.act_cum[*prm.act_n]) return;
   for (int t = threadIdx.x; t < NFPE * NQL * ND; t += blockDim.x) {
     const int s = t % ND, q = (t / ND) % NQL, lf = t / (ND * NQL);
-    sBl[lf][q][s] = T->Bl[lf][q][s];
+    const double b = T->Bl[lf][q][s];
+    if constexpr (F32) {
+      const float h = (float)b;
+      sBl[lf][q][s] = make_float2(h, (float)(b - (double)h));
+    } else {
+      sBl[lf][q][s] = b;
+    }
   }
   for (int t = threadIdx.x; t < NV * ND; t += blockDim.x) sBv[t / ND][t % ND] = (R)T->Bv[t / ND][t % ND];
   __syncthreads();
@@ -625,20 +835,25 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
   R el[NEQ][ND];
   float lo[DS ? NEQ : 1][DS ? ND : 1];
 #pragma unroll
-  for (int k = 0; k < NEQ; ++k)
-#pragma unroll
-    for (int j = 0; j < ND; ++j) {
-      el[k][j] = u[k * NDa + (long long)e * ND + j];
-      if constexpr (DS) lo[k][j] = ulo[k * NDa + (long long)e * ND + j];
-    }
+  for (int k = 0; k < NEQ; ++k) {
+    ld_row<ND>(u + k * NDa + (long long)e * ND, el[k]);
+    if constexpr (DS) ld_row<ND>(ulo + k * NDa + (long long)e * ND, lo[k]);
+  }
   R um[NEQ];
   float umh[NEQ], uml[NEQ];
 #pragma unroll
   for (int k = 0; k < NEQ; ++k) {
-    const double m = prm.means[(long long)k * ne + e];
-    um[k] = (R)m;
-    umh[k] = (float)m;
-    uml[k] = (float)(m - (double)umh[k]);
+    if constexpr (F32) {
+      const float2 m = prm.means32[(long long)k * ne + e];
+      um[k] = m.x;
+      umh[k] = m.x;
+      uml[k] = m.y;
+    } else {
+      const double m = prm.means[(long long)k * ne + e];
+      um[k] = (R)m;
+      umh[k] = (float)m;
+      uml[k] = (float)(m - (double)umh[k]);
+    }
   }
   double minValue;
   double elind[NEQ];
@@ -657,12 +872,24 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
     for (int k = 0; k < NEQ; ++k) elind[k] = (double)sv[k];
     minValue = 1.0;  // FinDiff only: the Multi limiter is rejected with Shu
   } else {
-    double mI[NEQ], MI[NEQ], yMin[NEQ], umd[NEQ];
+    // stencil min / max of the means, started from the element's own mean
+    // clamped to +-1e9: FP64, or for the float path float pairs compared
+    // lexicographically (a normalised pair orders as its value)
+    using MeanT = typename std::conditional<F32, float2, double>::type;
+    MeanT mI[NEQ], MI[NEQ];
+    double yMin[NEQ], umd[NEQ];
 #pragma unroll
     for (int k = 0; k < NEQ; ++k) {
-      umd[k] = prm.means[(long long)k * ne + e];
-      mI[k] = umd[k] < 1e9 ? umd[k] : 1e9;
-      MI[k] = umd[k] > -1e9 ? umd[k] : -1e9;
+      if constexpr (F32) {
+        const float2 own = make_float2(umh[k], uml[k]);
+        const float2 big = make_float2(1e9f, 0.0f), small = make_float2(-1e9f, 0.0f);
+        mI[k] = mean_lt(own, big) ? own : big;
+        MI[k] = mean_lt(small, own) ? own : small;
+      } else {
+        umd[k] = prm.means[(long long)k * ne + e];
+        mI[k] = umd[k] < 1e9 ? umd[k] : 1e9;
+        MI[k] = umd[k] > -1e9 ? umd[k] : -1e9;
+      }
       yMin[k] = 1e9;
     }
     for (int lf = 0; lf < NFPE; ++lf) {
@@ -670,9 +897,9 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
       if (nb < 0) continue;
 #pragma unroll
       for (int k = 0; k < NEQ; ++k) {
-        const double v = prm.means[(long long)k * ne + nb];
-        mI[k] = v < mI[k] ? v : mI[k];
-        MI[k] = v > MI[k] ? v : MI[k];
+        const MeanT v = load_mean<F32>(prm, (long long)k * ne + nb);
+        if (mean_lt(v, mI[k])) mI[k] = v;
+        if (mean_lt(MI[k], v)) MI[k] = v;
       }
     }
     // hanging faces: the elements across them are stencil cells
@@ -687,44 +914,99 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
         ncfaces |= 1u << prm.nc_face[f * 4 + (side ? 3 : 1)];
 #pragma unroll
         for (int k = 0; k < NEQ; ++k) {
-          const double v = prm.means[(long long)k * ne + nb];
-          mI[k] = v < mI[k] ? v : mI[k];
-          MI[k] = v > MI[k] ? v : MI[k];
+          const MeanT v = load_mean<F32>(prm, (long long)k * ne + nb);
+          if (mean_lt(v, mI[k])) mI[k] = v;
+          if (mean_lt(MI[k], v)) MI[k] = v;
         }
       }
     }
-    for (int lf = 0; lf < NFPE; ++lf) {
-      const int nb = prm.fnbr[lf * ne + e];
-      if (nb < 0 && !((ncfaces >> lf) & 1u)) continue;  // only interior faces carry indicator points
+    if constexpr (F32) {
+      // double-single: the +-1e-3 switches as float pairs, the numerators of
+      // the ratio (stencil max / min minus the mean) rounded to FP32
+      const float th = 1e-3f, tl = (float)(1e-3 - (double)1e-3f);
+      float nMax[NEQ], nMin[NEQ], yMf[NEQ];
 #pragma unroll
-      for (int q = 0; q < NQL; ++q) {
+      for (int k = 0; k < NEQ; ++k) {
+        nMax[k] = (MI[k].x - umh[k]) + (MI[k].y - uml[k]);
+        nMin[k] = (mI[k].x - umh[k]) + (mI[k].y - uml[k]);
+        yMf[k] = 1e9f;
+      }
+      for (int lf = 0; lf < NFPE; ++lf) {
+        const int nb = prm.fnbr[lf * ne + e];
+        if (nb < 0 && !((ncfaces >> lf) & 1u)) continue;  // only interior faces carry indicator points
 #pragma unroll
-        for (int k = 0; k < NEQ; ++k) {
-          double v = 0.0;
+        for (int q = 0; q < NQL; ++q) {
 #pragma unroll
-          for (int j = 0; j < ND; ++j) {
-            v += (double)el[k][j] * sBl[lf][q][j];
-            if constexpr (DS) v += (double)lo[k][j] * sBl[lf][q][j];
+          for (int k = 0; k < NEQ; ++k) {
+            // value at the point minus the mean, as a float pair
+            float sh = -umh[k], sl = -uml[k];
+#pragma unroll
+            for (int j = 0; j < ND; ++j) {
+              const float2 bq = sBl[lf][q][j];
+              const float x = (float)el[k][j];
+              const float ph = x * bq.x;
+              float pl = fmaf(x, bq.x, -ph);
+              pl = fmaf(x, bq.y, pl);
+              if constexpr (DS) pl = fmaf(lo[k][j], bq.x, pl);
+              float t, er;
+              two_sum(sh, ph, t, er);
+              er += sl + pl;
+              sh = t + er;
+              sl = er - (sh - t);
+            }
+            const bool above = sh > th || (sh == th && sl > tl);
+            const bool below = sh < -th || (sh == -th && sl < -tl);
+            const float y = above ? nMax[k] / sh : (below ? nMin[k] / sh : 1.0f);
+            if (prm.function == 0) {
+              yMf[k] = fminf(fminf(y, yMf[k]), 1.0f);
+            } else if (prm.function == 1) {
+              const float yc = (y * y + 2.0f * y) / (y * y + y + 2.0f);
+              yMf[k] = fminf(yc, yMf[k]);
+            } else {
+              const float ys = 1.5f;
+              const float yr = y / ys;
+              const float yc = y < 1.0f ? y + (3.0f - 2.0f * ys) * yr * yr + (ys - 2.0f) * yr * yr * yr : 1.0f;
+              yMf[k] = fminf(yc, yMf[k]);
+            }
           }
-          const double diff = v - umd[k];
-          double y;
-          if (diff > 1e-3)
-            y = (MI[k] - umd[k]) / diff;
-          else if (diff < -1e-3)
-            y = (mI[k] - umd[k]) / diff;
-          else
-            y = 1.0;
-          if (prm.function == 0) {
-            yMin[k] = y < yMin[k] ? y : yMin[k];
-            yMin[k] = yMin[k] > 1.0 ? 1.0 : yMin[k];
-          } else if (prm.function == 1) {
-            const double yc = (y * y + 2.0 * y) / (y * y + y + 2.0);
-            yMin[k] = yc < yMin[k] ? yc : yMin[k];
-          } else {
-            const double ys = 1.5;
-            const double yr = y / ys;
-            const double yc = y < 1.0 ? y + (3.0 - 2.0 * ys) * yr * yr + (ys - 2.0) * yr * yr * yr : 1.0;
-            yMin[k] = yc < yMin[k] ? yc : yMin[k];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < NEQ; ++k) yMin[k] = (double)yMf[k];
+    } else {
+      for (int lf = 0; lf < NFPE; ++lf) {
+        const int nb = prm.fnbr[lf * ne + e];
+        if (nb < 0 && !((ncfaces >> lf) & 1u)) continue;  // only interior faces carry indicator points
+#pragma unroll
+        for (int q = 0; q < NQL; ++q) {
+#pragma unroll
+          for (int k = 0; k < NEQ; ++k) {
+            double v = 0.0;
+#pragma unroll
+            for (int j = 0; j < ND; ++j) {
+              v += (double)el[k][j] * sBl[lf][q][j];
+              if constexpr (DS) v += (double)lo[k][j] * sBl[lf][q][j];
+            }
+            const double diff = v - umd[k];
+            double y;
+            if (diff > 1e-3)
+              y = (MI[k] - umd[k]) / diff;
+            else if (diff < -1e-3)
+              y = (mI[k] - umd[k]) / diff;
+            else
+              y = 1.0;
+            if (prm.function == 0) {
+              yMin[k] = y < yMin[k] ? y : yMin[k];
+              yMin[k] = yMin[k] > 1.0 ? 1.0 : yMin[k];
+            } else if (prm.function == 1) {
+              const double yc = (y * y + 2.0 * y) / (y * y + y + 2.0);
+              yMin[k] = yc < yMin[k] ? yc : yMin[k];
+            } else {
+              const double ys = 1.5;
+              const double yr = y / ys;
+              const double yc = y < 1.0 ? y + (3.0 - 2.0 * ys) * yr * yr + (ys - 2.0) * yr * yr * yr : 1.0;
+              yMin[k] = yc < yMin[k] ? yc : yMin[k];
+            }
           }
         }
       }
@@ -750,7 +1032,7 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
               if constexpr (DS) v += (double)lo[k][j];
               g[d] += v * T->dcen[j][d];
             }
-          const double m = prm.means[(long long)k * ne + e];
+          const double m = mean_value(prm, (long long)k * ne + e);
 #pragma unroll
           for (int j = 0; j < ND; ++j) {
             double v = m;
@@ -825,12 +1107,10 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
     }
   }
 #pragma unroll
-  for (int k = 0; k < NEQ; ++k)
-#pragma unroll
-    for (int j = 0; j < ND; ++j) {
-      u[k * NDa + (long long)e * ND + j] = el[k][j];
-      if constexpr (DS) ulo[k * NDa + (long long)e * ND + j] = lo[k][j];
-    }
+  for (int k = 0; k < NEQ; ++k) {
+    st_row<ND>(u + k * NDa + (long long)e * ND, el[k]);
+    if constexpr (DS) st_row<ND>(ulo + k * NDa + (long long)e * ND, lo[k]);
+  }
 }
 
 // ---- cell means (Averager::computeMeanValues, averager.cpp:84-109) -----------

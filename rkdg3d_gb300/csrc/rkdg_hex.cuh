@@ -373,13 +373,13 @@ __global__ void __launch_bounds__(256)
         for (int kk = 0; kk < NEQ; ++kk)
           if (kk == k) msum[kk] += T->wmean[j] * c;
       }
-      if (ep.mode == 1 && ep.means) {
+      if (ep.mode == 1 && (ep.means || ep.means32)) {
 #pragma unroll
         for (int k = 0; k < NEQ; ++k) {
           double s = msum[k];
 #pragma unroll
           for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-          if (lane == 0) ep.means[(long long)k * ne + e] = s;
+          if (lane == 0) store_mean(ep, (long long)k * ne + e, s);
         }
       }
     }

@@ -888,7 +888,7 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
   if (!prm.faces_only) {
     // coalesced Runge-Kutta epilogue over the CTA's elements; the combined
     // state (hi, lo) is kept in shared memory when the limiter needs means
-    const bool need_means = ep.mode == 1 && ep.means;
+    const bool need_means = ep.mode == 1 && (ep.means || ep.means32);
     if (ep.mode == 1 && !need_means) {
       // chunked: all loads of a chunk are issued before its stores (the final
       // stage updates the state in place, which would otherwise serialise
@@ -972,7 +972,7 @@ __global__ void __launch_bounds__(128, TeamSize<P>::template min_ctas<R, MODE>()
       for (int t = tid; t < nel * NEQ; t += blockDim.x) {
         double m = 0.0;
         for (int i = 0; i < ND; ++i) m += T->wmean[i] * ((double)sU[t * ND + i] + (double)sX[t * ND + i]);
-        ep.means[(long long)(t % NEQ) * ne + eid(t / NEQ)] = m;
+        store_mean(ep, (long long)(t % NEQ) * ne + eid(t / NEQ), m);
       }
     }
   }

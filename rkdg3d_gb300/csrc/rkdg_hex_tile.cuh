@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
   }
   __syncthreads();
   // Runge-Kutta epilogue over the tile, coalesced within each element's run
-  const bool need_means = ep.mode == 1 && ep.means;
+  const bool need_means = ep.mode == 1 && (ep.means || ep.means32);
   R* sLo = sT;  // low parts of the combined state when the limiter needs means
   const int total = NEQ * nel * ND;
   if (ep.mode == 1 && !need_means) {
@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
         double m = 0.0;
         for (int i = 0; i < ND; ++i)
           m += RT->wmean[i] * ((double)sU[(kk * E + s) * ND + i] + (double)sLo[(kk * E + s) * ND + i]);
-        ep.means[(long long)kk * ne + sTile.el[s]] = m;
+        store_mean(ep, (long long)kk * ne + sTile.el[s], m);
       }
     }
   }

@@ -624,13 +624,16 @@ int enqueue_step32(rkdg_ctx* c, double dt, bool batch = false) {
       ep.outlo = c->d_xl;
       ep.final_stage = 1;
     }
-    ep.means = lim ? c->d_means : nullptr;
+    // the FP32 path's means are float pairs in the same buffer (8 bytes each)
+    ep.means32 = lim ? reinterpret_cast<float2*>(c->d_means) : nullptr;
     RhsParams P = rhs_params(c, 1, 0, i);
     if (batch) set_batch(c, P, i);
     CUDA_TRY(c, launch_rhs_nc(c, 1, P, in, &ep));
     c->launches += rhs_kernels(c, P);
     if (lim) {
       LimParams L = lim_params_for(c, batch);
+      L.means = nullptr;
+      L.means32 = reinterpret_cast<const float2*>(c->d_means);
       if (i < s - 1)
         CUDA_TRY(c, rkdg::launch_limit(c->geom, c->p, 1, L, c->d_y32[(i + 1) % 2], nullptr, c->stream));
       else
