@@ -159,7 +159,11 @@ int rkdg_set_precision(rkdg_ctx* ctx, int precision);
  * into per-element flux slots the context allocates) + element pass,
  * 4 five-lane team over Morton-ordered groups of 24 elements whose faces
  * inside the group are evaluated once (order <= 2 hexahedra; the plain team
- * kernel when the mesh's face graph needs more than 8 rounds).
+ * kernel when the mesh's face graph needs more than 8 rounds), 5 face-once
+ * tiles of 32 Morton-ordered elements (order <= 2; the FP32 Q2 default),
+ * 6 the tile kernel with the collocated volume contraction on the tensor
+ * cores (tcgen05 TF32 MMAs, operands split into TF32 hi + lo; FP32-bulk Q2
+ * only, else the default).
  * RKDG_TUNE_GENERIC_BLOCK /
  * RKDG_TUNE_LIMITER_BLOCK: elements (threads) per CTA of the triangle/quad
  * right-hand-side kernel and of the limiter, 0 (default 128) or a multiple of

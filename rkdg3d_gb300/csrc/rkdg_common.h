@@ -216,6 +216,10 @@ struct RhsParams {
   const HexTile* htile;        // face-once tiled hexahedral kernel: one entry per CTA (or null)
   int ntile;
   int tile_hs;                 // its halo-buffer stride: the largest halo list, odd
+  // tensor-core variant of the tile kernel (Q2): the volume operator of each
+  // direction as a dense 32 x 32 TF32 pair (hi, lo) in the K-major core-matrix
+  // layout, [3][2][1024] floats (or null)
+  const float* tcb;
   // nonconforming meshes: element -> row of xface (-1: none) and the face
   // terms of the hanging faces, [row][neq][nd] in the kernel's precision,
   // added to the element's face + volume terms before the inverse mass

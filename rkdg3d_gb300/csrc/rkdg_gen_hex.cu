@@ -103,10 +103,12 @@ template cudaError_t launch_means_t<5, 2>(int, int, long long, const RefTables*,
 // autotuner (0 = default choice above, 1 = warp-per-element sum
 // factorisation, 2 = team kernel, 3 = face pass + element pass, 4 = team
 // kernel with shared-face rounds, 5 = face-once tiled kernel where the
-// context holds tiles, else the default).
+// context holds tiles, 6 = the tiled kernel with the volume contraction on
+// the tensor cores for FP32 Q2, else the default).
 cudaError_t launch_hex_variant(int variant, int p, int prec, const RhsParams& prm, const void* u,
                                const void* ep, cudaStream_t st) {
   if (variant == 5 && prm.htile) return launch_hex_tile(p, prec, prm, u, ep, st);
+  if (variant == 6 && prm.htile && prm.tcb && p == 2 && prec == 1) return launch_hex_tile_tc(prm, u, ep, st);
   if (variant == 4) {
     if (p == 1)
       return prec == 0 ? launch_hex_shared<1, double>(prm, (const double*)u, *(const EpiParams<double>*)ep, st)

@@ -35,6 +35,7 @@
 #include "rkdg_generic.cuh"
 #include "rkdg_hex_team.cuh"
 #include "rkdg_physics.cuh"
+#include "rkdg_tc.cuh"
 
 namespace rkdg {
 
@@ -56,6 +57,17 @@ struct TileSize {
   static constexpr size_t smem_bytes(int hs) { return sizeof(R) * (size_t)(OFF_H + NEQ * NQF * hs); }
   template <typename R>
   __host__ __device__ static constexpr int min_ctas() { return sizeof(R) == 4 ? 4 : 2; }
+  // tensor-core variant (FP32, P = 2): after the staged DOFs, the volume
+  // operands A_hi, A_lo ([160 rows (variable, slot)][32 nodes], core-matrix
+  // layout) and one direction's B_hi, B_lo ([32][32]) alias the trace and
+  // halo regions
+  static constexpr int TC_ROWS = NEQ * E, TC_A = TC_ROWS * 32, TC_B = 32 * 32;
+  static constexpr int TC_FLOATS = 2 * TC_A + 2 * TC_B;
+  static constexpr size_t smem_bytes_tc(int hs) {
+    return sizeof(float) * (size_t)(OFF_T + (2 * NEQ * NQF * TS + NEQ * NQF * hs > TC_FLOATS
+                                                 ? 2 * NEQ * NQF * TS + NEQ * NQF * hs
+                                                 : TC_FLOATS));
+  }
 };
 
 // Local face of axis AX on side SD (MFEM hexahedron numbering).
@@ -246,8 +258,23 @@ __device__ __forceinline__ void tile_sweep(const R (&g)[(P + 1) * (P + 1) * (P +
       }
 }
 
-template <int P, typename R>
-__global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_ctas<R>())
+// Float offset of element (row, col) of a K-major TF32 operand with 32
+// columns: core matrices of 8 rows x 4 columns (128 bytes), 8 per row group
+// along K (LBO 128 bytes), row groups 1024 bytes apart (SBO).
+__device__ __forceinline__ int tc_off(int row, int col) {
+  return (row >> 3) * 256 + (col >> 2) * 32 + (row & 7) * 4 + (col & 3);
+}
+
+// TC = true (FP32, P = 2): the collocated volume contraction on the tensor
+// cores (tcgen05, kind::tf32) instead of the three sweeps: per direction r
+// the contravariant flux of every (variable, slot) row over the 27 nodes is
+// A (160 x 32, split into TF32 hi + lo), the direction's sweep with the other
+// two node weights is a dense 27 x 27 operator B_r (hi + lo), and
+// A_hi B_hi + A_hi B_lo + A_lo B_hi accumulates over the three directions in
+// FP32 in tensor memory: rows 0-127 in columns 0-31, rows 32-159 in columns
+// 32-63 (lanes 96-127 hold rows 128-159, read by warp 3 for warp 4).
+template <int P, typename R, bool TC = false>
+__global__ void __launch_bounds__(TileSize<P>::NT, TC ? 3 : TileSize<P>::template min_ctas<R>())
     k_rhs_hex_tile(const __grid_constant__ RhsParams prm, const R* __restrict__ u,
                    const EpiParams<R> ep) {
   using S = TileSize<P>;
@@ -260,6 +287,10 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
   __shared__ R sEG[2 * E][4];  // per evaluation of the current axis: normal, |J_f|
   __shared__ unsigned char sPerm[RKDG_HEX_MAX_PERM][NQF];
   __shared__ unsigned char sFab[6][NQF];
+  __shared__ uint64_t sMbar;     // tensor-core completion (TC)
+  __shared__ uint32_t sTmem;     // tensor-memory base address (TC)
+  __shared__ int sTcFail;        // a completion wait gave up (TC)
+  static_assert(!TC || (std::is_same<R, float>::value && P == 2), "tensor-core variant: FP32, P = 2");
   R* sm = reinterpret_cast<R*>(smraw);
   R* sU = sm;              // [NEQ][E][ND]; the right-hand side after the volume phase
   R* sT = sm + S::OFF_T;   // [2][NEQ][NQF][TS]
@@ -275,6 +306,12 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
   for (int t = tid; t < min(RT->nperm, RKDG_HEX_MAX_PERM) * NQF; t += NT)
     sPerm[t / NQF][t % NQF] = (unsigned char)RT->perm[t / NQF][t % NQF];
   for (int t = tid; t < 6 * NQF; t += NT) sFab[t / NQF][t % NQF] = (unsigned char)RT->fab[t / NQF][t % NQF];
+  if constexpr (TC) {
+    if (tid == 0) {
+      tc::mbar_init(&sMbar, 1);
+      sTcFail = 0;
+    }
+  }
   __syncthreads();
   const int nel = sTile.nel;
   const long long NDa = prm.ndofs;
@@ -359,6 +396,126 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
   // collocated sweep along r
   R* sG = sT;  // [NEQ][E][ND]
   const R gamma = (R)prm.gamma, cov = (R)prm.covolume;
+  if constexpr (TC) {
+    float* A0 = sT;                // A_hi; A_lo follows
+    float* A1 = sT + S::TC_A;
+    float* B0 = sT + 2 * S::TC_A;  // B_hi; B_lo follows
+    float* B1 = B0 + S::TC_B;
+    constexpr uint32_t IDESC = tc::idesc_tf32(128, 32);
+    constexpr int kWaitPolls = 1 << 20;
+    const int warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) {
+      tc::tmem_alloc(&sTmem, 64);
+      tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();  // also: the lifts are done with the trace region
+    tc::fence_after_sync();
+    const uint32_t tbase = sTmem;
+    // the K padding (nodes 27-31) of every row stays zero
+    for (int t = tid; t < S::TC_ROWS * 5; t += NT) {
+      const int row = t / 5, col = 27 + t % 5;
+      A0[tc_off(row, col)] = 0.0f;
+      A1[tc_off(row, col)] = 0.0f;
+    }
+    bool failed = false;
+#pragma unroll 1
+    for (int r = 0; r < 3; ++r) {
+      // this direction's operator (hi, lo) from the table
+      {
+        const float4* src = reinterpret_cast<const float4*>(prm.tcb + (size_t)r * 2 * S::TC_B);
+        float4* dst = reinterpret_cast<float4*>(B0);
+        for (int t = tid; t < 2 * S::TC_B / 4; t += NT) dst[t] = __ldg(src + t);
+      }
+      // contravariant fluxes, one (slot, node) per thread (slot fastest: the
+      // staged reads stride 27 words), split into the two A operands
+      for (int t = tid; t < E * ND; t += NT) {
+        const int m = t / E, sl = t - m * E;
+        if (sl >= nel) continue;
+        R st[NEQ];
+#pragma unroll
+        for (int kk = 0; kk < NEQ; ++kk) st[kk] = sU[(kk * E + sl) * ND + m];
+        R F[NEQ][3];
+        const R sp = flux_and_speed<3>(st, F, gamma, cov);
+        if (r == 0) lmax = fmax(lmax, sp);
+        const R a0 = sGeo[sl][3 * r], a1 = sGeo[sl][3 * r + 1], a2 = sGeo[sl][3 * r + 2];
+#pragma unroll
+        for (int kk = 0; kk < NEQ; ++kk) {
+          const float g = a0 * F[kk][0] + a1 * F[kk][1] + a2 * F[kk][2];
+          const float h = tc::tf32_hi(g);
+          const int o = tc_off(kk * E + sl, m);
+          A0[o] = h;
+          A1[o] = g - h;
+        }
+      }
+      tc::fence_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t a_base[2] = {tc::smem_u32(A0), tc::smem_u32(A1)};
+        const uint32_t b_base[2] = {tc::smem_u32(B0), tc::smem_u32(B1)};
+        const int terms[3][2] = {{0, 0}, {0, 1}, {1, 0}};  // (A part, B part)
+#pragma unroll
+        for (int blk = 0; blk < 2; ++blk)
+#pragma unroll
+          for (int tm = 0; tm < 3; ++tm)
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              // block 1 starts at row 32 (row group 4, 4096 bytes); K step ks
+              // at column 8 ks (two core matrices, 256 bytes)
+              const uint64_t ad = tc::desc_kmajor(a_base[terms[tm][0]] + blk * 4096 + ks * 256, 128, 1024);
+              const uint64_t bd = tc::desc_kmajor(b_base[terms[tm][1]] + ks * 256, 128, 1024);
+              const uint32_t acc_in = (r > 0 || tm > 0 || ks > 0) ? 1u : 0u;
+              tc::mma_tf32(tbase + blk * 32, ad, bd, IDESC, acc_in);
+            }
+        tc::commit(&sMbar);
+      }
+      // the MMAs read A and B before either is rewritten
+      if (!tc::mbar_wait(&sMbar, r & 1, kWaitPolls)) failed = true;
+      if (failed) sTcFail = 1;
+      __syncthreads();
+      if (sTcFail) break;
+    }
+    if (sTcFail) {
+      // give the tensor core one more bounded wait, free the tensor memory
+      // and leave the tile unwritten with the error flagged
+      if (tid == 0) flag_error(prm.err, 8, blockIdx.x);
+      tc::mbar_wait(&sMbar, 0, kWaitPolls);
+      tc::mbar_wait(&sMbar, 1, kWaitPolls);
+      tc::fence_before_sync();
+      __syncthreads();
+      if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tbase, 64);
+      }
+      return;
+    }
+    tc::fence_after_sync();
+    float v[32];
+    if (warp < 4) {
+      tc::ld32(tbase + ((uint32_t)(32 * warp) << 16), v);
+      if (act) {
+#pragma unroll
+        for (int i = 0; i < ND; ++i) acc[i] += v[i];
+      }
+    }
+    float* sX = A0;  // rows 128-159 handed from warp 3 to warp 4
+    if (warp == 3) {
+      tc::ld32(tbase + (96u << 16) + 32u, v);
+#pragma unroll
+      for (int i = 0; i < ND; ++i) sX[lane * ND + i] = v[i];
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 4 && act) {
+#pragma unroll
+      for (int i = 0; i < ND; ++i) acc[i] += sX[lane * ND + i];
+    }
+    if (warp == 0) {
+      tc::fence_after_sync();
+      tc::tmem_dealloc(tbase, 64);
+    }
+  } else {
 #pragma unroll 1
   for (int r = 0; r < 3; ++r) {
     __syncthreads();  // the lifts (r = 0) or the previous sweeps are done with sT
@@ -385,6 +542,7 @@ __global__ void __launch_bounds__(TileSize<P>::NT, TileSize<P>::template min_cta
         default: tile_sweep<P, 2>(gv, H, acc); break;
       }
     }
+  }
   }
   R g[ND];
   if (act) {

@@ -55,6 +55,7 @@ struct rkdg_ctx {
   HexTeamSched* d_hsched = nullptr;  // per-CTA schedules of the shared-face hexahedral kernel
   int hsched_rounds = 0;
   HexTile* d_htile = nullptr;  // tiles of the face-once hexahedral kernel
+  float* d_tcb = nullptr;      // volume operators of its tensor-core variant (Q2)
   int ntile = 0;
   int tile_hs = 1;             // halo-buffer stride of its CTAs (odd)
   // hanging faces of a nonconforming mesh (see rkdg_nc.cu)
@@ -211,6 +212,7 @@ void free_mesh(rkdg_ctx* c) {
   dfree(c->d_hsched);
   c->hsched_rounds = 0;
   dfree(c->d_htile);
+  dfree(c->d_tcb);
   c->ntile = 0;
   dfree(c->d_nc_face);
   dfree(c->d_nc_bnc);
@@ -318,6 +320,7 @@ RhsParams rhs_params(rkdg_ctx* c, int prec, int faces_only, int slot) {
   P.fslot = c->d_fslot;
   P.hsched = c->d_hsched;
   P.htile = c->d_htile;
+  P.tcb = c->d_tcb;
   P.ntile = c->ntile;
   P.tile_hs = c->tile_hs;
   P.ncidx = c->nnc ? c->d_ncidx : nullptr;
@@ -466,12 +469,52 @@ int ensure_scratch(rkdg_ctx* c) {
   return RKDG_OK;
 }
 
+// TF32 part of an FP32 value (10 explicit mantissa bits, rounded to nearest).
+float tf32_hi_host(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  b = (b + 0x1000u) & 0xFFFFE000u;
+  float y;
+  std::memcpy(&y, &b, 4);
+  return y;
+}
+
+// Volume operators of the tensor-core tile kernel (Q2 hexahedra): for
+// direction r the collocated sweep along r with the other two node weights,
+// acc[j] += w1[j_a] w1[j_b] d1[j_r][m_r] g_r[m] over the nodes m that share
+// j's other two indices, as a dense 32 x 32 matrix B_r[j][m] (zero beyond 27),
+// split into TF32 hi and the FP32 remainder lo, stored K-major (m along K) in
+// 8 x 4 core matrices: float offset (j / 8) * 256 + (m / 4) * 32 +
+// (j % 8) * 4 + m % 4.  Layout [r][hi, lo][1024].
+std::vector<float> tc_volume_operators(const RefTables& T) {
+  std::vector<float> out(3 * 2 * 1024, 0.0f);
+  for (int r = 0; r < 3; ++r)
+    for (int j = 0; j < 27; ++j)
+      for (int m = 0; m < 27; ++m) {
+        const int jx = j % 3, jy = (j / 3) % 3, jz = j / 9;
+        const int mx = m % 3, my = (m / 3) % 3, mz = m / 9;
+        double v = 0.0;
+        if (r == 0 && my == jy && mz == jz) v = T.w1[jy] * T.w1[jz] * T.d1[jx][mx];
+        if (r == 1 && mx == jx && mz == jz) v = T.w1[jx] * T.w1[jz] * T.d1[jy][my];
+        if (r == 2 && mx == jx && my == jy) v = T.w1[jx] * T.w1[jy] * T.d1[jz][mz];
+        const float hi = tf32_hi_host((float)v);
+        const float lo = (float)(v - (double)hi);
+        const int o = (j / 8) * 256 + (m / 4) * 32 + (j % 8) * 4 + m % 4;
+        out[(size_t)(r * 2 + 0) * 1024 + o] = hi;
+        out[(size_t)(r * 2 + 1) * 1024 + o] = lo;
+      }
+  return out;
+}
+
 int check_device_error(rkdg_ctx* c) {
   if (c->h_err[0] != 0) {
     const int code = c->h_err[0];
     char msg[128];
-    snprintf(msg, sizeof msg, "non-physical state in the Riemann solver at element %d",
-             c->h_err[1]);
+    if (code == 8)  // a bounded wait on the tensor core gave up (tile kernel)
+      snprintf(msg, sizeof msg, "tensor-core completion wait timed out in tile %d", c->h_err[1]);
+    else
+      snprintf(msg, sizeof msg, "non-physical state in the Riemann solver at element %d",
+               c->h_err[1]);
     CUDA_TRY(c, cudaMemsetAsync(c->d_err, 0, 2 * sizeof(int), c->stream));
     return fail(c, code == 2 ? RKDG_ERR_UNPHYSICAL : RKDG_ERR_CUDA, msg, c->h_err[1]);
   }
@@ -833,7 +876,7 @@ int rkdg_set_solver_quirks(rkdg_ctx* c, int flags) {
 
 int rkdg_set_tuning(rkdg_ctx* c, int key, int value) {
   if (!c) return RKDG_ERR_INVALID;
-  if (key == RKDG_TUNE_HEX_KERNEL && value >= 0 && value <= 5) {
+  if (key == RKDG_TUNE_HEX_KERNEL && value >= 0 && value <= 6) {
     if (value == 3 && c->has_mesh) {
       const int st = ensure_fslot(c);
       if (st) return st;
@@ -1285,6 +1328,11 @@ int rkdg_upload_mesh(rkdg_ctx* c, const rkdg_mesh_desc* m) {
       for (const HexTile& t : ht)
         for (int a = 0; a < 3; ++a) mh = std::max(mh, t.nh[a]);
       c->tile_hs = mh | 1;
+    }
+    if (c->p == 2) {
+      const std::vector<float> tcb = tc_volume_operators(c->tab);
+      CUDA_TRY(c, dalloc(c->d_tcb, tcb.size()));
+      CUDA_TRY(c, cudaMemcpy(c->d_tcb, tcb.data(), tcb.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
   }
   c->has_mesh = true;
@@ -1985,8 +2033,9 @@ int rkdg_autotune(rkdg_ctx* c, const double* x, int* hex_kernel, int* generic_bl
     if ((st = ensure_fslot(c))) return st;
     int best = 0;
     float tbest = 0.0f;
-    for (int v = 1; v <= 5; ++v) {
+    for (int v = 1; v <= 6; ++v) {
       if ((v == 4 && !c->d_hsched) || (v == 5 && !c->d_htile)) continue;
+      if (v == 6 && !(c->d_htile && c->d_tcb && c->precision != RKDG_FP64)) continue;
       c->hex_variant = v;
       float ms = 0.0f;
       if ((st = time_rhs(&ms))) return st;

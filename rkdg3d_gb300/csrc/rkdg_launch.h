@@ -19,6 +19,8 @@ cudaError_t launch_hex_variant(int variant, int p, int prec, const RhsParams& pr
 // Face-once tiled hexahedral kernel (orders 1 and 2; needs prm.htile).
 cudaError_t launch_hex_tile(int p, int prec, const RhsParams& prm, const void* u, const void* ep,
                             cudaStream_t st);
+// the tile kernel with the volume contraction on the tensor cores (FP32, Q2)
+cudaError_t launch_hex_tile_tc(const RhsParams& prm, const void* u, const void* ep, cudaStream_t st);
 // mode: 0 = double in place, 1 = float in place, 2 = float pair (u = hi, ulo = lo)
 cudaError_t launch_limit(int geom, int p, int mode, const LimParams& prm, void* u, float* ulo,
                          cudaStream_t st);

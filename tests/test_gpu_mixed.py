@@ -19,7 +19,7 @@ def make(case, prec):
     return ctx
 
 
-@pytest.mark.parametrize("variant", [0, 2, 3, 4, 5])
+@pytest.mark.parametrize("variant", [0, 2, 3, 4, 5, 6])
 def test_mixed_rhs_close_to_fp64(cuda, variant):
     """FP32-bulk right-hand side (fused team kernel, or face pass + element
     pass) against the plain FP64 one."""
