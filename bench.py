@@ -51,11 +51,11 @@ def workload_config(case, n_elem_side):
     }
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element per
-# stage launch of k_rhs_hex_team<2,float>: mean of the three stage launches of
-# one RK step captured with ncu on the 48^3 pulse (329.5 MB / 110,592
+# DRAM bytes (read + write) per element and stage launch of the C2 stage
+# kernel k_rhs_hex_tile<2,float>: mean of the three stage launches of one RK
+# step captured with ncu on the 64^3 pulse itself (840.2 MB / 262,144
 # elements); traffic scales with the element count.
-TRAFFIC_BYTES_PER_ELEMENT_LAUNCH = 2979.5
+TRAFFIC_BYTES_PER_ELEMENT_LAUNCH = 3205.0
 
 
 def algorithmic_bytes_per_step(N, ne, precision):
@@ -326,7 +326,7 @@ def run_ours(args, rank, world, local):
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak,
             "traffic": args.traffic_per_launch or TRAFFIC_BYTES_PER_ELEMENT_LAUNCH * ctx32.ne,
-            "traffic_source": "ncu dram bytes, 48^3 capture scaled by elements"
+            "traffic_source": "ncu dram bytes per launch, 64^3 capture (per element, scaled by elements)"
                               if not args.traffic_per_launch else "command line",
             "peak_source": peak_src,
             "kernel": ("k_rhs_hex_tile<2,float> (face-once tiled stage kernel, 3 launches per step)"
