@@ -199,6 +199,8 @@ struct RhsParams {
   const int* prob;
   const double* pgamma;
   const double* pcov;
+  const float* pgamma32;  // the same constants rounded to FP32 (the FP32 kernels)
+  const float* pcov32;
   const int* pactive;
   unsigned long long* pmcs;
   int* pfail;           // per-problem failure flag (non-physical state)
@@ -281,6 +283,7 @@ struct EpiParams {
   // coefficients and are multiplied by the problem's dt (pdt[prob[e]])
   const int* prob;
   const double* pdt;
+  const float2* pdt2;  // pdt as float pairs (hi, lo), read by the FP32 kernels
 };
 
 #ifdef __CUDACC__
@@ -311,6 +314,8 @@ struct LimParams {
   const int* prob;      // batched problems (or null)
   const double* pgamma;
   const double* pcov;
+  const float* pgamma32;  // the same constants rounded to FP32 (the FP32 kernels)
+  const float* pcov32;
   const int* pactive;
   const int* act_cum;   // map of the active work (as RhsParams; or null)
   const int* act_pid;
@@ -332,6 +337,7 @@ struct BatchState {
   const double* hmin;   // [nprob]
   double* dt;           // [nprob] dt of the reference bookkeeping
   double* dtr;          // [nprob] dt_real used by the current step
+  float2* dtr2;         // [nprob] the same as float pairs (hi, lo)
   double* t;            // [nprob]
   double* sum_dt;       // [nprob]
   int* active;          // [nprob]

@@ -216,7 +216,7 @@ __device__ __forceinline__ void epilogue(const EpiParams<R>& ep, long long base_
       ch[j] = ep.cprev_hi[j];
       cl[j] = ep.cprev_lo[j];
     }
-    if (ep.pdt) {  // unscaled tableau coefficients times the problem's dt
+    if (ep.pdt || ep.pdt2) {  // unscaled tableau coefficients times the problem's dt
 #pragma unroll
       for (int j = 0; j < 3; ++j)
         if (j < ep.nprev) ds_mul(ch[j], cl[j], dts2.x, dts2.y, ch[j], cl[j]);
@@ -346,14 +346,21 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
   if (live && prm.prob) {
     if (!prm.act_cum) pb = prm.prob[e];
     live = prm.pactive[pb] != 0;
-    gamma = (R)prm.pgamma[pb];
-    cov = (R)prm.pcov[pb];
-    if (ep.pdt) {
-      dts = ep.pdt[pb];
-      if constexpr (std::is_same<R, float>::value) {
+    if constexpr (std::is_same<R, float>::value) {
+      // FP32 copies: no FP64 conversions per element
+      gamma = prm.pgamma32 ? prm.pgamma32[pb] : (R)prm.pgamma[pb];
+      cov = prm.pcov32 ? prm.pcov32[pb] : (R)prm.pcov[pb];
+      if (ep.pdt2) {
+        dts2 = ep.pdt2[pb];
+      } else if (ep.pdt) {
+        dts = ep.pdt[pb];
         const float h = (float)dts;
         dts2 = make_float2(h, (float)(dts - (double)h));
       }
+    } else {
+      gamma = (R)prm.pgamma[pb];
+      cov = (R)prm.pcov[pb];
+      if (ep.pdt) dts = ep.pdt[pb];
     }
   }
   if (live) {
@@ -829,8 +836,13 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
   if (prm.prob) {
     const int pb = prm.act_cum ? pmap : prm.prob[e];
     if (!prm.pactive[pb]) return;
-    gamma = (R)prm.pgamma[pb];
-    cov = (R)prm.pcov[pb];
+    if constexpr (F32) {
+      gamma = prm.pgamma32 ? prm.pgamma32[pb] : (R)prm.pgamma[pb];
+      cov = prm.pcov32 ? prm.pcov32[pb] : (R)prm.pcov[pb];
+    } else {
+      gamma = (R)prm.pgamma[pb];
+      cov = (R)prm.pcov[pb];
+    }
   }
   R el[NEQ][ND];
   float lo[DS ? NEQ : 1][DS ? ND : 1];
@@ -855,8 +867,12 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
       uml[k] = (float)(m - (double)umh[k]);
     }
   }
-  double minValue;
-  double elind[NEQ];
+  // the indicator's results: FP64, or FP32 for a float state (they only
+  // scale the FP32 multiplier and feed FinDiff's 0.999 test, where no float
+  // lies between 0.999 and its FP32 rounding)
+  using IndT = typename std::conditional<F32, float, double>::type;
+  IndT minValue;
+  IndT elind[NEQ];
   if (prm.indicator == 0) {
     minValue = 1.0;
 #pragma unroll
@@ -869,7 +885,7 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
     R sv[NEQ];
     shu_indicator<G, P, DS>(prm, u, ulo, e, sv);
 #pragma unroll
-    for (int k = 0; k < NEQ; ++k) elind[k] = (double)sv[k];
+    for (int k = 0; k < NEQ; ++k) elind[k] = (IndT)sv[k];
     minValue = 1.0;  // FinDiff only: the Multi limiter is rejected with Shu
   } else {
     // stencil min / max of the means, started from the element's own mean
@@ -877,7 +893,8 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
     // lexicographically (a normalised pair orders as its value)
     using MeanT = typename std::conditional<F32, float2, double>::type;
     MeanT mI[NEQ], MI[NEQ];
-    double yMin[NEQ], umd[NEQ];
+    IndT yMin[NEQ];
+    double umd[NEQ];
 #pragma unroll
     for (int k = 0; k < NEQ; ++k) {
       if constexpr (F32) {
@@ -972,7 +989,7 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
         }
       }
 #pragma unroll
-      for (int k = 0; k < NEQ; ++k) yMin[k] = (double)yMf[k];
+      for (int k = 0; k < NEQ; ++k) yMin[k] = yMf[k];
     } else {
       for (int lf = 0; lf < NFPE; ++lf) {
         const int nb = prm.fnbr[lf * ne + e];
@@ -1091,7 +1108,7 @@ __global__ void __launch_bounds__(kGenericMaxBlock)
       }
     }
   } else {
-    const bool totalInd = elind[NEQ - 1] < 0.999;
+    const bool totalInd = elind[NEQ - 1] < IndT(0.999);
     if (totalInd) {
 #pragma unroll
       for (int k = 0; k < NEQ; ++k)

@@ -117,6 +117,9 @@ struct rkdg_ctx {
   int* d_prob = nullptr;
   double* d_pgamma = nullptr;
   double* d_pcov = nullptr;
+  float* d_pgamma32 = nullptr;  // FP32 copies for the FP32 kernels
+  float* d_pcov32 = nullptr;
+  float2* d_pdt2 = nullptr;     // dt_real as float pairs
   double* d_phmin = nullptr;
   double* d_pdt = nullptr;
   double* d_pdtr = nullptr;
@@ -191,6 +194,9 @@ void free_mesh(rkdg_ctx* c) {
   dfree(c->d_prob);
   dfree(c->d_pgamma);
   dfree(c->d_pcov);
+  dfree(c->d_pgamma32);
+  dfree(c->d_pcov32);
+  dfree(c->d_pdt2);
   dfree(c->d_phmin);
   dfree(c->d_pdt);
   dfree(c->d_pdtr);
@@ -404,6 +410,8 @@ void set_batch(rkdg_ctx* c, RhsParams& P, int slot) {
   P.prob = c->d_prob;
   P.pgamma = c->d_pgamma;
   P.pcov = c->d_pcov;
+  P.pgamma32 = c->d_pgamma32;
+  P.pcov32 = c->d_pcov32;
   P.pactive = c->d_pactive;
   P.act_cum = c->d_act_cum;
   P.act_pid = c->d_act_pid;
@@ -527,6 +535,8 @@ LimParams lim_params_for(rkdg_ctx* c, bool batch) {
     L.prob = c->d_prob;
     L.pgamma = c->d_pgamma;
     L.pcov = c->d_pcov;
+    L.pgamma32 = c->d_pgamma32;
+    L.pcov32 = c->d_pcov32;
     L.pactive = c->d_pactive;
     L.act_cum = c->d_act_cum;
     L.act_pid = c->d_act_pid;
@@ -640,6 +650,7 @@ int enqueue_step32(rkdg_ctx* c, double dt, bool batch = false) {
     if (batch) {
       ep.prob = c->d_prob;
       ep.pdt = c->d_pdtr;
+      ep.pdt2 = c->d_pdt2;
     }
     if (i < s - 1) {
       const int row = (i + 1) * i / 2;
@@ -1582,6 +1593,9 @@ int rkdg_batch_setup(rkdg_ctx* c, int nprob, const int* elem_offsets, const doub
   CUDA_TRY(c, dalloc(c->d_prob, (size_t)c->ne));
   CUDA_TRY(c, dalloc(c->d_pgamma, (size_t)nprob));
   CUDA_TRY(c, dalloc(c->d_pcov, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_pgamma32, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_pcov32, (size_t)nprob));
+  CUDA_TRY(c, dalloc(c->d_pdt2, (size_t)nprob));
   CUDA_TRY(c, dalloc(c->d_phmin, (size_t)nprob));
   CUDA_TRY(c, dalloc(c->d_pdt, (size_t)nprob));
   CUDA_TRY(c, dalloc(c->d_pdtr, (size_t)nprob));
@@ -1600,6 +1614,11 @@ int rkdg_batch_setup(rkdg_ctx* c, int nprob, const int* elem_offsets, const doub
   CUDA_TRY(c, cudaMemcpy(c->d_prob, prob.data(), prob.size() * sizeof(int), cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy(c->d_pgamma, gamma, nprob * sizeof(double), cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy(c->d_pcov, covolume, nprob * sizeof(double), cudaMemcpyHostToDevice));
+  {
+    std::vector<float> g32(gamma, gamma + nprob), c32(covolume, covolume + nprob);
+    CUDA_TRY(c, cudaMemcpy(c->d_pgamma32, g32.data(), nprob * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_pcov32, c32.data(), nprob * sizeof(float), cudaMemcpyHostToDevice));
+  }
   CUDA_TRY(c, cudaMemcpy(c->d_phmin, phmin.data(), nprob * sizeof(double), cudaMemcpyHostToDevice));
   return RKDG_OK;
 }
@@ -1627,6 +1646,7 @@ int rkdg_batch_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0,
   bs.hmin = c->d_phmin;
   bs.dt = c->d_pdt;
   bs.dtr = c->d_pdtr;
+  bs.dtr2 = c->d_pdt2;
   bs.t = c->d_pt;
   bs.sum_dt = c->d_psum;
   bs.active = c->d_pactive;

@@ -216,6 +216,14 @@ __device__ void build_active_map(const BatchState& bs) {
 
 __global__ void k_batch_map(BatchState bs) { build_active_map(bs); }
 
+// dt_real of problem p as a float pair for the FP32 stage kernels
+__device__ __forceinline__ void store_dtr2(const BatchState& bs, int p) {
+  if (!bs.dtr2) return;
+  const double d = bs.dtr[p];
+  const float h = (float)d;
+  bs.dtr2[p] = make_float2(h, (float)(d - (double)h));
+}
+
 __global__ void k_batch_init(BatchState bs, double dt0) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < bs.nprob; p += gridDim.x * blockDim.x) {
     double dt = dt0;
@@ -227,6 +235,7 @@ __global__ void k_batch_init(BatchState bs, double dt0) {
     const bool ok = isfinite(dt) && dt > 0.0;
     bs.active[p] = ok ? 1 : 0;
     bs.dtr[p] = fmin(dt, bs.t_end);
+    store_dtr2(bs, p);
   }
 }
 
@@ -258,6 +267,7 @@ __global__ void k_batch_control(BatchState bs, cudaGraphConditionalHandle handle
       bs.active[p] = 0;
     } else {
       bs.dtr[p] = fmin(dt, bs.t_end - t);
+      store_dtr2(bs, p);
       ++local;
     }
   }
