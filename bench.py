@@ -378,6 +378,20 @@ def run_ours(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def one_thread_rate(fn, units, sample, threads):
+    """The oracle on one host thread (the reference's one-rank behaviour):
+    units / seconds of fn(), then the thread count is restored."""
+    from oracle import refcpu
+    refcpu.set_threads(1)
+    try:
+        t0 = time.perf_counter()
+        fn()
+        sec = time.perf_counter() - t0
+    finally:
+        refcpu.set_threads(threads)
+    return {"value": units / sec, "cores": 1, "sample": f"{sample} ({sec:.1f} s)"}
+
+
 def run_config(args, local):
     """The other configurations of the workload set, one JSON line each (the
     headline line is the C2 pulse of run_ours):
@@ -472,6 +486,10 @@ def run_config(args, local):
         sec = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": orc.n * STAGES * ksteps / sec, "cores": threads,
                                 "kind": "port", "sample": f"{ksteps} RK steps, FP64 oracle"}
+        k1 = 100 if w == "c1" else 1
+        line["cpu_baseline"]["one_thread"] = one_thread_rate(
+            lambda: orc.run(xo, case.t_end, case.cfl, max_steps=k1), orc.n * STAGES * k1,
+            f"{k1} RK step(s), FP64 oracle", threads)
     elif w == "c4":
         bc = cases.batched_riemann()
         for name, prec in (("fp64", FP64), ("fp32_bulk", FP32_BULK)):
@@ -558,6 +576,10 @@ def run_config(args, local):
                                     "kind": "port",
                                     "sample": f"the smallest problem ({np.diff(bc.offsets)[small]} "
                                               "elements) run alone, FP64 oracle"}
+            x_small = cases.project(c, orc.node_coords())
+            line["cpu_baseline"]["one_thread"] = one_thread_rate(
+                lambda: orc.run(x_small, c.t_end, c.cfl, max_steps=200), orc.n * STAGES * 200,
+                "200 RK steps of the smallest problem, FP64 oracle", threads)
         except refcpu.OracleError as ex:
             line["cpu_baseline"] = {"unavailable": str(ex)[:80]}
     elif w == "c6":
@@ -623,6 +645,9 @@ def run_config(args, local):
         sec = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": orc.n * STAGES * 2 / sec, "cores": threads,
                                 "kind": "port", "sample": "2 RK steps, FP64 oracle"}
+        line["cpu_baseline"]["one_thread"] = one_thread_rate(
+            lambda: orc.run(xo, 1e30, dt0=dt, dt_mode=2, max_steps=1, limit_initial=False),
+            orc.n * STAGES, "1 RK step, FP64 oracle", threads)
     print(json.dumps(line), flush=True)
 
 
