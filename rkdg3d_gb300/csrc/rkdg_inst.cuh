@@ -2,6 +2,8 @@
 // unit per geometry keeps the build parallel).
 #pragma once
 
+#include <algorithm>
+
 #include "rkdg_generic.cuh"
 #include "rkdg_launch.h"
 
@@ -18,7 +20,9 @@ inline int generic_block(int b) {
 template <int G, int P>
 cudaError_t launch_rhs_t(int prec, const RhsParams& prm, const void* u, const void* ep,
                          cudaStream_t st) {
-  const int blk = generic_block(prm.block);
+  constexpr int NVAL = El<G, P>::NEQ * El<G, P>::ND;
+  const int blk = prec == 0 ? generic_block(prm.block)
+                            : std::min(generic_block(prm.block), generic_max_block<float, NVAL>());
   const int grid = (prm.ne + blk - 1) / blk;
   if (prec == 0)
     k_rhs_generic<G, P, double><<<grid, blk, 0, st>>>(prm, (const double*)u,
@@ -31,7 +35,9 @@ cudaError_t launch_rhs_t(int prec, const RhsParams& prm, const void* u, const vo
 
 template <int G, int P>
 cudaError_t launch_limit_t(int mode, const LimParams& prm, void* u, float* ulo, cudaStream_t st) {
-  const int blk = generic_block(prm.block);
+  constexpr int NVAL = El<G, P>::NEQ * El<G, P>::ND;
+  const int blk = mode == 0 ? generic_block(prm.block)
+                            : std::min(generic_block(prm.block), generic_max_block<float, NVAL>());
   const int grid = (prm.ne + blk - 1) / blk;
   if (mode == 0)
     k_limit_generic<G, P, double, false><<<grid, blk, 0, st>>>(prm, (double*)u, nullptr);
