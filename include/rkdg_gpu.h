@@ -217,6 +217,15 @@ int rkdg_step(rkdg_ctx* ctx, double* x_dev, double dt, double* next_mcs);
 int rkdg_run(rkdg_ctx* ctx, double* x_dev, double t_end, double cfl, double dt0,
              int dt_mode, int max_steps, int* steps_out, double* t_out,
              double* dt_out, double* sum_dt_out);
+/* The same time loop continued from time t0 with the next step's dt already
+ * known: no limit of the state and no initial dt (the reference's restart,
+ * main.cpp:461-490: t and dt from the restart frame), or the next chunk of a
+ * run split into pieces (t0 = *t_out and dt = *dt_out of the previous piece:
+ * the pieces together step exactly as one rkdg_run).  dt_mode 0 forms the
+ * following dts from CFL, 1 and 2 keep dt. */
+int rkdg_run_continue(rkdg_ctx* ctx, double* x_dev, double t0, double dt, double t_end,
+                      double cfl, int dt_mode, int max_steps, int* steps_out, double* t_out,
+                      double* dt_out, double* sum_dt_out);
 /* Discretely conserved totals sum_e sum_j (int phi_j) u_j per equation
  * (host output [neq]); the device form of check_total_energy.cpp:3-62. */
 int rkdg_totals(rkdg_ctx* ctx, const double* x_dev, double* totals_host);

@@ -42,6 +42,8 @@ _SIGS = [
     ("rkdg_step", C.c_int, [_vp, _vp, C.c_double, _dp]),
     ("rkdg_run", C.c_int, [_vp, _vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                            _ip, _dp, _dp, _dp]),
+    ("rkdg_run_continue", C.c_int, [_vp, _vp, C.c_double, C.c_double, C.c_double, C.c_double,
+                                    C.c_int, C.c_int, _ip, _dp, _dp, _dp]),
     ("rkdg_totals", C.c_int, [_vp, _vp, _dp]),
     ("rkdg_riemann_batch", C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     ("rkdg_batch_setup", C.c_int, [_vp, C.c_int, _ip, _dp, _dp]),

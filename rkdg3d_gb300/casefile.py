@@ -11,7 +11,16 @@ restates that set-up on top of the GPU context: ``load_case`` builds a
 with ``rkdg_run`` (the time loop of ``main.cpp:509-553``), ``write_vtu``
 writes cell means for ParaView.
 
-Not restated: restart and VisIt output, the adaptive refiner (``adaptive: 1``
+Restart frames follow the reference's cycle (``main.cpp:453-495, 735-775``,
+``CaseManager::loadMesh / loadInitialSolution / initializeRestartQueue /
+cleanPreviousRestartFrames``): a frame before the loop and every
+``postProcess.visSteps`` steps and at the end, named ``restart_<cycle>``, the
+``time.nSavedFrames`` newest kept; ``time.restart`` continues from frame
+``time.restartCycle`` with its mesh, state, time, cycle and time step.  The
+frame contents are this module's own files (a NumPy mesh and state, a JSON
+root) in place of MFEM's VisIt data collection, which needs MFEM.
+
+Not restated: VisIt output for viewing, the adaptive refiner (``adaptive: 1``
 is refused: its error estimator is MFEM's), parallel partitioning.  The
 settings parser reads the subset of YAML the reference's files use: block
 mappings by indentation, ``key: value`` scalars, ``[a, b, c]`` lists and
@@ -19,7 +28,10 @@ mappings by indentation, ``key: value`` scalars, ``[a, b, c]`` lists and
 """
 from __future__ import annotations
 
+import json
 import os
+import re
+import shutil
 from typing import Any
 
 import numpy as np
@@ -265,22 +277,163 @@ def load_case(case_dir: str, settings: dict | None = None) -> C.Case:
 
 # ---- running and output --------------------------------------------------------
 
+RESTART_FIELD = "restart_conservative_vars"
+_FRAME = re.compile(r"^restart_(\d{6,})$")
+
+
+def restart_name(cycle: int) -> str:
+    return f"restart_{cycle:06d}"
+
+
+def save_restart(out_dir: str, cycle: int, t: float, dt: float, mesh: M.Mesh, order: int,
+                 x) -> str:
+    """Write restart frame ``cycle`` (the reference's restart_dc.Save with
+    SetCycle / SetTime / SetTimeStep, main.cpp:757-760): the directory
+    ``restart_<cycle>`` with the mesh and the conservative state (MFEM byNODES
+    order) and the root ``restart_<cycle>.json`` with cycle, time and time
+    step.  Returns the frame's name."""
+    name = restart_name(cycle)
+    d = os.path.join(out_dir, name)
+    os.makedirs(d, exist_ok=True)
+    m = mesh.contiguous()
+    np.savez(os.path.join(d, "mesh.npz"), dim=m.dim, geom=m.geom, elem_vertices=m.elem_vertices,
+             elem_coords=m.elem_coords, bdr_vertices=m.bdr_vertices, bdr_attr=m.bdr_attr)
+    xs = x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x)
+    np.save(os.path.join(d, RESTART_FIELD + ".npy"), np.ascontiguousarray(xs, dtype=np.float64))
+    root = {"cycle": int(cycle), "time": float(t), "time_step": float(dt), "order": int(order),
+            "mesh": f"{name}/mesh.npz", "fields": {RESTART_FIELD: f"{name}/{RESTART_FIELD}.npy"}}
+    with open(os.path.join(out_dir, name + ".json"), "w") as fh:
+        json.dump(root, fh, indent=1)
+    return name
+
+
+def load_restart(out_dir: str, cycle: int) -> dict:
+    """Read restart frame ``cycle`` (restart_data_c.Load(restartCycle),
+    case_manager.cpp:237-260, 488-505): mesh, order, state, time, cycle and
+    time step.  A missing frame or field is a CaseError, as the reference
+    prints and exits."""
+    name = restart_name(cycle)
+    rp = os.path.join(out_dir, name + ".json")
+    if not os.path.isfile(rp):
+        raise CaseError(f"Error loading data collection: no restart frame {name} in {out_dir}")
+    with open(rp) as fh:
+        root = json.load(fh)
+    if RESTART_FIELD not in root.get("fields", {}):
+        raise CaseError(f"The given data collection has no '{RESTART_FIELD}' field.")
+    z = np.load(os.path.join(out_dir, root["mesh"]))
+    mesh = M.Mesh(int(z["dim"]), int(z["geom"]), z["elem_vertices"], z["elem_coords"],
+                  z["bdr_vertices"], z["bdr_attr"])
+    x = np.load(os.path.join(out_dir, root["fields"][RESTART_FIELD]))
+    return {"mesh": mesh, "order": int(root["order"]), "x": x, "time": float(root["time"]),
+            "cycle": int(root["cycle"]), "time_step": float(root["time_step"])}
+
+
+class RestartFrames:
+    """The reference's queue of saved frames (initializeRestartQueue and
+    cleanPreviousRestartFrames, case_manager.cpp:895-985): frames already in
+    the directory join the queue, those of a later cycle than the one a run
+    restarts from are removed; after each save the oldest frames beyond
+    ``n_saved`` are removed.  Only names of the form restart_<digits> (and
+    their roots) are touched."""
+
+    def __init__(self, out_dir: str, n_saved: int, restart_cycle: int | None = None):
+        self.out_dir, self.n_saved = out_dir, int(n_saved)
+        current = restart_name(restart_cycle if restart_cycle is not None else 0)
+        self.queue: list[str] = []
+        for entry in sorted(os.listdir(out_dir)):
+            if not (_FRAME.match(entry) and os.path.isdir(os.path.join(out_dir, entry))):
+                continue
+            if entry > current:
+                self._remove(entry)
+            else:
+                self.queue.append(entry)
+        if not self.queue:
+            self.queue.append(restart_name(0))
+
+    def _remove(self, name: str) -> None:
+        shutil.rmtree(os.path.join(self.out_dir, name), ignore_errors=True)
+        root = os.path.join(self.out_dir, name + ".json")
+        if os.path.isfile(root):
+            os.remove(root)
+
+    def saved(self, cycle: int) -> None:
+        self.queue.append(restart_name(cycle))
+        self.queue.sort()
+        if len(self.queue) > self.n_saved:
+            self._remove(self.queue.pop(0))
+
+
 def run_case(case_dir: str, device: int = 0, precision: int = 0, max_steps: int = 0,
-             t_end: float | None = None, settings: dict | None = None):
-    """Project the initial field, run the case to tEnd (or t_end / max_steps)
-    on the GPU with the reference's time bookkeeping; returns (case, context,
-    final state as a CUDA tensor, run info)."""
+             t_end: float | None = None, settings: dict | None = None,
+             out_dir: str | None = None, restart_frames: bool = False):
+    """Run a case directory on the GPU with the reference's time bookkeeping;
+    returns (case, context, final state as a CUDA tensor, run info).
+
+    The initial state is the projected initial field, limited (main.cpp:
+    264-265), or with ``time.restart`` set the state of restart frame
+    ``time.restartCycle`` in ``out_dir`` (default: the case directory), also
+    limited, continuing from that frame's time, cycle and time step.  With
+    ``restart_frames`` (or a restart) frames are written as the reference
+    writes them: one before the loop (cycle 0 and time 0, also when the run
+    restarts), every ``postProcess.visSteps`` steps and at the end, keeping
+    the ``time.nSavedFrames`` newest.  The run stops at tEnd (or t_end, or
+    after max_steps steps)."""
     import torch
 
     from .solver import Context
-    case = load_case(case_dir, settings)
+    s = settings if settings is not None else read_settings(os.path.join(case_dir, "settings.yml"))
+    case = load_case(case_dir, s)
+    out_dir = case_dir if out_dir is None else out_dir
+    tm = s.get("time", {})
+    restart = bool(tm.get("restart", False))
+    write = restart_frames or restart
+    vis_steps = max(1, int((s.get("postProcess") or {}).get("visSteps", 1)))
+    t_stop = case.t_end if t_end is None else t_end
+    t0, ti, dt = 0.0, 0, None
+    if restart:
+        fr = load_restart(out_dir, int(tm.get("restartCycle", 0)))
+        if fr["order"] != case.order:
+            raise CaseError("the restart frame's polynomial order differs from the settings'")
+        case.mesh = fr["mesh"]
+        t0, ti, dt = fr["time"], fr["cycle"], fr["time_step"]
     ctx = Context(case.mesh, case.order, device=device, precision=precision)
     C.configure_context(case, ctx)
-    x = torch.tensor(C.project(case, ctx.node_coords()), dtype=torch.float64,
-                     device=f"cuda:{device}")
-    info = ctx.run(x, case.t_end if t_end is None else t_end, cfl=case.cfl, dt0=case.dt0,
-                   dt_mode=case.dt_mode, max_steps=max_steps)
-    return case, ctx, x, info
+    if restart:
+        x = torch.tensor(fr["x"], dtype=torch.float64, device=f"cuda:{device}")
+        if x.numel() != ctx.n:
+            raise CaseError("the restart frame's state does not match its mesh")
+    else:
+        x = torch.tensor(C.project(case, ctx.node_coords()), dtype=torch.float64,
+                         device=f"cuda:{device}")
+    if not write:
+        info = ctx.run(x, t_stop, cfl=case.cfl, dt0=case.dt0, dt_mode=case.dt_mode,
+                       max_steps=max_steps)
+        return case, ctx, x, info
+    frames = RestartFrames(out_dir, int(tm.get("nSavedFrames", 0)),
+                           ti if restart else None)
+    ctx.limit(x)  # l->update(sol) after loadInitialSolution (main.cpp:264-265)
+    if dt is None:  # the initial dt of main.cpp:467-484 (as rkdg_run forms it)
+        dt = case.dt0 if case.dt_mode == 2 else \
+            case.cfl * ctx.hmin() / ctx.face_speed(x) / (2 * case.order + 1)
+    save_restart(out_dir, 0, 0.0, dt, case.mesh, case.order, x)  # main.cpp:492-495
+    t, steps, sum_dt, done = t0, 0, 0.0, False
+    while not done:
+        chunk = vis_steps - (ti % vis_steps)
+        if max_steps > 0:
+            chunk = min(chunk, max_steps - steps)
+        info = ctx.run_continue(x, t, dt, t_stop, cfl=case.cfl, dt_mode=case.dt_mode,
+                                max_steps=chunk)
+        t, dt = info["t"], info["dt"]
+        ti += info["steps"]
+        steps += info["steps"]
+        sum_dt += info["sum_dt"]
+        done = t >= t_stop - 1e-8 * dt
+        if done or ti % vis_steps == 0:
+            save_restart(out_dir, ti, t, dt, case.mesh, case.order, x)
+            frames.saved(ti)
+        if max_steps > 0 and steps >= max_steps:
+            break
+    return case, ctx, x, {"steps": steps, "t": t, "dt": dt, "sum_dt": sum_dt, "cycle": ti}
 
 
 _VTK_CELL = {M.GEOM_TRIANGLE: 5, M.GEOM_SQUARE: 9, M.GEOM_CUBE: 12}

@@ -715,6 +715,56 @@ int read_mcs(rkdg_ctx* c, int slot, double* out) {
   return RKDG_OK;
 }
 
+// The time loop of main.cpp:509-553,701-733 from time t with the step's
+// dt known: dt_real = min(dt, t_end - t), one step, the next dt from the
+// last stage's speed (dt_mode 0), t += that dt (the reference books t with
+// the new dt), done when t >= t_end - 1e-8 dt.
+int run_loop(rkdg_ctx* c, double* x, double t, double dt, double t_end, double cfl, int dt_mode,
+             int max_steps, int* steps_out, double* t_out, double* dt_out, double* sum_dt_out) {
+  if (!(dt > 0)) return fail(c, RKDG_ERR_INVALID, "non-positive dt");
+  const long long n = c->ndofs * c->neq;
+  const double denom = 2.0 * c->p + 1.0;
+  const bool fp32 = c->precision != RKDG_FP64;
+  int st;
+  if (fp32) {
+    CUDA_TRY(c, rkdg::launch_split(n, x, c->d_xh, c->d_xl, c->stream));
+    c->launches++;
+  }
+  double sum_dt = 0.0;
+  int ti = 0;
+  bool done = false;
+  while (!done) {
+    const double dt_real = std::min(dt, t_end - t);
+    st = fp32 ? enqueue_step32(c, dt_real) : enqueue_step64(c, x, dt_real);
+    if (st) return st;
+    sum_dt += dt_real;
+    if (dt_mode == 0) {
+      double mcs = 0;
+      st = read_mcs(c, c->s - 1, &mcs);
+      if (st) return st;
+      dt = cfl * c->hmin / mcs / denom;
+      // The reference loops forever on a non-finite or vanishing dt; stop instead.
+      if (!std::isfinite(dt) || !(dt > 0.0) || (t_end < 1e20 && dt < 1e-14 * t_end))
+        return fail(c, RKDG_ERR_UNPHYSICAL, "non-finite or vanishing CFL time step", ti);
+    }
+    t += dt;
+    ti++;
+    done = (t >= t_end - 1e-8 * dt);
+    if (max_steps > 0 && ti >= max_steps) break;
+  }
+  if (fp32) {
+    CUDA_TRY(c, rkdg::launch_join(n, c->d_xh, c->d_xl, x, c->stream));
+    c->launches++;
+  }
+  st = read_mcs(c, c->s - 1, nullptr);
+  if (st) return st;
+  if (steps_out) *steps_out = ti;
+  if (t_out) *t_out = t;
+  if (dt_out) *dt_out = dt;
+  if (sum_dt_out) *sum_dt_out = sum_dt;
+  return RKDG_OK;
+}
+
 #define NEED_MESH(c)                                              \
   do {                                                            \
     if (!(c)) return RKDG_ERR_INVALID;                            \
@@ -1469,7 +1519,6 @@ int rkdg_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0, int d
   if (!x || dt_mode < 0 || dt_mode > 2) return fail(c, RKDG_ERR_INVALID, "invalid run arguments");
   int st = ensure_scratch(c);
   if (st) return st;
-  const long long n = c->ndofs * c->neq;
   // The reference limits the projected initial state once before it forms the
   // initial dt and enters the loop (main.cpp:264-265).
   if (!(c->solver_quirks & RKDG_QUIRK_NO_INITIAL_LIMIT)) {
@@ -1477,53 +1526,27 @@ int rkdg_run(rkdg_ctx* c, double* x, double t_end, double cfl, double dt0, int d
     if (st) return st;
   }
   double dt = dt0;
-  const double denom = 2.0 * c->p + 1.0;
   if (dt_mode != 2) {
     double mcs = 0;
     st = rkdg_face_speed(c, x, &mcs);
     if (st) return st;
     if (!(mcs > 0)) return fail(c, RKDG_ERR_INVALID, "zero wave speed: cannot form a CFL dt");
-    dt = cfl * c->hmin / mcs / denom;
+    dt = cfl * c->hmin / mcs / (2.0 * c->p + 1.0);
   }
-  if (!(dt > 0)) return fail(c, RKDG_ERR_INVALID, "non-positive dt");
-  const bool fp32 = c->precision != RKDG_FP64;
-  if (fp32) {
-    CUDA_TRY(c, rkdg::launch_split(n, x, c->d_xh, c->d_xl, c->stream));
-    c->launches++;
-  }
-  double t = 0.0, sum_dt = 0.0;
-  int ti = 0;
-  bool done = false;
-  while (!done) {
-    const double dt_real = std::min(dt, t_end - t);
-    st = fp32 ? enqueue_step32(c, dt_real) : enqueue_step64(c, x, dt_real);
-    if (st) return st;
-    sum_dt += dt_real;
-    if (dt_mode == 0) {
-      double mcs = 0;
-      st = read_mcs(c, c->s - 1, &mcs);
-      if (st) return st;
-      dt = cfl * c->hmin / mcs / denom;
-      // The reference loops forever on a non-finite or vanishing dt; stop instead.
-      if (!std::isfinite(dt) || !(dt > 0.0) || (t_end < 1e20 && dt < 1e-14 * t_end))
-        return fail(c, RKDG_ERR_UNPHYSICAL, "non-finite or vanishing CFL time step", ti);
-    }
-    t += dt;
-    ti++;
-    done = (t >= t_end - 1e-8 * dt);
-    if (max_steps > 0 && ti >= max_steps) break;
-  }
-  if (fp32) {
-    CUDA_TRY(c, rkdg::launch_join(n, c->d_xh, c->d_xl, x, c->stream));
-    c->launches++;
-  }
-  st = read_mcs(c, c->s - 1, nullptr);
+  return run_loop(c, x, 0.0, dt, t_end, cfl, dt_mode, max_steps, steps_out, t_out, dt_out,
+                  sum_dt_out);
+}
+
+int rkdg_run_continue(rkdg_ctx* c, double* x, double t0, double dt, double t_end, double cfl,
+                      int dt_mode, int max_steps, int* steps_out, double* t_out, double* dt_out,
+                      double* sum_dt_out) {
+  NEED_MESH(c);
+  if (!x || dt_mode < 0 || dt_mode > 2 || !std::isfinite(t0))
+    return fail(c, RKDG_ERR_INVALID, "invalid run arguments");
+  int st = ensure_scratch(c);
   if (st) return st;
-  if (steps_out) *steps_out = ti;
-  if (t_out) *t_out = t;
-  if (dt_out) *dt_out = dt;
-  if (sum_dt_out) *sum_dt_out = sum_dt;
-  return RKDG_OK;
+  return run_loop(c, x, t0, dt, t_end, cfl, dt_mode, max_steps, steps_out, t_out, dt_out,
+                  sum_dt_out);
 }
 
 int rkdg_totals(rkdg_ctx* c, const double* x, double* totals) {

@@ -290,6 +290,21 @@ class Context:
                                    C.byref(steps), C.byref(t), C.byref(dt), C.byref(sdt)))
         return {"steps": steps.value, "t": t.value, "dt": dt.value, "sum_dt": sdt.value}
 
+    def run_continue(self, x, t0: float, dt: float, t_end: float, cfl: float = 0.3,
+                     dt_mode: int = 0, max_steps: int = 0) -> dict:
+        """The time loop continued at time t0 with the next dt known
+        (rkdg_run_continue): a restart frame's t and dt, or the t and dt that
+        the previous piece of a run returned."""
+        if max_steps <= 0 and not (t_end < 1e20):
+            raise ValueError("run_continue() needs a finite t_end or max_steps > 0")
+        steps = C.c_int()
+        t = C.c_double()
+        dto = C.c_double()
+        sdt = C.c_double()
+        self._chk(self._L.rkdg_run_continue(self.h, _ptr(x), t0, dt, t_end, cfl, dt_mode, max_steps,
+                                            C.byref(steps), C.byref(t), C.byref(dto), C.byref(sdt)))
+        return {"steps": steps.value, "t": t.value, "dt": dto.value, "sum_dt": sdt.value}
+
     def totals(self, x) -> np.ndarray:
         out = np.zeros(self.neq)
         self._chk(self._L.rkdg_totals(self.h, _ptr(x), out.ctypes.data_as(_capi._dp)))

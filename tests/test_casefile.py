@@ -218,3 +218,49 @@ def test_reference_settings_parse():
             assert {"mesh", "physics", "internalField", "spatial", "time"} <= set(s)
             n += 1
     assert n > 10
+
+
+def test_restart_frame_round_trip(tube, tmp_path):
+    """A restart frame keeps mesh, order, state, time, cycle and time step
+    exactly; a missing frame is refused as the reference refuses it."""
+    case = CF.load_case(tube)
+    x = np.random.default_rng(3).normal(size=4 * 4 * case.mesh.num_elements)
+    out = tmp_path / "frames"
+    out.mkdir()
+    name = CF.save_restart(str(out), 40, 0.0123, 4.5e-4, case.mesh, case.order, x)
+    assert name == "restart_000040"
+    assert (out / "restart_000040" / "mesh.npz").exists() and (out / "restart_000040.json").exists()
+    fr = CF.load_restart(str(out), 40)
+    assert fr["cycle"] == 40 and fr["time"] == 0.0123 and fr["time_step"] == 4.5e-4
+    assert fr["order"] == case.order and np.array_equal(fr["x"], x)
+    m = fr["mesh"]
+    assert m.dim == case.mesh.dim and m.geom == case.mesh.geom
+    for f in ("elem_vertices", "elem_coords", "bdr_vertices", "bdr_attr"):
+        assert np.array_equal(getattr(m, f), getattr(case.mesh, f))
+    with pytest.raises(CF.CaseError, match="Error loading data collection"):
+        CF.load_restart(str(out), 41)
+
+
+def test_restart_frame_queue(tube, tmp_path):
+    """initializeRestartQueue / cleanPreviousRestartFrames: frames later than
+    the restarted cycle are removed at start, then the n newest are kept;
+    other files are left alone."""
+    case = CF.load_case(tube)
+    x = np.zeros(4 * 4 * case.mesh.num_elements)
+    out = str(tmp_path)
+    for c in (0, 10, 20, 30):
+        CF.save_restart(out, c, 0.1 * c, 1e-3, case.mesh, case.order, x)
+    fq = CF.RestartFrames(out, 2, restart_cycle=20)
+    assert fq.queue == ["restart_000000", "restart_000010", "restart_000020"]
+    assert not os.path.exists(os.path.join(out, "restart_000030"))
+    assert not os.path.exists(os.path.join(out, "restart_000030.json"))
+    CF.save_restart(out, 25, 2.5, 1e-3, case.mesh, case.order, x)
+    fq.saved(25)
+    # one removal per save, the oldest (the reference pops once when the
+    # queue is longer than nSavedFrames)
+    assert fq.queue == ["restart_000010", "restart_000020", "restart_000025"]
+    assert not os.path.exists(os.path.join(out, "restart_000000"))
+    assert os.path.exists(os.path.join(tube, "settings.yml")) and os.path.exists(
+        os.path.join(tube, "tube.msh"))
+    names = sorted(e for e in os.listdir(out) if e.startswith("restart_") and not e.endswith(".json"))
+    assert names == fq.queue
