@@ -296,7 +296,8 @@ long long rkdg_kernel_launches(rkdg_ctx* ctx);
  * call before any stream capture; the address stays cached for the life of
  * the process, so a device reset (cudaDeviceReset) ends the use of this entry
  * point in that process.  The call returns once the limiter has finished on
- * the context's stream.  The array is shared by every context on a device:
+ * the context's stream (it synchronises that stream, so it is never called
+ * while the stream is being captured into a graph).  The array is shared by every context on a device:
  * calls that overlap in time on one device (other host threads, other
  * streams) race on it and must be serialised by the caller. */
 #define RKDG_LIMIT_STATIC_MAX_VALUES (1u << 21)
