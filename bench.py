@@ -563,6 +563,25 @@ def run_config(args, local):
             "fp32_bulk_vs_fp64": errors(matched["fp32_bulk"][0][sel], matched["fp64"][0][sel], nk),
             "fp64_perturbed_1e-7_vs_fp64": errors(matched["fp64_perturbed_1e-7"][0][sel],
                                                   matched["fp64"][0][sel], nk)}
+
+        # the same differences problem by problem (density rows: 4 nodes per
+        # Q1 quad), as quantiles over the problems
+        def per_problem(a, b):
+            out = []
+            for p_ in range(len(bc.offsets) - 1):
+                if not okm[p_]:
+                    continue
+                lo, hi = 4 * bc.offsets[p_], 4 * bc.offsets[p_ + 1]
+                ref = np.abs(b[lo:hi]).sum()
+                out.append(float(np.abs(a[lo:hi] - b[lo:hi]).sum() / max(ref, 1e-300)))
+            q = np.asarray(out)
+            return {"median": float(np.median(q)), "p90": float(np.quantile(q, 0.9)),
+                    "max": float(q.max()), "problems_le_1e-6": int((q <= 1e-6).sum()),
+                    "problems_le_1e-4": int((q <= 1e-4).sum()), "problems": int(q.size)}
+        line["matched_steps"]["rho_rel_l1_per_problem"] = {
+            "fp32_bulk_vs_fp64": per_problem(matched["fp32_bulk"][0], matched["fp64"][0]),
+            "fp64_perturbed_1e-7_vs_fp64": per_problem(matched["fp64_perturbed_1e-7"][0],
+                                                       matched["fp64"][0])}
         small = int(np.argmin(np.diff(bc.offsets)))
         c = bc.cases[small]
         orc = refcpu.Oracle(c.mesh, c.order)
