@@ -458,6 +458,25 @@ def run_config(args, local):
             n, nd = ctx.n, ctx.ndofs
         line["unknowns"] = n
         line["error_fp32_bulk_vs_fp64"] = errors(out["fp32_bulk"][0], out["fp64"][0], nd)
+        if w == "c1":
+            # the same run as a batch of one problem: the whole time loop in one
+            # CUDA-graph launch (device-side dt and stopping test), without the
+            # host round trip per step of rkdg_run
+            ctx = context(case, FP32_BULK)
+            ctx.batch_setup(np.array([0, case.mesh.num_elements], np.int32),
+                            np.array([case.gamma]), np.array([case.covolume]))
+            x0 = torch.tensor(cases.project(case, ctx.node_coords()), dtype=torch.float64, device=dev)
+            x = x0.clone()
+            ctx.batch_run(x, case.t_end, case.cfl, max_steps=2)  # warm-up (graph build)
+            x = x0.clone()
+            binfo, sec = timed(lambda: ctx.batch_run(x, case.t_end, case.cfl))
+            bsteps = int(np.asarray(binfo["steps"])[0])
+            line["fp32_bulk_one_graph_launch"] = {
+                "value": ctx.n * STAGES * bsteps / sec, "steps": bsteps,
+                "ms_per_step": 1e3 * sec / max(bsteps, 1),
+                "rho_rel_l1_vs_fp32_bulk_host_loop": float(
+                    np.abs(x.cpu().numpy()[:nd] - out["fp32_bulk"][0][:nd]).sum()
+                    / np.abs(out["fp32_bulk"][0][:nd]).sum())}
         # at matched step counts: dt fixed from the FP64 CFL evaluation of the
         # initial state, the same in both arms; and the FP64 path's own spread
         # when its initial state is perturbed by 1e-7 (FP32 rounding) relative
