@@ -2092,7 +2092,10 @@ int rkdg_autotune(rkdg_ctx* c, const double* x, int* hex_kernel, int* generic_bl
   } else {
     int best = 0;
     float tbest = 0.0f;
-    for (int b = 64; b <= 256; b *= 2) {
+    // the FP32 kernels of small elements (Q1 quads, P1 triangles) run at most
+    // 128 threads per CTA (their launch bounds)
+    const int bmax = (c->precision != RKDG_FP64 && c->neq * c->nd <= 16) ? 128 : 256;
+    for (int b = 64; b <= bmax; b *= 2) {
       c->gen_block = b;
       float ms = 0.0f;
       if ((st = time_rhs(&ms))) return st;
@@ -2107,7 +2110,8 @@ int rkdg_autotune(rkdg_ctx* c, const double* x, int* hex_kernel, int* generic_bl
     c->launches++;
     int best = 0;
     float tbest = 0.0f;
-    for (int b = 64; b <= 256; b *= 2) {
+    const int bmax = (c->precision != RKDG_FP64 && c->neq * c->nd <= 16) ? 128 : 256;
+    for (int b = 64; b <= bmax; b *= 2) {
       c->lim_block = b;
       const LimParams L = lim_params(c);
       for (int r = 0; r < kWarm + kReps; ++r) {

@@ -76,3 +76,22 @@ def test_mixed_conservation_periodic(cuda):
         ctx.step(x, 2e-3)
     t1 = ctx.totals(x)
     assert np.all(np.abs(t1 - t0) <= 1e-9 * np.abs(t0).max())
+
+
+def test_mixed_autotune_small_elements(cuda):
+    """FP32-bulk Q1 quadrilaterals: the autotuner keeps the CTA sizes within
+    the 128 threads the FP32 kernels of small elements are built for, and the
+    right-hand side stays within the FP32-bulk bound of FP64."""
+    from tests.helpers import walled_case
+    from rkdg3d_gb300.solver import BC_SLIP, FUN_MICHALAK, IND_BJ, LIM_MULTI, RS_HLLC as HLLC
+    case = walled_case(M.GEOM_SQUARE, 12, 1, HLLC, bc=BC_SLIP)
+    case.limiter = (LIM_MULTI, IND_BJ, FUN_MICHALAK, 1, 0)
+    c64, c32 = make(case, FP64), make(case, FP32_BULK)
+    x = torch.tensor(random_state(c64.node_coords(), seed=2, amp=0.05, vel=0.1), device="cuda",
+                     dtype=torch.float64)
+    choice = c32.autotune(x)
+    assert choice["generic_block"] in (64, 128) and choice["limiter_block"] in (64, 128)
+    y64, y32 = torch.empty_like(x), torch.empty_like(x)
+    c64.rhs(x, y64)
+    c32.rhs(x, y32)
+    assert rel_l1(y32.cpu().numpy(), y64.cpu().numpy()) < 1e-5
