@@ -1773,23 +1773,13 @@ int ref_step(ref_ctx* c, double* x, double dt, double* next_mcs) {
   return REF_OK;
 }
 
-int ref_run(ref_ctx* c, double* x, double t_end, double cfl, double dt0, int dt_mode,
-            int max_steps, int* steps_out, double* t_out, double* dt_out, double* sum_dt_out) {
-  // The projected initial state is limited once before the initial dt and the
-  // loop (main.cpp:264-265, `l->update(sol)` after loadInitialSolution).
-  if (!(c->solver_quirks & 2)) {
-    int st = ref_limit(c, x);
-    if (st) return st;
-  }
-  const double hmin = (dt_mode == 2) ? 0.0 : ref_hmin(c);
-  double dt = dt0;
-  if (dt_mode != 2) {
-    double mcs;
-    int st = ref_face_speed(c, x, &mcs);
-    if (st) return st;
-    dt = cfl * hmin / mcs / (2 * c->p + 1);
-  }
-  double t = 0.0, sum_dt = 0.0;
+// The time loop of main.cpp:509-553,701-733 from time t with the next dt
+// known (ref_run after its initial limit and dt; ref_run_continue).
+static int run_loop(ref_ctx* c, double* x, double t, double dt, double t_end, double cfl,
+                    int dt_mode, int max_steps, int* steps_out, double* t_out, double* dt_out,
+                    double* sum_dt_out) {
+  const double hmin = (dt_mode == 0) ? ref_hmin(c) : 0.0;
+  double sum_dt = 0.0;
   int ti = 0;
   bool done = false;
   while (!done) {
@@ -1813,6 +1803,39 @@ int ref_run(ref_ctx* c, double* x, double t_end, double cfl, double dt0, int dt_
   if (dt_out) *dt_out = dt;
   if (sum_dt_out) *sum_dt_out = sum_dt;
   return REF_OK;
+}
+
+int ref_run(ref_ctx* c, double* x, double t_end, double cfl, double dt0, int dt_mode,
+            int max_steps, int* steps_out, double* t_out, double* dt_out, double* sum_dt_out) {
+  // The projected initial state is limited once before the initial dt and the
+  // loop (main.cpp:264-265, `l->update(sol)` after loadInitialSolution).
+  if (!(c->solver_quirks & 2)) {
+    int st = ref_limit(c, x);
+    if (st) return st;
+  }
+  double dt = dt0;
+  if (dt_mode != 2) {
+    double mcs;
+    int st = ref_face_speed(c, x, &mcs);
+    if (st) return st;
+    dt = cfl * ref_hmin(c) / mcs / (2 * c->p + 1);
+  }
+  return run_loop(c, x, 0.0, dt, t_end, cfl, dt_mode, max_steps, steps_out, t_out, dt_out,
+                  sum_dt_out);
+}
+
+// The loop continued at time t0 with the next dt known: the reference's
+// restart (main.cpp:461-490, t and dt from the restart frame), without the
+// initial limit and the initial dt.
+int ref_run_continue(ref_ctx* c, double* x, double t0, double dt, double t_end, double cfl,
+                     int dt_mode, int max_steps, int* steps_out, double* t_out, double* dt_out,
+                     double* sum_dt_out) {
+  if (!(dt > 0.0)) {
+    c->err = "non-positive dt";
+    return REF_ERR_INVALID;
+  }
+  return run_loop(c, x, t0, dt, t_end, cfl, dt_mode, max_steps, steps_out, t_out, dt_out,
+                  sum_dt_out);
 }
 
 // Discretely conserved totals: sum_e sum_j (int phi_j) u_j per equation.

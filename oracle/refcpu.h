@@ -108,6 +108,11 @@ int ref_step(ref_ctx* c, double* x, double dt, double* next_mcs);
 int ref_run(ref_ctx* c, double* x, double t_end, double cfl, double dt0,
             int dt_mode, int max_steps, int* steps_out, double* t_out,
             double* dt_out, double* sum_dt_out);
+/* The same loop continued at time t0 with the next dt known (no initial
+ * limit, no initial dt): the reference's restart, main.cpp:461-490. */
+int ref_run_continue(ref_ctx* c, double* x, double t0, double dt, double t_end, double cfl,
+                     int dt_mode, int max_steps, int* steps_out, double* t_out,
+                     double* dt_out, double* sum_dt_out);
 int ref_totals(ref_ctx* c, const double* x, double* totals); /* [neq] */
 double ref_total_energy(ref_ctx* c, const double* x); /* check_total_energy.cpp */
 /* pointwise Riemann solver on n states: u1,u2 [n][neq], nor [n][dim] (unit) */

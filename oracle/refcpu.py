@@ -60,6 +60,8 @@ def lib():
         L.ref_step.argtypes = [C.c_void_p, _dp, C.c_double, _dp]
         L.ref_run.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                               _ip, _dp, _dp, _dp]
+        L.ref_run_continue.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.c_int, C.c_int, _ip, _dp, _dp, _dp]
         L.ref_totals.argtypes = [C.c_void_p, _dp, _dp]
         L.ref_total_energy.restype = C.c_double
         L.ref_total_energy.argtypes = [C.c_void_p, _dp]
@@ -208,6 +210,18 @@ class Oracle:
         self._chk(lib().ref_run(self.h, _d(x), t_end, cfl, dt0, dt_mode, max_steps, C.byref(steps),
                                 C.byref(t), C.byref(dt), C.byref(sdt)))
         return x, {"steps": steps.value, "t": t.value, "dt": dt.value, "sum_dt": sdt.value}
+
+    def run_continue(self, x, t0, dt, t_end, cfl=0.3, dt_mode=0, max_steps=0):
+        """ref_run_continue: the loop from time t0 with the next dt known
+        (the reference's restart, main.cpp:461-490)."""
+        x = np.array(x, dtype=np.float64, copy=True)
+        steps = C.c_int()
+        t = C.c_double()
+        dto = C.c_double()
+        sdt = C.c_double()
+        self._chk(lib().ref_run_continue(self.h, _d(x), t0, dt, t_end, cfl, dt_mode, max_steps,
+                                         C.byref(steps), C.byref(t), C.byref(dto), C.byref(sdt)))
+        return x, {"steps": steps.value, "t": t.value, "dt": dto.value, "sum_dt": sdt.value}
 
     def totals(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)

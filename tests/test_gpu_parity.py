@@ -656,3 +656,4 @@ def test_bilinear_quads_refusals(cuda):
     ctx, _ = pair(_bilinear_case(1, True))
     with pytest.raises(RkdgError):
         ctx.set_limiter(LIM_FINDIFF, IND_SHU, FUN_MICHALAK, 1, 0)
+

@@ -5,7 +5,7 @@ import os
 import numpy as np
 import pytest
 
-from oracle.refcpu import Oracle
+from oracle.refcpu import Oracle, OracleError
 from rkdg3d_gb300 import cases
 from rkdg3d_gb300 import mesh as M
 from rkdg3d_gb300.solver import (AVG_EINFELDT, AVG_TRRS, BC_SLIP, FUN_MICHALAK, IND_BJ,
@@ -394,3 +394,23 @@ def test_bilinear_quads_free_stream_and_conservation(order):
     x = random_state(Xn, seed=6, amp=0.05, vel=0.1)
     y, _ = o.rhs(x)
     assert np.abs(o.totals(y)).max() < 1e-12 * np.abs(o.totals(x)).max()
+
+
+@pytest.mark.parametrize("dt_mode", [0, 1, 2])
+def test_run_in_pieces_equals_one_run(dt_mode):
+    """ref_run_continue with the t and dt a piece returned steps exactly as one
+    ref_run (the restart path of main.cpp:461-490 without the frame's limit)."""
+    from rkdg3d_gb300 import cases
+    case = cases.sod(nx=30, ny=2, t_end=0.05)
+    o = Oracle(case.mesh, case.order)
+    cases.configure_oracle(case, o)
+    x0 = cases.project(case, o.node_coords())
+    dt0 = 1e-3 if dt_mode == 2 else 0.0
+    x_all, i_all = o.run(x0, case.t_end, case.cfl, dt0=dt0, dt_mode=dt_mode)
+    x1, i1 = o.run(x0, case.t_end, case.cfl, dt0=dt0, dt_mode=dt_mode, max_steps=7)
+    x2, i2 = o.run_continue(x1, i1["t"], i1["dt"], case.t_end, case.cfl, dt_mode=dt_mode)
+    assert i1["steps"] + i2["steps"] == i_all["steps"]
+    assert np.array_equal(x2, x_all)
+    assert i2["t"] == i_all["t"] and i2["dt"] == i_all["dt"]
+    with pytest.raises(OracleError):
+        o.run_continue(x1, 0.0, 0.0, case.t_end, case.cfl)
